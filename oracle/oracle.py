@@ -1,0 +1,405 @@
+"""ORACLE — test infrastructure only.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import
+this module, and only as the checker; the product (``hfsolver_gb300``) never
+calls it.  It is a CPU restatement of hfsolver's molecular GTO path:
+
+* basis construction and normalisation   src/basis.f90:93-141, 275-488
+* S, T, V and the packed ERIs            src/qc.c:6-131 via oracle/tho.c (C)
+* Boys function                          src/special_functions.f90:189-248 via oracle/fm.c
+* RHF SCF (formP, formG, linear mixing)  src/scf.f90:12-136
+* nuclear repulsion, rhf_gauss           src/scf.f90:138-150, src/drivers.f90:12-51
+* AO->MO transform                       src/mbpt.f90:11-79
+* MBPT2 energy                           src/mbpt2.f90:8-31, src/mbpt.f90:154-159
+
+Parity is pinned against the reference's own known answers
+(src/tests/test_gaussians_molecules.f90, test_gaussians_atoms.f90, test_fm.f90,
+test_ijkl.f90, test_basis.f90) and, in the build container, against the
+reference's src/cints.c + src/qc.c compiled unmodified into oracle/_ref/.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+BASIS_HEADER = os.path.join(ROOT, "hfsolver_gb300", "csrc", "basis_631gss.h")
+
+PI = 3.1415926535897932384626433832795  # src/constants.f90:12
+ANG2BOHR = 1 / 0.529177249  # src/constants.f90:43-44
+
+# --------------------------------------------------------------------------
+# C part
+
+
+def _lib_path():
+    return os.path.join(HERE, "liboracle.so")
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = _lib_path()
+        if not os.path.exists(path):
+            from oracle.build import build_oracle
+
+            build_oracle()
+        _LIB = ctypes.CDLL(path)
+        _bind(_LIB)
+    return _LIB
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def _bind(L, prefix="oracle_"):
+    basis_args = [ctypes.c_int, _ip, _ip, _dp, _dp, _dp, _ip, _ip, _ip, ctypes.c_int, _dp, _dp]
+    for nm in ("getS", "getT", "getInts"):
+        f = getattr(L, prefix + nm)
+        f.argtypes = basis_args + [_dp]
+        f.restype = None
+    f = getattr(L, prefix + "getV")
+    f.argtypes = basis_args + [ctypes.c_int, _ip, _dp, _dp, _dp, _dp]
+    f.restype = None
+    if prefix == "oracle_":
+        L.oracle_boys.argtypes = [ctypes.c_int, ctypes.c_double, _dp]
+        L.oracle_boys.restype = ctypes.c_int
+        L.oracle_formG.argtypes = [ctypes.c_int, _dp, _dp, _dp]
+        L.oracle_formG.restype = None
+        L.oracle_eri_list.argtypes = [ctypes.c_int, _ip, _ip, _dp, _dp, _dp, _ip, _ip, _ip, _dp, _dp,
+                                      ctypes.c_int64, _ip, _dp]
+        L.oracle_eri_list.restype = None
+        L.oracle_ijkl.argtypes = [ctypes.c_int64] * 4
+        L.oracle_ijkl.restype = ctypes.c_int64
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+# --------------------------------------------------------------------------
+# Boys function
+
+
+def boys(maxm, t):
+    F = np.zeros(maxm + 1)
+    rc = lib().oracle_boys(int(maxm), float(t), _d(F))
+    if rc:
+        raise ValueError("Fm: invalid arguments")
+    return F
+
+
+# --------------------------------------------------------------------------
+# basis (src/basis.f90)
+
+
+def _parse_header(path=BASIS_HEADER):
+    txt = open(path).read()
+    out = {}
+    for name, body in re.findall(r"static const \w+ (\w+)\[\d+\] = \{([^}]*)\};", txt):
+        vals = body.split(",")
+        out[name] = [float(v) if ("." in v or "e" in v) else int(v) for v in vals]
+    return out
+
+
+_TABLE = None
+
+
+def read_basis(Z):
+    """Shells of atom Z: list of (L, alphas, coefs) (basis.f90:143-249)."""
+    global _TABLE
+    if _TABLE is None:
+        _TABLE = _parse_header()
+    t = _TABLE
+    if Z < 1 or Z >= len(t["k631_nshell"]) or t["k631_nshell"][Z] == 0:
+        raise ValueError(f"read_basis: atom Z={Z} not found")
+    shells = []
+    s0 = t["k631_shell0"][Z]
+    for s in range(s0, s0 + t["k631_nshell"][Z]):
+        p0, n = t["k631_shell_prim0"][s], t["k631_shell_nprim"][s]
+        shells.append((t["k631_shell_l"][s], [float(a) for a in t["k631_alpha"][p0:p0 + n]],
+                       [float(c) for c in t["k631_coef"][p0:p0 + n]]))
+    return shells
+
+
+def fact2(n):
+    r = 1.0
+    while n > 1:
+        r *= n
+        n -= 2
+    return r
+
+
+def cartesian_shell(L):
+    """(l, m, n) triplets in the order of get_cartesian_shell (basis.f90:371-409)."""
+    out = []
+    for k in range(L + 1):
+        for n in range(k + 1):
+            out.append((L - k, k - n, n))
+    return out
+
+
+def getstart(nprim):
+    """1-based start of each function's primitives (basis.f90:411-423)."""
+    st = [1]
+    for n in nprim[:-1]:
+        st.append(st[-1] + n)
+    return st
+
+
+def norm_prim(l, m, n, alpha):
+    """basis.f90:93-98.  2**(2*(l+m+n)+1.5) is a default-real (single
+    precision) power in the reference, since 1.5 carries no kind suffix."""
+    two_pow = float(np.float32(2.0 ** (2 * (l + m + n) + 1.5)))
+    return np.sqrt(two_pow * alpha ** (l + m + n + 1.5) / fact2(2 * l - 1) / fact2(2 * m - 1)
+                   / fact2(2 * n - 1) / PI ** 1.5)
+
+
+def norm_contr(l, m, n, alpha, coefu):
+    """basis.f90:100-132."""
+    L_ = float(l + m + n)
+    S = 0.0
+    for i in range(len(alpha)):
+        for j in range(len(alpha)):
+            S = S + coefu[i] * coefu[j] / (alpha[i] + alpha[j]) ** (L_ + 3.0 / 2)
+    return 1 / PI ** (3.0 / 4) * np.sqrt(2 ** L_ / fact2(2 * l - 1) / fact2(2 * m - 1)
+                                         / fact2(2 * n - 1)) / np.sqrt(S)
+
+
+class Basis:
+    """Contracted Cartesian GTOs in the reference's function order."""
+
+    def __init__(self, atno, xyz):
+        atno = [int(z) for z in atno]
+        xyz = np.asarray(xyz, dtype=np.float64).reshape(len(atno), 3)
+        nprim, center, power, coef, alpha = [], [], [], [], []
+        for z, r in zip(atno, xyz):
+            for L, al, co in read_basis(z):
+                for (l, m, n) in cartesian_shell(L):
+                    nprim.append(len(al))
+                    center.append(r.copy())
+                    power.append((l, m, n))
+                    cu = [c * norm_prim(l, m, n, a) for c, a in zip(co, al)]
+                    if len(al) > 1:  # fix_normalization (basis.f90:346-369)
+                        nn = norm_contr(l, m, n, al, cu)
+                        cu = [c * nn for c in cu]
+                    coef.extend(cu)
+                    alpha.extend(al)
+        self.atno = np.array(atno, dtype=np.int32)
+        self.xyz = xyz
+        self.n = len(nprim)
+        self.nprim = np.array(nprim, dtype=np.int32)
+        self.istart = np.array(getstart(nprim), dtype=np.int32) - 1  # 0-based (C side)
+        self.center = np.array(center, dtype=np.float64).reshape(-1, 3)
+        self.power = np.array(power, dtype=np.int32).reshape(-1, 3)
+        self.coef = np.array(coef, dtype=np.float64)
+        self.alpha = np.array(alpha, dtype=np.float64)
+
+    def cargs(self):
+        """Arguments in the order of the C drivers (qc.h:8-33)."""
+        xc = np.ascontiguousarray(self.center[:, 0])
+        yc = np.ascontiguousarray(self.center[:, 1])
+        zc = np.ascontiguousarray(self.center[:, 2])
+        lp = np.ascontiguousarray(self.power[:, 0])
+        mp = np.ascontiguousarray(self.power[:, 1])
+        npw = np.ascontiguousarray(self.power[:, 2])
+        self._keep = (xc, yc, zc, lp, mp, npw)
+        return [self.n, _i(self.nprim), _i(self.istart), _d(xc), _d(yc), _d(zc), _i(lp), _i(mp),
+                _i(npw), len(self.coef), _d(self.coef), _d(self.alpha)]
+
+
+def n_ints(n):
+    m = n * (n + 1) // 2
+    return m * (m + 1) // 2
+
+
+def ijkl(i, j, k, l):
+    """0-based packed index (cints.c:327-347), vectorised over numpy arrays."""
+    i, j, k, l = (np.asarray(x, dtype=np.int64) for x in (i, j, k, l))
+    a, b = np.maximum(i, j), np.minimum(i, j)
+    c, d = np.maximum(k, l), np.minimum(k, l)
+    ij = a * (a + 1) // 2 + b
+    kl = c * (c + 1) // 2 + d
+    hi, lo = np.maximum(ij, kl), np.minimum(ij, kl)
+    return hi * (hi + 1) // 2 + lo
+
+
+def one_electron(basis, which, L=None, prefix="oracle_"):
+    L = L or lib()
+    n = basis.n
+    out = np.zeros(n * n)
+    args = basis.cargs()
+    if which == "V":
+        x = np.ascontiguousarray(basis.xyz[:, 0])
+        y = np.ascontiguousarray(basis.xyz[:, 1])
+        z = np.ascontiguousarray(basis.xyz[:, 2])
+        getattr(L, prefix + "getV")(*args, len(basis.atno), _i(basis.atno), _d(x), _d(y), _d(z),
+                                    _d(out))
+    else:
+        getattr(L, prefix + "get" + which)(*args, _d(out))
+    return out.reshape(n, n, order="F")
+
+
+def getInts(basis, L=None, prefix="oracle_"):
+    L = L or lib()
+    out = np.zeros(n_ints(basis.n))
+    getattr(L, prefix + "getInts")(*basis.cargs(), _d(out))
+    return out
+
+
+def eri_list(basis, quartets):
+    q = np.ascontiguousarray(np.asarray(quartets, dtype=np.int32).reshape(-1, 4))
+    out = np.zeros(len(q))
+    lib().oracle_eri_list(*basis.cargs()[:9], _d(basis.coef), _d(basis.alpha), len(q), _i(q),
+                          _d(out))
+    return out
+
+
+# --------------------------------------------------------------------------
+# SCF (src/scf.f90)
+
+
+class SCFNotConverged(RuntimeError):
+    pass
+
+
+def formP(C, nocc):
+    """P(i,j) = 2 sum_{a<=nocc} C(i,a) C(j,a)  (scf.f90:12-24)."""
+    Co = C[:, :nocc]
+    return 2 * Co @ Co.T
+
+
+def formG(P, int2):
+    """G = J - K/2 from the packed integrals (scf.f90:26-58)."""
+    n = P.shape[0]
+    Pf = np.asfortranarray(P)
+    G = np.zeros((n, n), order="F")
+    lib().oracle_formG(n, _d(Pf), _d(int2), _d(G))
+    return np.array(G)
+
+
+def eigh(F, S):
+    """Generalised symmetric eigenproblem, lower triangles (linalg.f90:241-280)."""
+    import scipy.linalg
+
+    return scipy.linalg.eigh(F, S, lower=True, driver="gvd")
+
+
+def doscf(H, int2, S, nocc, nscf, tolE, tolP, alpha, verbose=False):
+    """Restates scf.f90:72-136 (P = 0 start, linear mixing, 4-energy window)."""
+    n = H.shape[0]
+    P = np.zeros((n, n))
+    Escf = []
+    for it in range(nscf):
+        G = formG(P, int2)
+        F = H + G
+        E0 = 0.5 * np.sum(P * (H + F))
+        Escf.append(E0)
+        if verbose:
+            print(it + 1, E0)
+        lam, C = eigh(F, S)
+        Pold = P
+        P = formP(C, nocc)
+        dP = np.sqrt(np.sum((P - Pold) ** 2) / 4)
+        if it + 1 > 3:
+            w = Escf[it - 3:it + 1]
+            if dP < tolP and max(w) - min(w) < tolE:
+                return dict(C=C, P=P, lam=lam, E0=E0, niter=it + 1, dP=dP)
+        P = (1 - alpha) * Pold + alpha * P
+    raise SCFNotConverged(f"SCF did not converge in {nscf} iterations.")
+
+
+def nuclear_energy(atno, xyz):
+    """scf.f90:138-150."""
+    E = 0.0
+    for i in range(len(atno)):
+        for j in range(i):
+            R = xyz[i] - xyz[j]
+            E += atno[i] * atno[j] / np.sqrt(np.dot(R, R))
+    return E
+
+
+def rhf_gauss(atno, xyz, nscf=40, alpha=1.0, tolE=1e-10, tolP=1e-8, verbose=False):
+    """drivers.f90:12-51: integrals, H = T + V, SCF with Nocc = sum(atno)/2."""
+    b = Basis(atno, xyz)
+    S = one_electron(b, "S")
+    T = one_electron(b, "T")
+    V = one_electron(b, "V")
+    int2 = getInts(b)
+    H = T + V
+    r = doscf(H, int2, S, int(sum(atno)) // 2, nscf, tolE, tolP, alpha, verbose)
+    Enuc = nuclear_energy(b.atno, b.xyz)
+    r.update(basis=b, S=S, T=T, V=V, H=H, int2=int2, Enuc=Enuc, Ekin=float(np.sum(r["P"] * T)),
+             Etot=r["E0"] + Enuc)
+    return r
+
+
+# --------------------------------------------------------------------------
+# AO -> MO and MBPT2 (src/mbpt.f90, src/mbpt2.f90)
+
+
+def unpack(int2, n):
+    i = np.arange(n)
+    idx = ijkl(i[:, None, None, None], i[None, :, None, None], i[None, None, :, None],
+               i[None, None, None, :])
+    return int2[idx]
+
+
+def transform_int2(int2, C):
+    """Full (mu nu|la si) -> (ij|kl) into the packed layout (mbpt.f90:11-79)."""
+    n = C.shape[0]
+    I = unpack(int2, n)
+    t = np.einsum("abcd,ck->abkd", I, C, optimize=True)
+    t = np.einsum("abkd,ai->ibkd", t, C, optimize=True)
+    t = np.einsum("ibkd,dl->ibkl", t, C, optimize=True)
+    mo = np.einsum("ibkl,bj->ijkl", t, C, optimize=True)
+    out = np.zeros_like(int2)
+    i = np.arange(n)
+    I4 = np.broadcast_arrays(i[:, None, None, None], i[None, :, None, None], i[None, None, :, None],
+                             i[None, None, None, :])
+    out[ijkl(*I4)] = mo
+    return out
+
+
+def mbpt2(moint2, lam, nocc):
+    """E2 = sum_{ab occ, rs virt} [2 (ar|bs)^2 - (ar|bs)(as|br)] / (e_a+e_b-e_r-e_s)
+    (mbpt2.f90:8-31; all electrons correlated)."""
+    n = len(lam)
+    a = np.arange(nocc)
+    r = np.arange(nocc, n)
+    A, R, B, S = np.meshgrid(a, r, a, r, indexing="ij")
+    arbs = moint2[ijkl(A, R, B, S)]
+    asbr = moint2[ijkl(A, S, B, R)]
+    den = lam[A] + lam[B] - lam[R] - lam[S]
+    return float(np.sum((2 * arbs * arbs - arbs * asbr) / den))
+
+
+def mp2_semidirect(int2, C, lam, nocc, block=8):
+    """The same E2 as mbpt2(transform_int2(...)), built from (ia|jb) only, in
+    blocks of mu so that no n^4 tensor is formed (for n beyond 120)."""
+    n = C.shape[0]
+    Co, Cv = C[:, :nocc], C[:, nocc:]
+    iajb = np.zeros((nocc, n - nocc, nocc, n - nocc))
+    i = np.arange(n)
+    for m0 in range(0, n, block):
+        mu = np.arange(m0, min(n, m0 + block))
+        X = int2[ijkl(mu[:, None, None, None], i[None, :, None, None], i[None, None, :, None],
+                      i[None, None, None, :])]
+        X = np.einsum("mnls,lj,sb->mnjb", X, Co, Cv, optimize=True)
+        iajb += np.einsum("mnjb,mi,na->iajb", X, Co[mu], Cv, optimize=True)
+    e_o, e_v = lam[:nocc], lam[nocc:]
+    den = e_o[:, None, None, None] - e_v[None, :, None, None] + e_o[None, None, :, None] \
+        - e_v[None, None, None, :]
+    return float(np.sum((2 * iajb ** 2 - iajb * iajb.transpose(0, 3, 2, 1)) / den))
