@@ -1,0 +1,208 @@
+"""Python mirror of hfsolver's molecular GTO interfaces over libhfgpu.
+
+Same names and argument meaning as the reference's routines, numpy in and out:
+
+=====================  ==============================================  =======================
+this module            reference                                       libhfgpu entry point
+=====================  ==============================================  =======================
+getS, getT, getV       src/qc.c:6-93 (C drivers)                       hfgpu_getS/T/V
+getInts                src/qc.c:95-131                                 hfgpu_getInts
+getints2               src/gaussians_hfsolver.f90:13-34 (plugin)       hfgpu_getints2
+doscf                  src/scf.f90:72-136                              hfgpu_doscf
+transform_int2         src/mbpt.f90:11-79                              hfgpu_transform_int2
+mbpt2                  src/mbpt.f90:154-159, src/mbpt2.f90:8-31        hfgpu_mbpt2
+rhf_gauss / rhf        src/drivers.f90:12-51 (+ MBPT2)                 hfgpu_rhf
+=====================  ==============================================  =======================
+
+Errors raise HFGPUError (the reference stops the process instead); an SCF
+that does not converge raises SCFNotConverged, like stop_error in doscf.
+"""
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import HFGPUError
+
+_dp = _lib._dp
+_ip = _lib._ip
+
+
+class SCFNotConverged(HFGPUError):
+    pass
+
+
+def _check(code):
+    if code == _lib.ERR_NOT_CONVERGED:
+        raise SCFNotConverged(code, _lib.lib().hfgpu_last_error().decode())
+    _lib.check(code)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def packed_size(n):
+    m = n * (n + 1) // 2
+    return m * (m + 1) // 2
+
+
+def _basis_args(nprim, istart, xcenter, ycenter, zcenter, lpower, mpower, npower, coef, alpha):
+    arrs = [_i32(nprim), _i32(istart), _f64(xcenter), _f64(ycenter), _f64(zcenter), _i32(lpower), _i32(mpower),
+            _i32(npower), _f64(coef), _f64(alpha)]
+    n = len(arrs[0])
+    for a in arrs[1:8]:
+        if len(a) != n:
+            raise ValueError("per-function arrays must all have length nbf")
+    args = [n, _i(arrs[0]), _i(arrs[1]), _d(arrs[2]), _d(arrs[3]), _d(arrs[4]), _i(arrs[5]), _i(arrs[6]),
+            _i(arrs[7]), len(arrs[8]), _d(arrs[8]), _d(arrs[9])]
+    return n, args, arrs
+
+
+def getS(nprim, istart, xcenter, ycenter, zcenter, lpower, mpower, npower, coef, alpha):
+    n, args, keep = _basis_args(nprim, istart, xcenter, ycenter, zcenter, lpower, mpower, npower, coef, alpha)
+    S = np.zeros((n, n), order="F")
+    _check(_lib.lib().hfgpu_getS(*args, _d(S)))
+    return S
+
+
+def getT(nprim, istart, xcenter, ycenter, zcenter, lpower, mpower, npower, coef, alpha):
+    n, args, keep = _basis_args(nprim, istart, xcenter, ycenter, zcenter, lpower, mpower, npower, coef, alpha)
+    T = np.zeros((n, n), order="F")
+    _check(_lib.lib().hfgpu_getT(*args, _d(T)))
+    return T
+
+
+def getV(nprim, istart, xcenter, ycenter, zcenter, lpower, mpower, npower, coef, alpha, atno, x, y, z):
+    n, args, keep = _basis_args(nprim, istart, xcenter, ycenter, zcenter, lpower, mpower, npower, coef, alpha)
+    at, xa, ya, za = _i32(atno), _f64(x), _f64(y), _f64(z)
+    V = np.zeros((n, n), order="F")
+    _check(_lib.lib().hfgpu_getV(*args, len(at), _i(at), _d(xa), _d(ya), _d(za), _d(V)))
+    return V
+
+
+def getInts(nprim, istart, xcenter, ycenter, zcenter, lpower, mpower, npower, coef, alpha):
+    """All unique (ij|kl) in the 8-fold packed layout (istart 0-based, as qc.c)."""
+    n, args, keep = _basis_args(nprim, istart, xcenter, ycenter, zcenter, lpower, mpower, npower, coef, alpha)
+    out = np.zeros(packed_size(n))
+    _check(_lib.lib().hfgpu_getInts(*args, _d(out)))
+    return out
+
+
+def getints2(nprim, istart, center, power, coef, alpha):
+    """Plugin form: center(3, n), power(3, n), 1-based istart (Fortran layout)."""
+    nprim, istart = _i32(nprim), _i32(istart)
+    n = len(nprim)
+    center = np.asfortranarray(np.asarray(center, dtype=np.float64).reshape(3, n))
+    power = np.asfortranarray(np.asarray(power, dtype=np.int32).reshape(3, n))
+    coef, alpha = _f64(coef), _f64(alpha)
+    out = np.zeros(packed_size(n))
+    _check(_lib.lib().hfgpu_getints2(n, _i(nprim), _i(istart), center.ctypes.data_as(_dp),
+                                     power.ctypes.data_as(_ip), len(coef), _d(coef), _d(alpha), _d(out),
+                                     len(out)))
+    return out
+
+
+def doscf(H, int2, S, Noccupied, Nscf, tolE, tolP, alpha):
+    """Returns (C, P, lam, E0, niter); raises SCFNotConverged like stop_error."""
+    H = np.asfortranarray(H, dtype=np.float64)
+    S = np.asfortranarray(S, dtype=np.float64)
+    int2 = _f64(int2)
+    n = H.shape[0]
+    if int2.size != packed_size(n):
+        raise ValueError("int2 has the wrong length")
+    C = np.zeros((n, n), order="F")
+    P = np.zeros((n, n), order="F")
+    lam = np.zeros(n)
+    E0 = np.zeros(1)
+    it = np.zeros(1, dtype=np.int32)
+    _check(_lib.lib().hfgpu_doscf(n, H.ctypes.data_as(_dp), _d(int2), S.ctypes.data_as(_dp), int(Noccupied),
+                                  int(Nscf), float(tolE), float(tolP), float(alpha), C.ctypes.data_as(_dp),
+                                  P.ctypes.data_as(_dp), _d(lam), _d(E0), _i(it)))
+    return C, P, lam, float(E0[0]), int(it[0])
+
+
+def transform_int2(int2, C):
+    C = np.asfortranarray(C, dtype=np.float64)
+    int2 = _f64(int2)
+    n = C.shape[0]
+    out = np.zeros(packed_size(n))
+    _check(_lib.lib().hfgpu_transform_int2(n, _d(int2), C.ctypes.data_as(_dp), _d(out)))
+    return out
+
+
+def mbpt2(moint2, lam, Noccupied):
+    moint2, lam = _f64(moint2), _f64(lam)
+    E2 = np.zeros(1)
+    _check(_lib.lib().hfgpu_mbpt2(len(lam), _d(moint2), _d(lam), int(Noccupied), _d(E2)))
+    return float(E2[0])
+
+
+@dataclass
+class RHFOptions:
+    nscf: int = 40
+    mix_alpha: float = 1.0
+    tolE: float = 1e-10
+    tolP: float = 1e-8
+    diis: bool = False
+    diis_size: int = 8
+    schwarz: float = 0.0
+    mp2: str = "fp64"          # "none" | "fp64" | "split_bf16"
+    mp2_nocc: int = 0          # <= 0: sum(Z)/2
+
+    def to_c(self):
+        o = _lib.Options()
+        _lib.lib().hfgpu_default_options(o)
+        o.nscf, o.mix_alpha, o.tolE, o.tolP = self.nscf, self.mix_alpha, self.tolE, self.tolP
+        o.scf_accel = _lib.SCF_DIIS if self.diis else _lib.SCF_MIXING
+        o.diis_size = self.diis_size
+        o.schwarz = self.schwarz
+        o.mp2 = {"none": _lib.MP2_NONE, "fp64": _lib.MP2_FP64, "split_bf16": _lib.MP2_SPLIT_BF16}[self.mp2]
+        o.mp2_nocc = self.mp2_nocc
+        return o
+
+
+def basis_size(atno):
+    at = _i32(atno)
+    return _lib.lib().hfgpu_basis_size(len(at), _i(at))
+
+
+def rhf(atno, xyz, options=None, want_orbitals=False):
+    """RHF (+ MBPT2) for nuclei atno at xyz (natoms x 3, bohr) in 6-31G**.
+
+    Returns a dict with Etot, E0, Enuc, Ekin, E2, niter, nbf, nocc, the
+    evaluated quartet counts and stage times; C and lam when want_orbitals."""
+    opt = (options or RHFOptions()).to_c()
+    at = _i32(atno)
+    xyz = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64).reshape(len(at), 3))
+    res = _lib.Result()
+    n = basis_size(at)
+    C = np.zeros((n, n), order="F") if want_orbitals and n else None
+    lam = np.zeros(n) if want_orbitals and n else None
+    code = _lib.lib().hfgpu_rhf(len(at), _i(at), _d(xyz), opt, res,
+                                C.ctypes.data_as(_dp) if C is not None else None,
+                                _d(lam) if lam is not None else None)
+    _check(code)
+    out = {k: getattr(res, k) for k, _ in _lib.Result._fields_ if k != "reserved"}
+    if want_orbitals:
+        out["C"], out["lam"] = C, lam
+    return out
+
+
+def rhf_gauss(atno, xyz, Nscf=40, alpha=1.0, tolE=1e-10, tolP=1e-8):
+    """drivers.f90 rhf_gauss: returns (C, lam, E0, Enuc, Ekin, Etot)."""
+    r = rhf(atno, xyz, RHFOptions(nscf=Nscf, mix_alpha=alpha, tolE=tolE, tolP=tolP, mp2="none"),
+            want_orbitals=True)
+    return r["C"], r["lam"], r["E0"], r["Enuc"], r["Ekin"], r["Etot"]

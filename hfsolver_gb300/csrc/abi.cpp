@@ -1,0 +1,345 @@
+// extern "C" entry points of libhfgpu (declared in include/hfgpu.h).
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "internal.h"
+#include "scf.h"
+
+using namespace hfgpu;
+
+namespace {
+
+template <class F>
+int guard(F&& f)
+{
+    try {
+        f();
+        return HFGPU_OK;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_last_error("host allocation failed");
+        return HFGPU_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return HFGPU_ERR_CUDA;
+    }
+}
+
+struct Timer {
+    cudaEvent_t a, b;
+    cudaStream_t s;
+    explicit Timer(cudaStream_t st) : s(st)
+    {
+        HF_CUDA(cudaEventCreate(&a));
+        HF_CUDA(cudaEventCreate(&b));
+        HF_CUDA(cudaEventRecord(a, s));
+    }
+    double ms()
+    {
+        HF_CUDA(cudaEventRecord(b, s));
+        HF_CUDA(cudaEventSynchronize(b));
+        float t = 0;
+        HF_CUDA(cudaEventElapsedTime(&t, a, b));
+        return t;
+    }
+    ~Timer()
+    {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+};
+
+void check_ptr(const void* p, const char* name)
+{
+    HF_CHECK(p != nullptr, HFGPU_ERR_INVALID, std::string(name) + " is NULL");
+}
+
+void onee_dropin(int which, int nbf, const int* nprim, const int* istart, const double* xc, const double* yc,
+                 const double* zc, const int* lp, const int* mp, const int* np, int n2, const double* coef,
+                 const double* alpha, int nat, const int* atno, const double* x, const double* y, const double* z,
+                 double* out)
+{
+    check_ptr(out, "output");
+    Basis b = basis_from_functions(nbf, nprim, istart, xc, yc, zc, lp, mp, np, n2, coef, alpha);
+    Context& ctx = context();
+    DBuf<double> d((size_t)nbf * nbf, ctx.stream);
+    onee_compute(ctx, b, nat, atno, x, y, z, which == 0 ? d.p : nullptr, which == 1 ? d.p : nullptr,
+                 which == 2 ? d.p : nullptr);
+    d.download(out, (size_t)nbf * nbf);
+    HF_CUDA(cudaStreamSynchronize(ctx.stream));
+}
+
+void ints_dropin(const Basis& b, double* Ints, double schwarz, EriStats* st)
+{
+    Context& ctx = context();
+    const int64_t np = packed_size(b.nbf);
+    DBuf<double> d(np, ctx.stream);
+    d.zero();
+    EriPlan* plan = eri_plan_create(ctx, b, schwarz);
+    try {
+        eri_compute_packed(ctx, plan, d.p, st);
+    } catch (...) {
+        eri_plan_destroy(plan);
+        throw;
+    }
+    eri_plan_destroy(plan);
+    d.download(Ints, np);
+    HF_CUDA(cudaStreamSynchronize(ctx.stream));
+}
+
+}  // namespace
+
+extern "C" {
+
+int hfgpu_getS(int nbf, const int* nprim, const int* istart, const double* xc, const double* yc, const double* zc,
+               const int* lp, const int* mp, const int* np, int n2, const double* coef, const double* alpha,
+               double* S)
+{
+    return guard([&] {
+        onee_dropin(0, nbf, nprim, istart, xc, yc, zc, lp, mp, np, n2, coef, alpha, 0, nullptr, nullptr, nullptr,
+                    nullptr, S);
+    });
+}
+
+int hfgpu_getT(int nbf, const int* nprim, const int* istart, const double* xc, const double* yc, const double* zc,
+               const int* lp, const int* mp, const int* np, int n2, const double* coef, const double* alpha,
+               double* T)
+{
+    return guard([&] {
+        onee_dropin(1, nbf, nprim, istart, xc, yc, zc, lp, mp, np, n2, coef, alpha, 0, nullptr, nullptr, nullptr,
+                    nullptr, T);
+    });
+}
+
+int hfgpu_getV(int nbf, const int* nprim, const int* istart, const double* xc, const double* yc, const double* zc,
+               const int* lp, const int* mp, const int* np, int n2, const double* coef, const double* alpha, int nat,
+               const int* atno, const double* x, const double* y, const double* z, double* V)
+{
+    return guard([&] {
+        HF_CHECK(nat >= 0, HFGPU_ERR_INVALID, "nat must be >= 0");
+        for (int i = 0; i < nat; i++)
+            HF_CHECK(std::isfinite(x[i]) && std::isfinite(y[i]) && std::isfinite(z[i]), HFGPU_ERR_INVALID,
+                     "non-finite nuclear coordinate");
+        onee_dropin(2, nbf, nprim, istart, xc, yc, zc, lp, mp, np, n2, coef, alpha, nat, atno, x, y, z, V);
+    });
+}
+
+int hfgpu_getInts(int nbf, const int* nprim, const int* istart, const double* xc, const double* yc,
+                  const double* zc, const int* lp, const int* mp, const int* np, int n2, const double* coef,
+                  const double* alpha, double* Ints)
+{
+    return guard([&] {
+        check_ptr(Ints, "Ints");
+        Basis b = basis_from_functions(nbf, nprim, istart, xc, yc, zc, lp, mp, np, n2, coef, alpha);
+        ints_dropin(b, Ints, 0.0, nullptr);
+    });
+}
+
+int hfgpu_getints2(int n, const int* nprim, const int* istart, const double* center, const int* power, int n2,
+                   const double* coef, const double* alpha, double* int2, int64_t nint2)
+{
+    return guard([&] {
+        HF_CHECK(n >= 1, HFGPU_ERR_INVALID, "n must be >= 1");
+        HF_CHECK(nint2 == packed_size(n), HFGPU_ERR_INVALID,
+                 "size(int2) must be m(m+1)/2 with m = n(n+1)/2");
+        check_ptr(int2, "int2");
+        std::vector<int> st0(n), lp(n), mp(n), npw(n);
+        std::vector<double> xc(n), yc(n), zc(n);
+        for (int i = 0; i < n; i++) {
+            st0[i] = istart[i] - 1;
+            xc[i] = center[3 * i]; yc[i] = center[3 * i + 1]; zc[i] = center[3 * i + 2];
+            lp[i] = power[3 * i]; mp[i] = power[3 * i + 1]; npw[i] = power[3 * i + 2];
+        }
+        Basis b = basis_from_functions(n, nprim, st0.data(), xc.data(), yc.data(), zc.data(), lp.data(), mp.data(),
+                                       npw.data(), n2, coef, alpha);
+        ints_dropin(b, int2, 0.0, nullptr);
+    });
+}
+
+int hfgpu_doscf(int n, const double* H, const double* int2, const double* S, int nocc, int nscf, double tolE,
+                double tolP, double alpha, double* C, double* P, double* lam, double* E0, int* niter)
+{
+    int conv = 1;
+    int rc = guard([&] {
+        HF_CHECK(n >= 1 && nocc >= 0 && nocc <= n && nscf >= 1, HFGPU_ERR_INVALID, "invalid sizes");
+        check_ptr(H, "H"); check_ptr(int2, "int2"); check_ptr(S, "S");
+        check_ptr(C, "C"); check_ptr(P, "P"); check_ptr(lam, "lam"); check_ptr(E0, "E0");
+        Context& ctx = context();
+        const size_t nn = (size_t)n * n;
+        DBuf<double> dH(nn, ctx.stream), dS(nn, ctx.stream), dI(packed_size(n), ctx.stream);
+        DBuf<double> dC(nn, ctx.stream), dP(nn, ctx.stream), dL(n, ctx.stream);
+        dH.upload(H, nn); dS.upload(S, nn); dI.upload(int2, packed_size(n));
+        ScfIn in;
+        in.n = n; in.nocc = nocc; in.nscf = nscf; in.dH = dH.p; in.dS = dS.p; in.d_int2 = dI.p;
+        in.tolE = tolE; in.tolP = tolP; in.alpha = alpha;
+        ScfOut o = run_scf(ctx, in, dC.p, dP.p, dL.p);
+        dC.download(C, nn); dP.download(P, nn); dL.download(lam, n);
+        HF_CUDA(cudaStreamSynchronize(ctx.stream));
+        *E0 = o.E0;
+        if (niter) *niter = o.niter;
+        conv = o.converged;
+    });
+    if (rc == HFGPU_OK && !conv) {
+        set_last_error("SCF did not converge in " + std::to_string(nscf) + " iterations.");
+        return HFGPU_ERR_NOT_CONVERGED;
+    }
+    return rc;
+}
+
+int hfgpu_transform_int2(int n, const double* int2, const double* C, double* moint2)
+{
+    return guard([&] {
+        HF_CHECK(n >= 1, HFGPU_ERR_INVALID, "n must be >= 1");
+        check_ptr(int2, "int2"); check_ptr(C, "C"); check_ptr(moint2, "moint2");
+        Context& ctx = context();
+        const int64_t np = packed_size(n);
+        DBuf<double> dI(np, ctx.stream), dC((size_t)n * n, ctx.stream), dM(np, ctx.stream);
+        dI.upload(int2, np);
+        dC.upload(C, (size_t)n * n);
+        transform_packed(ctx, n, dI.p, dC.p, dM.p);
+        dM.download(moint2, np);
+        HF_CUDA(cudaStreamSynchronize(ctx.stream));
+    });
+}
+
+int hfgpu_mbpt2(int n, const double* moint2, const double* lam, int nocc, double* E2)
+{
+    return guard([&] {
+        HF_CHECK(n >= 1 && nocc >= 0 && nocc <= n, HFGPU_ERR_INVALID, "invalid sizes");
+        check_ptr(moint2, "moint2"); check_ptr(lam, "lam"); check_ptr(E2, "E2");
+        Context& ctx = context();
+        const int64_t np = packed_size(n);
+        DBuf<double> dM(np, ctx.stream), dL(n, ctx.stream);
+        dM.upload(moint2, np);
+        dL.upload(lam, n);
+        *E2 = mbpt2_packed(ctx, n, dM.p, dL.p, nocc);
+    });
+}
+
+void hfgpu_default_options(hfgpu_options* o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->nscf = 40;
+    o->mix_alpha = 1.0;
+    o->tolE = 1e-10;
+    o->tolP = 1e-8;
+    o->scf_accel = HFGPU_SCF_MIXING;
+    o->diis_size = 8;
+    o->schwarz = 0.0;
+    o->mp2 = HFGPU_MP2_FP64;
+    o->mp2_nocc = 0;
+}
+
+int hfgpu_basis_size(int natoms, const int* atno)
+{
+    if (natoms < 1 || !atno) return 0;
+    return basis_size(natoms, atno);
+}
+
+int hfgpu_rhf(int natoms, const int* atno, const double* xyz, const hfgpu_options* opt_in, hfgpu_result* res,
+              double* C, double* lam)
+{
+    int conv = 1;
+    int nscf = 0;
+    int rc = guard([&] {
+        check_ptr(atno, "atno"); check_ptr(xyz, "xyz"); check_ptr(res, "res");
+        hfgpu_options opt;
+        if (opt_in) opt = *opt_in; else hfgpu_default_options(&opt);
+        nscf = opt.nscf;
+        HF_CHECK(opt.nscf >= 1, HFGPU_ERR_INVALID, "nscf must be >= 1");
+        HF_CHECK(opt.mp2 >= HFGPU_MP2_NONE && opt.mp2 <= HFGPU_MP2_FP64, HFGPU_ERR_UNSUPPORTED,
+                 "requested MP2 precision is not available");
+        std::memset(res, 0, sizeof(*res));
+        Basis b = build_basis(natoms, atno, xyz);  // validates the input before any device work
+        Context& ctx = context();
+        cudaStream_t st = ctx.stream;
+        Timer total(st);
+        const int n = b.nbf;
+        int nelec = 0;
+        for (int i = 0; i < natoms; i++) nelec += atno[i];
+        const int nocc = nelec / 2;
+        const size_t nn = (size_t)n * n;
+        res->nbf = n;
+        res->nocc = nocc;
+        res->nshell = (int)b.shells.size();
+        std::vector<double> x(natoms), y(natoms), z(natoms);
+        for (int i = 0; i < natoms; i++) { x[i] = xyz[3 * i]; y[i] = xyz[3 * i + 1]; z[i] = xyz[3 * i + 2]; }
+        DBuf<double> dS(nn, st), dT(nn, st), dV(nn, st), dH(nn, st);
+        onee_compute(ctx, b, natoms, atno, x.data(), y.data(), z.data(), dS.p, dT.p, dV.p);
+        {
+            const double one = 1.0;
+            HF_CUBLAS(cublasDgeam(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, &one, dT.p, n, &one, dV.p, n, dH.p, n));
+        }
+        // integrals, resident in HBM for the whole SCF
+        Timer te(st);
+        DBuf<double> dI(packed_size(n), st);
+        dI.zero();
+        EriStats es;
+        EriPlan* plan = eri_plan_create(ctx, b, opt.schwarz);
+        try {
+            eri_compute_packed(ctx, plan, dI.p, &es);
+        } catch (...) {
+            eri_plan_destroy(plan);
+            throw;
+        }
+        eri_plan_destroy(plan);
+        res->ms_eri = te.ms();
+        res->n_quartets = es.n_quartets;
+        res->n_bf_quartets = es.n_bf_quartets;
+        res->n_prim_quartets = es.n_prim_quartets;
+        res->eri_flops = es.flops;
+        // SCF
+        Timer ts(st);
+        DBuf<double> dC(nn, st), dP(nn, st), dL(n, st);
+        ScfIn in;
+        in.n = n; in.nocc = nocc; in.nscf = opt.nscf; in.dH = dH.p; in.dS = dS.p; in.d_int2 = dI.p;
+        in.tolE = opt.tolE; in.tolP = opt.tolP; in.alpha = opt.mix_alpha;
+        in.accel = opt.scf_accel; in.diis_size = opt.diis_size > 0 ? opt.diis_size : 8;
+        ScfOut so = run_scf(ctx, in, dC.p, dP.p, dL.p);
+        res->ms_scf = ts.ms();
+        conv = so.converged;
+        double Enuc = 0;
+        for (int i = 0; i < natoms; i++)
+            for (int j = 0; j < i; j++) {
+                double dx = xyz[3 * i] - xyz[3 * j], dy = xyz[3 * i + 1] - xyz[3 * j + 1],
+                       dz = xyz[3 * i + 2] - xyz[3 * j + 2];
+                Enuc += atno[i] * atno[j] / std::sqrt(dx * dx + dy * dy + dz * dz);
+            }
+        res->E0 = so.E0;
+        res->Enuc = Enuc;
+        res->Etot = so.E0 + Enuc;
+        res->Ekin = device_dot(ctx, (int64_t)nn, dP.p, dT.p);
+        res->dP = so.dP;
+        res->niter = so.niter;
+        // MBPT2
+        if (conv && opt.mp2 != HFGPU_MP2_NONE) {
+            Timer tm(st);
+            const int mo = opt.mp2_nocc > 0 ? opt.mp2_nocc : nocc;
+            HF_CHECK(mo <= n, HFGPU_ERR_INVALID, "mp2_nocc larger than the basis");
+            const int mv = n - mo;
+            if (mo > 0 && mv > 0) {
+                DBuf<double> iajb((size_t)mo * mv * mo * mv, st);
+                ao2mo_fp64(ctx, n, dI.p, dC.p, mo, dC.p + (size_t)n * mo, mv, iajb.p);
+                res->E2 = mp2_energy(ctx, mo, mv, iajb.p, dL.p);
+            }
+            res->ms_mp2 = tm.ms();
+        }
+        if (C) dC.download(C, nn);
+        if (lam) dL.download(lam, n);
+        HF_CUDA(cudaStreamSynchronize(st));
+        res->ms_total = total.ms();
+    });
+    if (rc == HFGPU_OK && !conv) {
+        set_last_error("SCF did not converge in " + std::to_string(nscf) + " iterations.");
+        return HFGPU_ERR_NOT_CONVERGED;
+    }
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,45 @@
+// Per-device context: stream, cuBLAS/cuSOLVER handles, Boys-function grid.
+#include <mutex>
+#include <vector>
+
+#include "boys.cuh"
+#include "internal.h"
+
+namespace hfgpu {
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string& m) { g_last_error = m; }
+
+static std::mutex g_ctx_mutex;
+static std::vector<Context*> g_ctx;
+
+Context& context()
+{
+    int dev = 0;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) throw Error(HFGPU_ERR_NO_DEVICE, "no CUDA device");
+    HF_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_ctx_mutex);
+    if ((int)g_ctx.size() < ndev) g_ctx.resize(ndev, nullptr);
+    if (g_ctx[dev]) return *g_ctx[dev];
+    auto* c = new Context();
+    c->device = dev;
+    HF_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    HF_CUBLAS(cublasCreate(&c->blas));
+    HF_CUBLAS(cublasSetStream(c->blas, c->stream));
+    HF_CUSOLVER(cusolverDnCreate(&c->solver));
+    HF_CUSOLVER(cusolverDnSetStream(c->solver, c->stream));
+    HF_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev));
+    std::vector<double> tab((size_t)BOYS_NROW * BOYS_STRIDE);
+    boys_make_table(tab.data());
+    HF_CUDA(cudaMalloc((void**)&c->boys, tab.size() * sizeof(double)));
+    HF_CUDA(cudaMemcpy(c->boys, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+    g_ctx[dev] = c;
+    return *c;
+}
+
+}  // namespace hfgpu
+
+extern "C" const char* hfgpu_last_error(void) { return hfgpu::g_last_error.c_str(); }
+extern "C" int hfgpu_version(void) { return 1; }

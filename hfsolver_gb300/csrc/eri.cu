@@ -1,0 +1,449 @@
+// Contracted electron-repulsion integrals (ab|cd) in FP64 on sm_103a.
+//
+// Replaces hfsolver's getInts -> contr_coulomb -> coulomb_repulsion
+// (src/qc.c:95-131, src/cints.c:72-183): the same contracted Cartesian
+// integrals, written into the same 8-fold packed array, but evaluated
+// shell-quartet-at-a-time with the McMurchie-Davidson scheme instead of one
+// Cartesian primitive quartet at a time with the THO formula.
+//
+//   (ab|cd) = 2 pi^{5/2} / (p q sqrt(p+q)) sum_{tuv} E^{ab}_{tuv}
+//             sum_{t'u'v'} (-1)^{t'+u'+v'} E^{cd}_{t'u'v'} R_{t+t',u+u',v+v'}(alpha, P-Q)
+//
+// GB300 layout and mapping:
+//  * Primitive-pair records (p, P and the Hermite coefficients of every
+//    component pair, scaled by the contraction coefficients, exp(-mu R_AB^2)
+//    and 1/p) are built once per molecule by pair_data_kernel and stay in HBM
+//    (L2-resident for molecules of a few hundred functions).
+//  * Quartets are grouped by class (bra pair type <= ket pair type, six pair
+//    types ss..dd) and by primitive count, so every warp runs a uniform loop.
+//    Each class is one kernel instantiation whose component loops are fully
+//    unrolled at compile time: only the non-zero Hermite terms are touched.
+//  * The ket's Cartesian components are split into G chunks of NCD; a warp
+//    handles 32 quartets for one chunk (warp-uniform), so each thread keeps
+//    NAB x NCD accumulators in registers.
+//  * Schwarz screening: pairs of a group are sorted by decreasing bound
+//    Q = sqrt(max |(ab|ab)|), so the kets surviving Q_bra Q_ket >= thr form a
+//    prefix; quartets are enumerated from prefix sums (no quartet list).
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <numeric>
+
+#include "boys.cuh"
+#include "eri_kernel.cuh"
+#include "internal.h"
+#include "md.cuh"
+
+namespace hfgpu {
+
+int64_t packed_size(int64_t n)
+{
+    int64_t m = n * (n + 1) / 2;
+    return m * (m + 1) / 2;
+}
+
+__host__ __device__ __forceinline__ int64_t packed_index(int64_t i, int64_t j, int64_t k, int64_t l)
+{
+    int64_t a = i > j ? i : j, b = i > j ? j : i;
+    int64_t c = k > l ? k : l, d = k > l ? l : k;
+    int64_t ij = a * (a + 1) / 2 + b, kl = c * (c + 1) / 2 + d;
+    return ij >= kl ? ij * (ij + 1) / 2 + kl : kl * (kl + 1) / 2 + ij;
+}
+
+// ------------------------------------------------------------------ pair data
+template <int LA, int LB>
+__device__ __forceinline__ void hermite_1d(double (&E)[LA + 1][LB + 1][LA + LB + 1], double xpa, double xpb,
+                                           double i2p)
+{
+#pragma unroll
+    for (int i = 0; i <= LA; ++i)
+#pragma unroll
+        for (int j = 0; j <= LB; ++j)
+#pragma unroll
+            for (int t = 0; t <= LA + LB; ++t) E[i][j][t] = 0.0;
+    E[0][0][0] = 1.0;
+#pragma unroll
+    for (int i = 0; i < LA; ++i)
+#pragma unroll
+        for (int t = 0; t <= i + 1; ++t) {
+            double v = xpa * E[i][0][t];
+            if (t > 0) v = fma(i2p, E[i][0][t - 1], v);
+            if (t + 1 <= i) v = fma((double)(t + 1), E[i][0][t + 1], v);
+            E[i + 1][0][t] = v;
+        }
+#pragma unroll
+    for (int i = 0; i <= LA; ++i)
+#pragma unroll
+        for (int j = 0; j < LB; ++j)
+#pragma unroll
+            for (int t = 0; t <= i + j + 1; ++t) {
+                double v = xpb * E[i][j][t];
+                if (t > 0) v = fma(i2p, E[i][j][t - 1], v);
+                if (t + 1 <= i + j) v = fma((double)(t + 1), E[i][j][t + 1], v);
+                E[i][j + 1][t] = v;
+            }
+}
+
+template <int T>
+__global__ void pair_data_kernel(ShellDev sh, PairDev pr, const int4* items, int nitems, double* pdata)
+{
+    constexpr int LA = ptype_la(T), LB = ptype_lb(T);
+    constexpr int STRIDE = pair_stride(LA, LB);
+    int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nitems) return;
+    int4 item = items[it];
+    int P = item.x, ia = item.y, ib = item.z;
+    int A = pr.A[P], B = pr.B[P];
+    double a = sh.alpha[sh.prim0[A] + ia], b = sh.alpha[sh.prim0[B] + ib];
+    double ax = sh.xyz[3 * A], ay = sh.xyz[3 * A + 1], az = sh.xyz[3 * A + 2];
+    double bx = sh.xyz[3 * B], by = sh.xyz[3 * B + 1], bz = sh.xyz[3 * B + 2];
+    double p = a + b, ip = 1.0 / p, mu = a * b * ip;
+    double px = (a * ax + b * bx) * ip, py = (a * ay + b * by) * ip, pz = (a * az + b * bz) * ip;
+    double rab2 = (ax - bx) * (ax - bx) + (ay - by) * (ay - by) + (az - bz) * (az - bz);
+    double kab = exp(-mu * rab2) * ip;
+    double Ex[LA + 1][LB + 1][LA + LB + 1], Ey[LA + 1][LB + 1][LA + LB + 1], Ez[LA + 1][LB + 1][LA + LB + 1];
+    hermite_1d<LA, LB>(Ex, px - ax, px - bx, 0.5 * ip);
+    hermite_1d<LA, LB>(Ey, py - ay, py - by, 0.5 * ip);
+    hermite_1d<LA, LB>(Ez, pz - az, pz - bz, 0.5 * ip);
+    int nb = sh.nprim[B];
+    double* rec = pdata + pr.off[P] + (int64_t)(ia * nb + ib) * STRIDE;
+    rec[0] = p;
+    rec[1] = px;
+    rec[2] = py;
+    rec[3] = pz;
+    const double* ca = sh.coef + sh.coef0[A];
+    const double* cb = sh.coef + sh.coef0[B];
+    int npa = sh.nprim[A];
+#pragma unroll
+    for (int ca_i = 0; ca_i < ncart(LA); ++ca_i)
+#pragma unroll
+        for (int cb_i = 0; cb_i < ncart(LB); ++cb_i) {
+            const Cart c1 = cart(LA, ca_i), c2 = cart(LB, cb_i);
+            double s = ca[ca_i * npa + ia] * cb[cb_i * nb + ib] * kab;
+            double* e = rec + PAIR_HDR + eoff(LA, LB, ca_i, cb_i);
+            int w = 0;
+#pragma unroll
+            for (int t = 0; t <= c1.l + c2.l; ++t)
+#pragma unroll
+                for (int u = 0; u <= c1.m + c2.m; ++u)
+#pragma unroll
+                    for (int v = 0; v <= c1.n + c2.n; ++v)
+                        e[w++] = s * Ex[c1.l][c2.l][t] * Ey[c1.m][c2.m][u] * Ez[c1.n][c2.n][v];
+        }
+}
+
+// ------------------------------------------------------------------ host side
+#define HF_DECL(B, K) KernelFn eri_kernel_##B##K(int mode);
+HF_DECL(0, 0) HF_DECL(0, 1) HF_DECL(0, 2) HF_DECL(0, 3) HF_DECL(0, 4) HF_DECL(0, 5)
+HF_DECL(1, 1) HF_DECL(1, 2) HF_DECL(1, 3) HF_DECL(1, 4) HF_DECL(1, 5)
+HF_DECL(2, 2) HF_DECL(2, 3) HF_DECL(2, 4) HF_DECL(2, 5)
+HF_DECL(3, 3) HF_DECL(3, 4) HF_DECL(3, 5)
+HF_DECL(4, 4) HF_DECL(4, 5)
+HF_DECL(5, 5)
+#undef HF_DECL
+
+static KernelFn get_kernel(int tb, int tk, int mode)
+{
+    static KernelFn (*const table[6][6])(int) = {
+        {eri_kernel_00, eri_kernel_01, eri_kernel_02, eri_kernel_03, eri_kernel_04, eri_kernel_05},
+        {nullptr, eri_kernel_11, eri_kernel_12, eri_kernel_13, eri_kernel_14, eri_kernel_15},
+        {nullptr, nullptr, eri_kernel_22, eri_kernel_23, eri_kernel_24, eri_kernel_25},
+        {nullptr, nullptr, nullptr, eri_kernel_33, eri_kernel_34, eri_kernel_35},
+        {nullptr, nullptr, nullptr, nullptr, eri_kernel_44, eri_kernel_45},
+        {nullptr, nullptr, nullptr, nullptr, nullptr, eri_kernel_55}};
+    KernelFn f = table[tb][tk] ? table[tb][tk](mode) : nullptr;
+    HF_CHECK(f != nullptr, HFGPU_ERR_CUDA, "missing ERI kernel for class");
+    return f;
+}
+
+static int class_G(int tb, int tk)
+{
+    int nab = ncart(ptype_la(tb)) * ncart(ptype_lb(tb));
+    int ncd = ncart(ptype_la(tk)) * ncart(ptype_lb(tk));
+    return ncd / pick_ncd(nab, ncd);
+}
+
+// McMurchie-Davidson reference flop count of one primitive quartet:
+//   30 + 3L + 2 C(L+4,4) + 2 nc_c nc_d nH(Lp) nH(Lq) + 2 nc_a nc_b nc_c nc_d nH(Lp)
+double md_flops(int la, int lb, int lc, int ld)
+{
+    auto binom4 = [](int n) { return (double)n * (n - 1) * (n - 2) * (n - 3) / 24.0; };
+    int Lp = la + lb, Lq = lc + ld, L = Lp + Lq;
+    return 30 + 3.0 * L + 2 * binom4(L + 4) + 2.0 * ncart(lc) * ncart(ld) * nherm(Lp) * nherm(Lq) +
+           2.0 * ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) * nherm(Lp);
+}
+
+struct ClassPlan {
+    int tb, tk;
+    std::vector<Seg> segs;
+    int64_t nwarps = 0;
+    DBuf<Seg> dsegs;
+};
+
+struct EriPlan {
+    Basis basis;
+    int npair = 0;
+    // device basis
+    DBuf<int> sL, snp, sp0, sc0, scf, cfn;
+    DBuf<double> sxyz, alpha, coef;
+    // pairs
+    std::vector<int> pA, pB, pK, pT;
+    std::vector<int64_t> poff;
+    DBuf<int> dA, dB, dK;
+    DBuf<int64_t> doff;
+    DBuf<double> pdata;
+    // screening
+    std::vector<double> Q;
+    DBuf<int> gpairs;
+    DBuf<int64_t> prefix;
+    std::vector<ClassPlan> classes;
+    EriStats stats;
+    ShellDev shdev() const
+    {
+        return ShellDev{sL.p, snp.p, sxyz.p, sp0.p, sc0.p, scf.p, alpha.p, coef.p, cfn.p};
+    }
+    PairDev prdev() const { return PairDev{dA.p, dB.p, dK.p, doff.p, pdata.p}; }
+};
+
+static void launch_class(Context& ctx, EriPlan* P, ClassPlan& c, int mode, double* out, const int2* list)
+{
+    if (c.nwarps == 0) return;
+    EriArgs a;
+    a.sh = P->shdev();
+    a.pr = P->prdev();
+    a.boys = ctx.boys;
+    a.gpairs = P->gpairs.p;
+    a.prefix = P->prefix.p;
+    a.list = list;
+    a.segs = c.dsegs.p;
+    a.nseg = (int)c.segs.size();
+    a.nwarps = c.nwarps;
+    a.out = out;
+    int64_t blocks = (c.nwarps + ERI_BLOCK / 32 - 1) / (ERI_BLOCK / 32);
+    get_kernel(c.tb, c.tk, mode)<<<(unsigned)blocks, ERI_BLOCK, 0, ctx.stream>>>(a);
+    HF_CUDA(cudaGetLastError());
+}
+
+EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
+{
+    cudaStream_t st = ctx.stream;
+    auto P = new EriPlan();
+    try {
+        P->basis = b;
+        const int ns = (int)b.shells.size();
+        std::vector<int> L(ns), np(ns), p0(ns), c0(ns), f0(ns);
+        std::vector<double> xyz(3 * ns);
+        for (int s = 0; s < ns; s++) {
+            const Shell& sh = b.shells[s];
+            L[s] = sh.L; np[s] = sh.nprim; p0[s] = sh.prim0; c0[s] = sh.coef0; f0[s] = sh.cfn0;
+            xyz[3 * s] = sh.x; xyz[3 * s + 1] = sh.y; xyz[3 * s + 2] = sh.z;
+        }
+        P->sL = to_device(L, st); P->snp = to_device(np, st); P->sp0 = to_device(p0, st);
+        P->sc0 = to_device(c0, st); P->scf = to_device(f0, st); P->cfn = to_device(b.comp_fn, st);
+        P->sxyz = to_device(xyz, st); P->alpha = to_device(b.alpha, st); P->coef = to_device(b.coef, st);
+
+        // shell pairs, larger angular momentum first
+        int64_t off = 0;
+        std::vector<int4> items[NPTYPE];
+        for (int i = 0; i < ns; i++)
+            for (int j = 0; j <= i; j++) {
+                int A = i, B = j;
+                if (L[A] < L[B]) std::swap(A, B);
+                int t = ptype_of(L[A], L[B]);
+                int id = (int)P->pA.size();
+                P->pA.push_back(A); P->pB.push_back(B); P->pT.push_back(t);
+                P->pK.push_back(np[A] * np[B]);
+                P->poff.push_back(off);
+                for (int x = 0; x < np[A]; x++)
+                    for (int y = 0; y < np[B]; y++) items[t].push_back(make_int4(id, x, y, 0));
+                off += (int64_t)np[A] * np[B] * pair_stride(ptype_la(t), ptype_lb(t));
+            }
+        P->npair = (int)P->pA.size();
+        P->dA = to_device(P->pA, st); P->dB = to_device(P->pB, st); P->dK = to_device(P->pK, st);
+        P->doff = to_device(P->poff, st);
+        P->pdata.alloc(off, st);
+        for (int t = 0; t < NPTYPE; t++) {
+            if (items[t].empty()) continue;
+            DBuf<int4> di = to_device(items[t], st);
+            int n = (int)items[t].size();
+            int blocks = (n + 127) / 128;
+            ShellDev sd = P->shdev();
+            PairDev pd = P->prdev();
+            switch (t) {
+                case 0: pair_data_kernel<0><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); break;
+                case 1: pair_data_kernel<1><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); break;
+                case 2: pair_data_kernel<2><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); break;
+                case 3: pair_data_kernel<3><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); break;
+                case 4: pair_data_kernel<4><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); break;
+                case 5: pair_data_kernel<5><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); break;
+            }
+            HF_CUDA(cudaGetLastError());
+        }
+
+        // groups: (pair type, primitive count)
+        std::map<std::pair<int, int>, std::vector<int>> gmap;
+        for (int id = 0; id < P->npair; id++) gmap[{P->pT[id], P->pK[id]}].push_back(id);
+
+        // Schwarz bounds from the diagonal quartets (ab|ab)
+        P->Q.assign(P->npair, 1.0);
+        if (thr > 0) {
+            std::vector<int2> dl;
+            std::vector<ClassPlan> dcls;
+            for (auto& g : gmap) {
+                int t = g.first.first;
+                ClassPlan c;
+                c.tb = t; c.tk = t;
+                Seg s{};
+                s.warp0 = 0; s.nq = (int64_t)g.second.size(); s.pref0 = (int64_t)dl.size();
+                s.list = 1;
+                for (int id : g.second) dl.push_back(make_int2(id, id));
+                bool merged = false;
+                for (auto& dc : dcls)
+                    if (dc.tb == t) {
+                        s.warp0 = dc.nwarps;
+                        dc.segs.push_back(s);
+                        dc.nwarps += (s.nq + 31) / 32 * class_G(t, t);
+                        merged = true;
+                    }
+                if (!merged) {
+                    c.segs.push_back(s);
+                    c.nwarps = (s.nq + 31) / 32 * class_G(t, t);
+                    dcls.push_back(std::move(c));
+                }
+            }
+            DBuf<int2> ddl = to_device(dl, st);
+            DBuf<double> diag((size_t)P->npair * 36, st);
+            diag.zero();
+            for (auto& c : dcls) {
+                c.dsegs = to_device(c.segs, st);
+                launch_class(ctx, P, c, MODE_DIAG, diag.p, ddl.p);
+            }
+            std::vector<double> hd((size_t)P->npair * 36);
+            diag.download(hd.data(), hd.size());
+            HF_CUDA(cudaStreamSynchronize(st));
+            for (int id = 0; id < P->npair; id++) {
+                double m = 0;
+                for (int k = 0; k < 36; k++) m = std::max(m, std::fabs(hd[(size_t)id * 36 + k]));
+                P->Q[id] = std::sqrt(m);
+            }
+            for (auto& g : gmap)
+                std::stable_sort(g.second.begin(), g.second.end(),
+                                 [&](int x, int y) { return P->Q[x] > P->Q[y]; });
+        }
+
+        // flatten the groups
+        std::vector<int> gp;
+        struct G { int t, k, off, n; std::vector<double> q; std::vector<int64_t> eff; };
+        std::vector<G> groups;
+        for (auto& g : gmap) {
+            G gg{g.first.first, g.first.second, (int)gp.size(), (int)g.second.size(), {}, {}};
+            gg.eff.push_back(0);
+            for (int id : g.second) {
+                gp.push_back(id);
+                gg.q.push_back(P->Q[id]);
+                int A = P->pA[id], B = P->pB[id];
+                int64_t na = 0, nb = 0;
+                for (int c = 0; c < ncart(L[A]); c++) na += b.comp_fn[f0[A] + c] >= 0;
+                for (int c = 0; c < ncart(L[B]); c++) nb += b.comp_fn[f0[B] + c] >= 0;
+                int64_t e = (A == B) ? na * (na + 1) / 2 : na * nb;
+                gg.eff.push_back(gg.eff.back() + e);
+            }
+            groups.push_back(std::move(gg));
+        }
+        P->gpairs = to_device(gp, st);
+
+        // segments per class
+        std::vector<int64_t> prefix;
+        EriStats stt;
+        for (int tb = 0; tb < NPTYPE; tb++)
+            for (int tk = tb; tk < NPTYPE; tk++) {
+                ClassPlan c;
+                c.tb = tb; c.tk = tk;
+                int G_ = class_G(tb, tk);
+                double fl = md_flops(ptype_la(tb), ptype_lb(tb), ptype_la(tk), ptype_lb(tk));
+                for (size_t g1 = 0; g1 < groups.size(); g1++) {
+                    if (groups[g1].t != tb) continue;
+                    for (size_t g2 = 0; g2 < groups.size(); g2++) {
+                        if (groups[g2].t != tk) continue;
+                        if (tb == tk && g2 < g1) continue;
+                        const G& A_ = groups[g1];
+                        const G& B_ = groups[g2];
+                        bool same = g1 == g2;
+                        Seg s{};
+                        s.pref0 = (int64_t)prefix.size();
+                        s.bra0 = A_.off; s.ket0 = B_.off; s.nbra = A_.n; s.list = 0;
+                        int64_t acc = 0, nbf = 0;
+                        prefix.push_back(0);
+                        for (int i = 0; i < A_.n; i++) {
+                            int64_t cnt;
+                            if (thr > 0) {
+                                double need = A_.q[i] > 0 ? thr / A_.q[i] : INFINITY;
+                                // number of leading kets with q >= need (q sorted descending)
+                                cnt = std::upper_bound(B_.q.begin(), B_.q.end(), need,
+                                                       [](double v, double e) { return v > e; }) -
+                                      B_.q.begin();
+                            } else {
+                                cnt = B_.n;
+                            }
+                            if (same) cnt = std::min<int64_t>(cnt, i + 1);
+                            acc += cnt;
+                            prefix.push_back(acc);
+                            int64_t ei = A_.eff[i + 1] - A_.eff[i];
+                            int64_t sum = B_.eff[cnt];
+                            nbf += ei * sum;
+                            if (same && cnt == i + 1) nbf -= ei * ei - ei * (ei + 1) / 2;
+                        }
+                        if (acc == 0) {
+                            prefix.resize(s.pref0);
+                            continue;
+                        }
+                        s.nq = acc;
+                        s.warp0 = c.nwarps;
+                        c.nwarps += (acc + 31) / 32 * G_;
+                        c.segs.push_back(s);
+                        stt.n_quartets += acc;
+                        stt.n_bf_quartets += nbf;
+                        stt.n_prim_quartets += acc * A_.k * B_.k;
+                        stt.flops += (double)acc * A_.k * B_.k * fl;
+                    }
+                }
+                if (!c.segs.empty()) {
+                    c.dsegs = to_device(c.segs, st);
+                    P->classes.push_back(std::move(c));
+                }
+            }
+        P->prefix = to_device(prefix, st);
+        P->stats = stt;
+        HF_CUDA(cudaStreamSynchronize(st));
+        return P;
+    } catch (...) {
+        delete P;
+        throw;
+    }
+}
+
+void eri_plan_destroy(EriPlan* p) { delete p; }
+EriStats eri_plan_stats(const EriPlan* p) { return p->stats; }
+
+void eri_compute_packed(Context& ctx, EriPlan* P, double* d_out, EriStats* st)
+{
+    cudaEvent_t e0, e1;
+    HF_CUDA(cudaEventCreate(&e0));
+    HF_CUDA(cudaEventCreate(&e1));
+    HF_CUDA(cudaEventRecord(e0, ctx.stream));
+    // heaviest classes first so the tail of the launch sequence is short
+    for (int i = (int)P->classes.size() - 1; i >= 0; --i)
+        launch_class(ctx, P, P->classes[i], MODE_PACKED, d_out, nullptr);
+    HF_CUDA(cudaEventRecord(e1, ctx.stream));
+    HF_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    HF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) {
+        *st = P->stats;
+        st->ms = ms;
+    }
+}
+
+}  // namespace hfgpu

@@ -1,0 +1,174 @@
+// Internal declarations shared by the libhfgpu translation units.
+#pragma once
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/hfgpu.h"
+
+namespace hfgpu {
+
+// ---------------------------------------------------------------- errors
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string& m);
+
+#define HF_CUDA(x)                                                                             \
+    do {                                                                                       \
+        cudaError_t e_ = (x);                                                                  \
+        if (e_ != cudaSuccess)                                                                 \
+            throw ::hfgpu::Error(e_ == cudaErrorMemoryAllocation ? HFGPU_ERR_NOMEM            \
+                                                                  : HFGPU_ERR_CUDA,           \
+                                 std::string(#x) + ": " + cudaGetErrorString(e_));             \
+    } while (0)
+#define HF_CUBLAS(x)                                                                           \
+    do {                                                                                       \
+        cublasStatus_t s_ = (x);                                                               \
+        if (s_ != CUBLAS_STATUS_SUCCESS)                                                       \
+            throw ::hfgpu::Error(HFGPU_ERR_CUDA, std::string(#x) + ": cublas status " +       \
+                                                     std::to_string((int)s_));                 \
+    } while (0)
+#define HF_CUSOLVER(x)                                                                         \
+    do {                                                                                       \
+        cusolverStatus_t s_ = (x);                                                             \
+        if (s_ != CUSOLVER_STATUS_SUCCESS)                                                     \
+            throw ::hfgpu::Error(HFGPU_ERR_CUDA, std::string(#x) + ": cusolver status " +     \
+                                                     std::to_string((int)s_));                 \
+    } while (0)
+#define HF_CHECK(cond, code, msg)                                                              \
+    do {                                                                                       \
+        if (!(cond)) throw ::hfgpu::Error(code, msg);                                          \
+    } while (0)
+
+// ---------------------------------------------------------------- device buffers
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaStream_t st = nullptr;
+    DBuf() = default;
+    DBuf(size_t count, cudaStream_t s) { alloc(count, s); }
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), st(o.st) { o.p = nullptr; o.n = 0; }
+    DBuf& operator=(DBuf&& o) noexcept
+    {
+        release();
+        p = o.p; n = o.n; st = o.st;
+        o.p = nullptr; o.n = 0;
+        return *this;
+    }
+    void alloc(size_t count, cudaStream_t s)
+    {
+        release();
+        st = s;
+        n = count;
+        if (count) HF_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), s));
+    }
+    void zero() { if (n) HF_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), st)); }
+    void upload(const T* h, size_t count)
+    {
+        if (count) HF_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
+    }
+    void upload(const std::vector<T>& v)
+    {
+        if (v.size() > n) alloc(v.size(), st);
+        upload(v.data(), v.size());
+    }
+    void download(T* h, size_t count) const
+    {
+        if (count) HF_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, st));
+    }
+    void release()
+    {
+        if (p) cudaFreeAsync(p, st);
+        p = nullptr;
+        n = 0;
+    }
+    ~DBuf() { release(); }
+};
+
+template <class T>
+DBuf<T> to_device(const std::vector<T>& v, cudaStream_t s)
+{
+    DBuf<T> b(v.size(), s);
+    b.upload(v.data(), v.size());
+    return b;
+}
+
+// ---------------------------------------------------------------- context
+// One per CUDA device, created on first use: stream, library handles and the
+// Boys-function grid.
+struct Context {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    cublasHandle_t blas = nullptr;
+    cusolverDnHandle_t solver = nullptr;
+    double* boys = nullptr;  // device copy of the Boys grid
+    int num_sms = 0;
+};
+Context& context();  // for the current device
+
+// ---------------------------------------------------------------- basis
+// A shell: all Cartesian components of one angular momentum on one centre with
+// shared exponents.  comp_fn maps each component to its basis-function index,
+// or -1 for a component that the caller's function list does not contain.
+struct Shell {
+    int L = 0, nprim = 0;
+    double x = 0, y = 0, z = 0;
+    int prim0 = 0;   // offset of the exponents in Basis::alpha
+    int coef0 = 0;   // offset of the ncart(L) x nprim coefficient block (component-major)
+    int cfn0 = 0;    // offset in Basis::comp_fn
+};
+
+struct Basis {
+    int nbf = 0;
+    std::vector<Shell> shells;
+    std::vector<double> alpha, coef;
+    std::vector<int> comp_fn;
+    int max_l() const;
+};
+
+// hfsolver's 6-31G** Cartesian basis for the given atoms (src/basis.f90:275-488)
+Basis build_basis(int natoms, const int* atno, const double* xyz);
+// group a reference-style function list (qc.h arguments) into shells
+Basis basis_from_functions(int nbf, const int* nprim, const int* istart, const double* xc,
+                           const double* yc, const double* zc, const int* lp, const int* mp,
+                           const int* np, int n2, const double* coef, const double* alpha);
+int basis_size(int natoms, const int* atno);
+
+// ---------------------------------------------------------------- integrals
+struct EriStats {
+    int64_t n_quartets = 0, n_bf_quartets = 0, n_prim_quartets = 0;
+    double flops = 0;
+    double ms = 0;
+};
+
+class EriEngine;  // eri.cu
+
+// Device-side basis + shell pairs + screened quartet segments for one molecule.
+struct EriPlan;
+EriPlan* eri_plan_create(Context& ctx, const Basis& b, double schwarz);
+void eri_plan_destroy(EriPlan* p);
+EriStats eri_plan_stats(const EriPlan* p);
+// all unique (ij|kl) into the packed array d_out (device, zeroed by the caller)
+void eri_compute_packed(Context& ctx, EriPlan* p, double* d_out, EriStats* st);
+
+// one-electron integrals (onee.cu): S, T, V on the device (n x n, symmetric)
+void onee_compute(Context& ctx, const Basis& b, int natoms, const int* atno, const double* x,
+                  const double* y, const double* z, double* dS, double* dT, double* dV);
+
+// J/K (jk.cu): G = J - K/2 from packed integrals and density P (device)
+void jk_from_packed(Context& ctx, int n, const double* d_int2, const double* dP, double* dG);
+
+int64_t packed_size(int64_t n);
+
+}  // namespace hfgpu

@@ -1,0 +1,242 @@
+// Closed-shell RHF SCF loop on the GPU.
+//
+// Follows doscf (src/scf.f90:72-136): P = 0 start, F = H + G(P),
+// E0 = sum P (H + F) / 2, generalised eigenproblem F C = S C lam solved with
+// the same LAPACK routine the reference calls (dsygvd, lower triangle,
+// src/linalg.f90:241-280; here cuSOLVER's device implementation),
+// P = 2 C_occ C_occ^T (formP, :12-24), dP = sqrt(sum (P - Pold)^2 / 4),
+// convergence from the 4th iteration when dP < tolP and the last four energies
+// span less than tolE, otherwise linear mixing P = (1-alpha) Pold + alpha P.
+// Optionally Pulay's DIIS (commutator error F P S - S P F) extrapolates F
+// instead of mixing P.  Everything stays on the device; each iteration reads
+// back two scalars (E0, dP) for the convergence test.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+#include "scf.h"
+
+namespace hfgpu {
+
+__global__ void add_kernel(int64_t nn, const double* __restrict__ A, const double* __restrict__ B, double* C)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nn) C[i] = A[i] + B[i];
+}
+
+__global__ void mix_kernel(int64_t nn, double alpha, const double* __restrict__ Pold, double* P)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nn) P[i] = (1 - alpha) * Pold[i] + alpha * P[i];
+}
+
+__global__ void comm_kernel(int n, const double* __restrict__ Y, double* E)
+{
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * n) return;
+    int i = idx % n, j = idx / n;
+    E[idx] = Y[idx] - Y[j + (int64_t)i * n];
+}
+
+// Deterministic single-block reductions (n^2 <= a few 1e5 elements).
+// mode 0: sum A*(B+C)/2, mode 1: sqrt(sum (A-B)^2 / 4), mode 2: sum A*B
+__global__ void reduce_kernel(int mode, int64_t nn, const double* __restrict__ A, const double* __restrict__ B,
+                              const double* __restrict__ C, double* out)
+{
+    __shared__ double sh[1024];
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < nn; i += blockDim.x) {
+        if (mode == 0)
+            s += A[i] * (B[i] + C[i]);
+        else if (mode == 1)
+            s += (A[i] - B[i]) * (A[i] - B[i]);
+        else
+            s += A[i] * B[i];
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double r = sh[0];
+        if (mode == 0) r *= 0.5;
+        if (mode == 1) r = sqrt(r / 4);
+        *out = r;
+    }
+}
+
+static void reduce(Context& ctx, int mode, int64_t nn, const double* A, const double* B, const double* C,
+                   double* dout)
+{
+    reduce_kernel<<<1, 1024, 0, ctx.stream>>>(mode, nn, A, B, C, dout);
+    HF_CUDA(cudaGetLastError());
+}
+
+static unsigned nblk(int64_t n) { return (unsigned)((n + 255) / 256); }
+
+// P = 2 C_occ C_occ^T
+static void form_density(Context& ctx, int n, int nocc, const double* C, double* P)
+{
+    const double two = 2.0, zero = 0.0;
+    if (nocc == 0) {
+        HF_CUDA(cudaMemsetAsync(P, 0, sizeof(double) * n * n, ctx.stream));
+        return;
+    }
+    HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, nocc, &two, C, n, C, n, &zero, P, n));
+}
+
+// small dense solve with partial pivoting (DIIS system, size <= 21)
+static bool solve_small(std::vector<double>& A, std::vector<double>& b, int m)
+{
+    for (int c = 0; c < m; c++) {
+        int piv = c;
+        for (int r = c + 1; r < m; r++)
+            if (std::fabs(A[r * m + c]) > std::fabs(A[piv * m + c])) piv = r;
+        if (std::fabs(A[piv * m + c]) < 1e-300) return false;
+        if (piv != c) {
+            for (int k = 0; k < m; k++) std::swap(A[c * m + k], A[piv * m + k]);
+            std::swap(b[c], b[piv]);
+        }
+        for (int r = c + 1; r < m; r++) {
+            double f = A[r * m + c] / A[c * m + c];
+            for (int k = c; k < m; k++) A[r * m + k] -= f * A[c * m + k];
+            b[r] -= f * b[c];
+        }
+    }
+    for (int c = m - 1; c >= 0; c--) {
+        double s = b[c];
+        for (int k = c + 1; k < m; k++) s -= A[c * m + k] * b[k];
+        b[c] = s / A[c * m + c];
+    }
+    return true;
+}
+
+ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dLam)
+{
+    cudaStream_t st = ctx.stream;
+    const int n = in.n;
+    const int64_t nn = (int64_t)n * n;
+    HF_CHECK(in.nocc >= 0 && in.nocc <= n, HFGPU_ERR_INVALID, "nocc out of range");
+    DBuf<double> G(nn, st), F(nn, st), Fw(nn, st), Sw(nn, st), Pold(nn, st), scal(4, st);
+    DBuf<int> info(1, st);
+    HF_CUDA(cudaMemsetAsync(dP, 0, sizeof(double) * nn, st));
+    int lwork = 0;
+    HF_CUSOLVER(cusolverDnDsygvd_bufferSize(ctx.solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                                            CUBLAS_FILL_MODE_LOWER, n, Fw.p, n, Sw.p, n, dLam, &lwork));
+    DBuf<double> work(std::max(lwork, 1), st);
+
+    const bool diis = in.accel == HFGPU_SCF_DIIS;
+    const int nd = std::max(2, std::min(in.diis_size, 20));
+    DBuf<double> Fh, Eh, Y, bvec;
+    if (diis) {
+        Fh.alloc((size_t)nd * nn, st);
+        Eh.alloc((size_t)nd * nn, st);
+        Y.alloc(nn, st);
+        bvec.alloc(nd, st);
+    }
+    std::vector<double> B((size_t)nd * nd, 0.0);
+    int nhist = 0, head = 0;
+
+    std::vector<double> Escf;
+    ScfOut out;
+    for (int it = 1; it <= in.nscf; ++it) {
+        if (in.direct_jk)
+            in.direct_jk(ctx, in.direct_ctx, dP, G.p);
+        else
+            jk_from_packed(ctx, n, in.d_int2, dP, G.p);
+        add_kernel<<<nblk(nn), 256, 0, st>>>(nn, in.dH, G.p, F.p);
+        reduce(ctx, 0, nn, dP, in.dH, F.p, scal.p);  // E0
+        const double* Fsolve = F.p;
+        if (diis) {
+            const double one = 1.0, zero = 0.0;
+            // error = F P S - S P F = Y - Y^T with Y = F P S
+            HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, F.p, n, dP, n, &zero, G.p, n));
+            HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, G.p, n, in.dS, n, &zero, Y.p, n));
+            double* ek = Eh.p + (size_t)head * nn;
+            comm_kernel<<<nblk(nn), 256, 0, st>>>(n, Y.p, ek);
+            HF_CUDA(cudaMemcpyAsync(Fh.p + (size_t)head * nn, F.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+            nhist = std::min(nhist + 1, nd);
+            // new row of B: <e_k, e_head>
+            HF_CUBLAS(cublasDgemv(ctx.blas, CUBLAS_OP_T, (int)nn, nd, &one, Eh.p, (int)nn, ek, 1, &zero, bvec.p, 1));
+            std::vector<double> row(nd);
+            bvec.download(row.data(), nd);
+            HF_CUDA(cudaStreamSynchronize(st));
+            for (int k = 0; k < nhist; k++) {
+                B[(size_t)head * nd + k] = row[k];
+                B[(size_t)k * nd + head] = row[k];
+            }
+            if (nhist >= 2) {
+                int m = nhist + 1;
+                std::vector<double> A((size_t)m * m, 0.0), rhs(m, 0.0);
+                double scale = 0;
+                for (int a = 0; a < nhist; a++) scale = std::max(scale, std::fabs(B[(size_t)a * nd + a]));
+                if (scale <= 0) scale = 1;
+                for (int a = 0; a < nhist; a++) {
+                    for (int b = 0; b < nhist; b++) A[(size_t)a * m + b] = B[(size_t)a * nd + b] / scale;
+                    A[(size_t)a * m + nhist] = -1;
+                    A[(size_t)nhist * m + a] = -1;
+                }
+                rhs[nhist] = -1;
+                if (solve_small(A, rhs, m)) {
+                    std::vector<double> c(nd, 0.0);
+                    for (int a = 0; a < nhist; a++) c[a] = rhs[a];
+                    bvec.upload(c.data(), nd);
+                    HF_CUBLAS(cublasDgemv(ctx.blas, CUBLAS_OP_N, (int)nn, nhist, &one, Fh.p, (int)nn, bvec.p, 1,
+                                          &zero, Y.p, 1));
+                    Fsolve = Y.p;
+                }
+            }
+            head = (head + 1) % nd;
+        }
+        HF_CUDA(cudaMemcpyAsync(Fw.p, Fsolve, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+        HF_CUDA(cudaMemcpyAsync(Sw.p, in.dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+        HF_CUSOLVER(cusolverDnDsygvd(ctx.solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                                     CUBLAS_FILL_MODE_LOWER, n, Fw.p, n, Sw.p, n, dLam, work.p, lwork, info.p));
+        HF_CUDA(cudaMemcpyAsync(Pold.p, dP, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+        form_density(ctx, n, in.nocc, Fw.p, dP);
+        reduce(ctx, 1, nn, dP, Pold.p, nullptr, scal.p + 1);  // dP
+        double h[2];
+        int hinfo = 0;
+        scal.download(h, 2);
+        info.download(&hinfo, 1);
+        HF_CUDA(cudaStreamSynchronize(st));
+        HF_CHECK(hinfo == 0, HFGPU_ERR_LINALG,
+                 "eigh: dsygvd returned info = " + std::to_string(hinfo) +
+                     (hinfo > n ? " (S is not positive definite)" : ""));
+        const double E0 = h[0], dPv = h[1];
+        Escf.push_back(E0);
+        out.E0 = E0;
+        out.dP = dPv;
+        out.niter = it;
+        if (it > 3) {
+            double emax = *std::max_element(Escf.end() - 4, Escf.end());
+            double emin = *std::min_element(Escf.end() - 4, Escf.end());
+            if (dPv < in.tolP && emax - emin < in.tolE) {
+                HF_CUDA(cudaMemcpyAsync(dC, Fw.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+                HF_CUDA(cudaStreamSynchronize(st));
+                out.converged = true;
+                return out;
+            }
+        }
+        if (!diis && in.alpha != 1.0) mix_kernel<<<nblk(nn), 256, 0, st>>>(nn, in.alpha, Pold.p, dP);
+    }
+    HF_CUDA(cudaMemcpyAsync(dC, Fw.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+    HF_CUDA(cudaStreamSynchronize(st));
+    out.converged = false;
+    return out;
+}
+
+double device_dot(Context& ctx, int64_t nn, const double* A, const double* B)
+{
+    DBuf<double> s(1, ctx.stream);
+    reduce(ctx, 2, nn, A, B, nullptr, s.p);
+    double h = 0;
+    s.download(&h, 1);
+    HF_CUDA(cudaStreamSynchronize(ctx.stream));
+    return h;
+}
+
+}  // namespace hfgpu

@@ -1,0 +1,45 @@
+// SCF driver interface (scf.cu) and the MP2 stage (mp2.cu).
+#pragma once
+#include "internal.h"
+
+namespace hfgpu {
+
+using DirectJK = void (*)(Context& ctx, void* user, const double* dP, double* dG);
+
+struct ScfIn {
+    int n = 0, nocc = 0, nscf = 40;
+    const double* dH = nullptr;
+    const double* dS = nullptr;
+    const double* d_int2 = nullptr;  // packed integrals (in-core Fock build)
+    DirectJK direct_jk = nullptr;    // or: integral-direct Fock build
+    void* direct_ctx = nullptr;
+    double tolE = 1e-10, tolP = 1e-8, alpha = 1.0;
+    int accel = HFGPU_SCF_MIXING;
+    int diis_size = 8;
+};
+
+struct ScfOut {
+    double E0 = 0, dP = 0;
+    int niter = 0;
+    bool converged = false;
+};
+
+ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dLam);
+double device_dot(Context& ctx, int64_t nn, const double* A, const double* B);
+
+// (i a | j b) for i, j over the n1 columns of C1 and a, b over the n2 columns
+// of C2 (both n x n1 / n x n2, column-major, leading dimension n), from the
+// packed AO integrals.  Output layout [i][a][j][b].
+void ao2mo_fp64(Context& ctx, int n, const double* d_int2, const double* dC1, int n1, const double* dC2, int n2,
+                double* d_out);
+// E2 from (ia|jb) in [i][a][j][b] layout and orbital energies (device)
+double mp2_energy(Context& ctx, int nocc, int nvir, const double* d_iajb, const double* d_eps);
+
+}  // namespace hfgpu
+
+namespace hfgpu {
+// full (ij|kl) over all orbitals into the packed layout (transform_int2 drop-in)
+void transform_packed(Context& ctx, int n, const double* d_int2, const double* dC, double* d_mo);
+// term1 of src/mbpt2.f90 on packed MO integrals (mbpt2 drop-in)
+double mbpt2_packed(Context& ctx, int n, const double* d_mo, const double* d_lam, int nocc);
+}  // namespace hfgpu

@@ -1,0 +1,149 @@
+/*
+ * hfgpu — GB300-native (sm_103a) kernels for hfsolver's molecular
+ * Gaussian-orbital path: contracted electron-repulsion integrals, the RHF Fock
+ * build, the AO->MO transform and the MBPT2 energy.
+ *
+ * C ABI.  Plain pointers and sizes; every entry point returns an int status
+ * (HFGPU_OK = 0) instead of aborting the process the way the reference's
+ * stop_error does, and hfgpu_last_error() gives the message of the last
+ * failure on the calling thread.  All arrays are host memory owned by the
+ * caller, as in the reference (the callee only writes outputs); device memory
+ * is managed inside the library on the current CUDA device, and each call
+ * returns after its results are in the caller's buffers.
+ *
+ * Matrices are column-major n x n, like the Fortran arrays they replace.
+ * Packed two-electron arrays use hfsolver's 8-fold index
+ * (src/cints.c:327-347 and src/scf.f90:184-223) with 64-bit positions:
+ * (ij|kl) with i>=j, k>=l, ij>=kl, ij = i(i+1)/2+j, lives at ij(ij+1)/2+kl
+ * (0-based); its length is m(m+1)/2 with m = n(n+1)/2.
+ */
+#ifndef HFGPU_H
+#define HFGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    HFGPU_OK = 0,
+    HFGPU_ERR_INVALID = 1,        /* bad argument: sizes, NaN coordinates, unknown Z */
+    HFGPU_ERR_CUDA = 2,           /* CUDA, cuBLAS or cuSOLVER failure */
+    HFGPU_ERR_NOT_CONVERGED = 3,  /* SCF did not converge in nscf iterations */
+    HFGPU_ERR_LINALG = 4,         /* eigensolver failure (S not positive definite) */
+    HFGPU_ERR_UNSUPPORTED = 5,    /* angular momentum beyond d, or similar */
+    HFGPU_ERR_NOMEM = 6,          /* device memory exhausted */
+    HFGPU_ERR_NO_DEVICE = 7       /* no CUDA device */
+};
+
+const char *hfgpu_last_error(void);
+int hfgpu_version(void);
+
+/* ---- Integral drivers: same arguments as hfsolver's C drivers --------------
+ * nbf functions; function i has nprim[i] primitives starting at the 0-based
+ * offset istart[i] in coef/alpha (n2 entries), centre (xcenter[i], ycenter[i],
+ * zcenter[i]) and Cartesian powers (lpower[i], mpower[i], npower[i]); coef
+ * already includes primitive and contraction normalisation. */
+
+/* replaces getS, src/qc.h:8-12 / src/qc.c:6-31 (S column-major nbf x nbf) */
+int hfgpu_getS(int nbf, const int *nprim, const int *istart, const double *xcenter,
+               const double *ycenter, const double *zcenter, const int *lpower, const int *mpower,
+               const int *npower, int n2, const double *coef, const double *alpha, double *S);
+
+/* replaces getT, src/qc.h:14-18 / src/qc.c:33-58 */
+int hfgpu_getT(int nbf, const int *nprim, const int *istart, const double *xcenter,
+               const double *ycenter, const double *zcenter, const int *lpower, const int *mpower,
+               const int *npower, int n2, const double *coef, const double *alpha, double *T);
+
+/* replaces getV, src/qc.h:20-25 / src/qc.c:61-93 (nat nuclei of charge atno at x, y, z) */
+int hfgpu_getV(int nbf, const int *nprim, const int *istart, const double *xcenter,
+               const double *ycenter, const double *zcenter, const int *lpower, const int *mpower,
+               const int *npower, int n2, const double *coef, const double *alpha, int nat,
+               const int *atno, const double *x, const double *y, const double *z, double *V);
+
+/* replaces getInts, src/qc.h:27-31 / src/qc.c:95-131: every unique (ij|kl) into
+ * the packed array Ints (length m(m+1)/2, 64-bit positions).  No screening:
+ * every quartet is computed, as in the reference. */
+int hfgpu_getInts(int nbf, const int *nprim, const int *istart, const double *xcenter,
+                  const double *ycenter, const double *zcenter, const int *lpower,
+                  const int *mpower, const int *npower, int n2, const double *coef,
+                  const double *alpha, double *Ints);
+
+/* replaces the plugin routine getints2 of module gaussians,
+ * src/gaussians_hfsolver.f90:13-34 (called from src/basis.f90:567): Fortran
+ * layout center(3,n), power(3,n), 1-based istart; nint2 is the length of int2
+ * and must equal m(m+1)/2. */
+int hfgpu_getints2(int n, const int *nprim, const int *istart, const double *center,
+                   const int *power, int n2, const double *coef, const double *alpha,
+                   double *int2, int64_t nint2);
+
+/* ---- SCF, transform, MBPT2 ------------------------------------------------ */
+
+/* replaces doscf, src/scf.f90:72-136: P = 0 start, F = H + G(P) with
+ * G(i,j) = sum_kl P(k,l) [(ij|kl) - (il|kj)/2] from the packed int2, generalised
+ * eigenproblem F C = S C lam, P = 2 C_occ C_occ^T, convergence when
+ * sqrt(sum (P - Pold)^2 / 4) < tolP and the last four energies span < tolE
+ * (checked from iteration 4), else linear mixing P = (1-alpha) Pold + alpha P.
+ * Outputs C (n x n), P (n x n), lam (n), E0 (electronic energy of the last
+ * iteration) and the iteration count; HFGPU_ERR_NOT_CONVERGED after nscf. */
+int hfgpu_doscf(int n, const double *H, const double *int2, const double *S, int nocc, int nscf,
+                double tolE, double tolP, double alpha, double *C, double *P, double *lam,
+                double *E0, int *niter);
+
+/* replaces transform_int2, src/mbpt.f90:11-79: (mu nu|la si) -> (ij|kl) over
+ * all orbitals, both arrays packed.  FP64. */
+int hfgpu_transform_int2(int n, const double *int2, const double *C, double *moint2);
+
+/* replaces mbpt2, src/mbpt.f90:154-159 (term1, src/mbpt2.f90:8-31):
+ * E2 = sum_{a,b<nocc; r,s>=nocc} [2 (ar|bs)^2 - (ar|bs)(as|br)] / (lam_a+lam_b-lam_r-lam_s)
+ * from the packed MO integrals. */
+int hfgpu_mbpt2(int n, const double *moint2, const double *lam, int nocc, double *E2);
+
+/* ---- Whole pipeline: rhf_gauss (src/drivers.f90:12-51) + MBPT2 ------------ */
+
+enum { HFGPU_MP2_NONE = 0, HFGPU_MP2_FP64 = 1, HFGPU_MP2_SPLIT_BF16 = 2 };
+enum { HFGPU_SCF_MIXING = 0, HFGPU_SCF_DIIS = 1 };
+
+typedef struct {
+    int nscf;            /* iteration cap (reference tests: 40) */
+    double mix_alpha;    /* linear mixing factor (reference: 1.0, CO: 0.8) */
+    double tolE;         /* energy-window tolerance (reference tests: 1e-10) */
+    double tolP;         /* density-change tolerance (reference tests: 1e-8) */
+    int scf_accel;       /* HFGPU_SCF_MIXING (reference algorithm) or HFGPU_SCF_DIIS */
+    int diis_size;       /* DIIS history length */
+    double schwarz;      /* quartet cut on sqrt((ab|ab)(cd|cd)); 0 = none (reference) */
+    int mp2;             /* HFGPU_MP2_* */
+    int mp2_nocc;        /* occupied orbitals passed to MBPT2; <= 0: sum(Z)/2 */
+    int reserved[8];
+} hfgpu_options;
+
+typedef struct {
+    double Etot, E0, Enuc, Ekin, E2;
+    double dP;               /* density change of the last iteration */
+    int niter, nbf, nocc, nshell;
+    int64_t n_quartets;      /* contracted shell quartets evaluated */
+    int64_t n_bf_quartets;   /* unique contracted basis-function quartets evaluated */
+    int64_t n_prim_quartets; /* primitive shell quartets evaluated */
+    double eri_flops;        /* McMurchie-Davidson reference flop count of those */
+    double ms_eri, ms_scf, ms_mp2, ms_total; /* device time of each stage */
+    double reserved[8];
+} hfgpu_result;
+
+void hfgpu_default_options(hfgpu_options *opt);
+
+/* natoms nuclei with charges atno at xyz (3 x natoms, bohr, column-major like
+ * the reference's xyz(3, :)); 6-31G** Cartesian basis as hfsolver builds it
+ * (src/basis.f90:143-569).  C (nbf x nbf) and lam (nbf) may be NULL; when
+ * given they must hold nbf*nbf and nbf doubles (nbf from hfgpu_basis_size). */
+int hfgpu_rhf(int natoms, const int *atno, const double *xyz, const hfgpu_options *opt,
+              hfgpu_result *res, double *C, double *lam);
+
+/* number of basis functions hfgpu_rhf will use for these atoms (0 on error) */
+int hfgpu_basis_size(int natoms, const int *atno);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HFGPU_H */

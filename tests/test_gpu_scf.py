@@ -1,0 +1,104 @@
+"""GPU RHF / transform / MBPT2 against the oracle and the reference's own
+known answers.  Tolerances: E_HF 1e-10 Ha and E_MP2 1e-8 Ha against the
+oracle on the same inputs; the reference's tolerances (1e-7 .. 1e-10) against
+its asserted values."""
+import numpy as np
+import pytest
+
+import hfsolver_gb300 as hf
+from tests.golden_reference_answers import CASES
+from tests.gpu_common import assert_close
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_rhf_reference_known_answers(oracle, name):
+    c = CASES[name]
+    atno, xyz = c["atno"], np.array(c["xyz"], float)
+    o = hf.RHFOptions(nscf=40, mix_alpha=c["alpha"], tolE=1e-10, tolP=1e-8, mp2="fp64",
+                      mp2_nocc=c["nocc_mp2"] or 0)
+    r = hf.rhf(atno, xyz, o, want_orbitals=True)
+    val, tol, _ = c["etot"]
+    assert abs(r["Etot"] - val) < tol
+    for idx, v, t, _ in c["lam"]:
+        assert abs(r["lam"][idx] - v) < t
+    if "e2" in c:
+        val, tol, _ = c["e2"]
+        assert abs(r["E2"] - val) < tol
+    # the same algorithm as the oracle, step for step: same iteration count
+    ref = oracle.rhf_gauss(atno, xyz, nscf=40, alpha=c["alpha"], tolE=1e-10, tolP=1e-8)
+    assert r["niter"] == ref["niter"]
+    assert abs(r["Etot"] - ref["Etot"]) < 1e-10
+
+
+def test_single_water_config(oracle):
+    """One H2O (0.9572 A, 104.52 deg), 6-31G**, RHF to dP < 1e-10, then MBPT2."""
+    from hfsolver_gb300.clusters import water
+
+    atno, xyz = water()
+    r = hf.rhf(atno, xyz, hf.RHFOptions(tolP=1e-10, tolE=1e-12))
+    ref = oracle.rhf_gauss(atno, xyz, nscf=40, tolE=1e-12, tolP=1e-10)
+    e2 = oracle.mbpt2(oracle.transform_int2(ref["int2"], ref["C"]), ref["lam"], 5)
+    assert abs(r["Etot"] - ref["Etot"]) < 1e-10
+    assert abs(r["E2"] - e2) < 1e-8
+    assert r["nbf"] == 25 and r["nocc"] == 5
+
+
+def test_doscf_dropin(oracle):
+    c = CASES["H2O"]
+    ref = oracle.rhf_gauss(c["atno"], np.array(c["xyz"], float))
+    C, P, lam, E0, it = hf.doscf(ref["H"], ref["int2"], ref["S"], 5, 40, 1e-10, 1e-8, 1.0)
+    assert it == ref["niter"]
+    assert abs(E0 - ref["E0"]) < 1e-10
+    assert_close(lam, ref["lam"], 1e-9, 0, "lam")
+    assert_close(P, ref["P"], 1e-8, 0, "P")
+
+
+def test_doscf_nonconvergence_is_reported(oracle):
+    c = CASES["H2O"]
+    ref = oracle.rhf_gauss(c["atno"], np.array(c["xyz"], float))
+    with pytest.raises(hf.SCFNotConverged):
+        hf.doscf(ref["H"], ref["int2"], ref["S"], 5, 3, 1e-10, 1e-8, 1.0)
+
+
+def test_transform_and_mbpt2_dropins(oracle):
+    c = CASES["CH4_1"]
+    ref = oracle.rhf_gauss(c["atno"], np.array(c["xyz"], float))
+    mo_ref = oracle.transform_int2(ref["int2"], ref["C"])
+    mo = hf.transform_int2(ref["int2"], ref["C"])
+    assert_close(mo, mo_ref, 1e-11, 1e-11, "moint2")
+    e2_ref = oracle.mbpt2(mo_ref, ref["lam"], 5)
+    assert abs(hf.mbpt2(mo_ref, ref["lam"], 5) - e2_ref) < 1e-12
+    assert abs(e2_ref - (-0.16815509)) < 1e-7  # test_gaussians_molecules.f90:114
+
+
+def test_diis_reaches_the_same_solution(oracle):
+    from hfsolver_gb300.clusters import water_cluster
+
+    atno, xyz = water_cluster(2, seed=11)
+    o = dict(tolP=1e-10, tolE=1e-12)
+    mix = hf.rhf(atno, xyz, hf.RHFOptions(nscf=100, **o))
+    diis = hf.rhf(atno, xyz, hf.RHFOptions(diis=True, **o))
+    assert diis["niter"] < mix["niter"]
+    assert abs(mix["Etot"] - diis["Etot"]) < 1e-10
+    assert abs(mix["E2"] - diis["E2"]) < 1e-9
+
+
+def test_water_dimer_against_oracle(oracle):
+    from hfsolver_gb300.clusters import water_cluster
+
+    atno, xyz = water_cluster(2, seed=3)
+    r = hf.rhf(atno, xyz, hf.RHFOptions(diis=True, tolP=1e-10, tolE=1e-12))
+    ref = oracle.rhf_gauss(atno, xyz, nscf=100, tolE=1e-12, tolP=1e-10)
+    e2 = oracle.mp2_semidirect(ref["int2"], ref["C"], ref["lam"], 10)
+    assert abs(r["Etot"] - ref["Etot"]) < 1e-10
+    assert abs(r["E2"] - e2) < 1e-8
+
+
+def test_gpu_errors_are_statuses():
+    from hfsolver_gb300.clusters import water
+
+    atno, xyz = water()
+    with pytest.raises(hf.SCFNotConverged):
+        hf.rhf(atno, xyz, hf.RHFOptions(nscf=2))
