@@ -32,8 +32,8 @@ class Result(ctypes.Structure):
                 ("nshell", ctypes.c_int), ("n_quartets", ctypes.c_int64),
                 ("n_bf_quartets", ctypes.c_int64), ("n_prim_quartets", ctypes.c_int64),
                 ("eri_flops", ctypes.c_double), ("ms_eri", ctypes.c_double), ("ms_scf", ctypes.c_double),
-                ("ms_mp2", ctypes.c_double), ("ms_total", ctypes.c_double),
-                ("reserved", ctypes.c_double * 8)]
+                ("ms_mp2", ctypes.c_double), ("ms_total", ctypes.c_double), ("ms_setup", ctypes.c_double),
+                ("reserved", ctypes.c_double * 7)]
 
 
 # name -> (restype, argtypes); the list every test of the ABI checks against
@@ -41,6 +41,9 @@ _BASIS = [ctypes.c_int, _ip, _ip, _dp, _dp, _dp, _ip, _ip, _ip, ctypes.c_int, _d
 SIGNATURES = {
     "hfgpu_last_error": (ctypes.c_char_p, []),
     "hfgpu_version": (ctypes.c_int, []),
+    "hfgpu_set_stream": (ctypes.c_int, [ctypes.c_void_p]),
+    "hfgpu_kernel_launches": (ctypes.c_int64, []),
+    "hfgpu_probe_fp64_tflops": (ctypes.c_int, [_dp]),
     "hfgpu_getS": (ctypes.c_int, _BASIS + [_dp]),
     "hfgpu_getT": (ctypes.c_int, _BASIS + [_dp]),
     "hfgpu_getV": (ctypes.c_int, _BASIS + [ctypes.c_int, _ip, _dp, _dp, _dp, _dp]),

@@ -221,6 +221,24 @@ int hfgpu_mbpt2(int n, const double* moint2, const double* lam, int nocc, double
     });
 }
 
+int hfgpu_set_stream(void* stream)
+{
+    return guard([&] {
+        Context& ctx = context();
+        ctx.stream = stream ? (cudaStream_t)stream : ctx.own_stream;
+        HF_CUBLAS(cublasSetStream(ctx.blas, ctx.stream));
+        HF_CUSOLVER(cusolverDnSetStream(ctx.solver, ctx.stream));
+    });
+}
+
+int hfgpu_probe_fp64_tflops(double* tflops)
+{
+    return guard([&] {
+        check_ptr(tflops, "tflops");
+        *tflops = probe_fp64_tflops(context());
+    });
+}
+
 void hfgpu_default_options(hfgpu_options* o)
 {
     if (!o) return;
@@ -277,11 +295,11 @@ int hfgpu_rhf(int natoms, const int* atno, const double* xyz, const hfgpu_option
             HF_CUBLAS(cublasDgeam(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, &one, dT.p, n, &one, dV.p, n, dH.p, n));
         }
         // integrals, resident in HBM for the whole SCF
-        Timer te(st);
         DBuf<double> dI(packed_size(n), st);
         dI.zero();
         EriStats es;
         EriPlan* plan = eri_plan_create(ctx, b, opt.schwarz);
+        res->ms_setup = total.ms();
         try {
             eri_compute_packed(ctx, plan, dI.p, &es);
         } catch (...) {
@@ -289,7 +307,7 @@ int hfgpu_rhf(int natoms, const int* atno, const double* xyz, const hfgpu_option
             throw;
         }
         eri_plan_destroy(plan);
-        res->ms_eri = te.ms();
+        res->ms_eri = es.ms;
         res->n_quartets = es.n_quartets;
         res->n_bf_quartets = es.n_bf_quartets;
         res->n_prim_quartets = es.n_prim_quartets;

@@ -1,4 +1,5 @@
 // Per-device context: stream, cuBLAS/cuSOLVER handles, Boys-function grid.
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -9,6 +10,9 @@ namespace hfgpu {
 
 static thread_local std::string g_last_error;
 void set_last_error(const std::string& m) { g_last_error = m; }
+
+static std::atomic<int64_t> g_launches{0};
+void count_launch(int n) { g_launches += n; }
 
 static std::mutex g_ctx_mutex;
 static std::vector<Context*> g_ctx;
@@ -25,7 +29,8 @@ Context& context()
     if (g_ctx[dev]) return *g_ctx[dev];
     auto* c = new Context();
     c->device = dev;
-    HF_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    HF_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+    c->stream = c->own_stream;
     HF_CUBLAS(cublasCreate(&c->blas));
     HF_CUBLAS(cublasSetStream(c->blas, c->stream));
     HF_CUSOLVER(cusolverDnCreate(&c->solver));
@@ -43,3 +48,4 @@ Context& context()
 
 extern "C" const char* hfgpu_last_error(void) { return hfgpu::g_last_error.c_str(); }
 extern "C" int hfgpu_version(void) { return 1; }
+extern "C" int64_t hfgpu_kernel_launches(void) { return hfgpu::g_launches.load(); }

@@ -221,6 +221,7 @@ static void launch_class(Context& ctx, EriPlan* P, ClassPlan& c, int mode, doubl
     a.out = out;
     int64_t blocks = (c.nwarps + ERI_BLOCK / 32 - 1) / (ERI_BLOCK / 32);
     get_kernel(c.tb, c.tk, mode)<<<(unsigned)blocks, ERI_BLOCK, 0, ctx.stream>>>(a);
+    count_launch();
     HF_CUDA(cudaGetLastError());
 }
 
@@ -270,12 +271,12 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
             ShellDev sd = P->shdev();
             PairDev pd = P->prdev();
             switch (t) {
-                case 0: pair_data_kernel<0><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); break;
-                case 1: pair_data_kernel<1><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); break;
-                case 2: pair_data_kernel<2><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); break;
-                case 3: pair_data_kernel<3><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); break;
-                case 4: pair_data_kernel<4><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); break;
-                case 5: pair_data_kernel<5><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); break;
+                case 0: pair_data_kernel<0><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); count_launch(); break;
+                case 1: pair_data_kernel<1><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); count_launch(); break;
+                case 2: pair_data_kernel<2><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); count_launch(); break;
+                case 3: pair_data_kernel<3><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); count_launch(); break;
+                case 4: pair_data_kernel<4><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); count_launch(); break;
+                case 5: pair_data_kernel<5><<<blocks, 128, 0, st>>>(sd, pd, di.p, n, P->pdata.p); count_launch(); break;
             }
             HF_CUDA(cudaGetLastError());
         }

@@ -109,13 +109,15 @@ DBuf<T> to_device(const std::vector<T>& v, cudaStream_t s)
 // Boys-function grid.
 struct Context {
     int device = -1;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // the stream every call runs on
+    cudaStream_t own_stream = nullptr;  // the library's own stream
     cublasHandle_t blas = nullptr;
     cusolverDnHandle_t solver = nullptr;
     double* boys = nullptr;  // device copy of the Boys grid
     int num_sms = 0;
 };
 Context& context();  // for the current device
+void count_launch(int n = 1);  // bookkeeping for hfgpu_kernel_launches
 
 // ---------------------------------------------------------------- basis
 // A shell: all Cartesian components of one angular momentum on one centre with
@@ -170,5 +172,8 @@ void onee_compute(Context& ctx, const Basis& b, int natoms, const int* atno, con
 void jk_from_packed(Context& ctx, int n, const double* d_int2, const double* dP, double* dG);
 
 int64_t packed_size(int64_t n);
+
+// probe.cu: measured FP64 FMA rate (TFLOP/s)
+double probe_fp64_tflops(Context& ctx);
 
 }  // namespace hfgpu

@@ -77,9 +77,11 @@ void jk_from_packed(Context& ctx, int n, const double* d_int2, const double* dP,
     Gh.zero();
     int blocks = (int)std::min<int64_t>((m + 7) / 8, (int64_t)ctx.num_sms * 16);
     jk_packed_kernel<<<blocks, 256, 0, ctx.stream>>>(n, m, d_int2, dP, tab.d.p, Gh.p);
+    count_launch();
     HF_CUDA(cudaGetLastError());
     int64_t nn = (int64_t)n * n;
     symmetrize_add_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, ctx.stream>>>(n, Gh.p, dG);
+    count_launch();
     HF_CUDA(cudaGetLastError());
 }
 

@@ -52,6 +52,7 @@ void ao2mo_fp64(Context& ctx, int n, const double* d_int2, const double* C1, int
     for (int mu0 = 0; mu0 < n; mu0 += bm) {
         const int b = std::min(bm, n - mu0);
         unpack_kernel<<<std::max(1, ctx.num_sms * 8), 256, 0, st>>>(n, mu0, b, d_int2, X.p);
+        count_launch();
         HF_CUDA(cudaGetLastError());
         HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_T, CUBLAS_OP_N, n1, b * n * n, n, &one, C1, n, X.p, n, &zero,
                               X1.p, n1));
@@ -93,6 +94,7 @@ double mp2_energy(Context& ctx, int o, int v, const double* d_iajb, const double
     if (o == 0 || v == 0) return 0.0;
     DBuf<double> part((size_t)o * o, ctx.stream);
     mp2_kernel<<<o * o, 256, 0, ctx.stream>>>(o, v, d_iajb, d_eps, part.p);
+    count_launch();
     HF_CUDA(cudaGetLastError());
     std::vector<double> h((size_t)o * o);
     part.download(h.data(), h.size());
@@ -131,6 +133,7 @@ void transform_packed(Context& ctx, int n, const double* d_int2, const double* d
     ao2mo_fp64(ctx, n, d_int2, dC, n, dC, n, full.p);
     const int64_t total = packed_size(n);
     pack_kernel<<<std::max(1, ctx.num_sms * 8), 256, 0, ctx.stream>>>(n, total, full.p, d_mo);
+    count_launch();
     HF_CUDA(cudaGetLastError());
     HF_CUDA(cudaStreamSynchronize(ctx.stream));
 }
@@ -164,6 +167,7 @@ double mbpt2_packed(Context& ctx, int n, const double* d_mo, const double* d_lam
     if (nocc <= 0 || nocc >= n) return 0.0;
     DBuf<double> part((size_t)nocc * nocc, ctx.stream);
     mbpt2_packed_kernel<<<nocc * nocc, 256, 0, ctx.stream>>>(n, nocc, d_mo, d_lam, part.p);
+    count_launch();
     HF_CUDA(cudaGetLastError());
     std::vector<double> h((size_t)nocc * nocc);
     part.download(h.data(), h.size());

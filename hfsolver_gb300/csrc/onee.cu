@@ -173,6 +173,7 @@ void onee_compute(Context& ctx, const Basis& b, int nat, const int* atno, const 
     FnDev f{dl.p, dn.p, da.p, dc.p, dx.p, dal.p, dco.p};
     int blocks = (n * n + 127) / 128;
     onee_kernel<<<blocks, 128, 0, st>>>(f, n, nat, dZ.p, dC.p, ctx.boys, dS, dT, dV);
+    count_launch();
     HF_CUDA(cudaGetLastError());
     HF_CUDA(cudaStreamSynchronize(st));
 }

@@ -72,6 +72,7 @@ static void reduce(Context& ctx, int mode, int64_t nn, const double* A, const do
                    double* dout)
 {
     reduce_kernel<<<1, 1024, 0, ctx.stream>>>(mode, nn, A, B, C, dout);
+    count_launch();
     HF_CUDA(cudaGetLastError());
 }
 
@@ -148,15 +149,19 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
         else
             jk_from_packed(ctx, n, in.d_int2, dP, G.p);
         add_kernel<<<nblk(nn), 256, 0, st>>>(nn, in.dH, G.p, F.p);
+        count_launch();
         reduce(ctx, 0, nn, dP, in.dH, F.p, scal.p);  // E0
         const double* Fsolve = F.p;
-        if (diis) {
+        // the first iteration has P = 0, whose commutator vanishes trivially: keep
+        // it out of the DIIS history
+        if (diis && it >= 2) {
             const double one = 1.0, zero = 0.0;
             // error = F P S - S P F = Y - Y^T with Y = F P S
             HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, F.p, n, dP, n, &zero, G.p, n));
             HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, G.p, n, in.dS, n, &zero, Y.p, n));
             double* ek = Eh.p + (size_t)head * nn;
             comm_kernel<<<nblk(nn), 256, 0, st>>>(n, Y.p, ek);
+            count_launch();
             HF_CUDA(cudaMemcpyAsync(Fh.p + (size_t)head * nn, F.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
             nhist = std::min(nhist + 1, nd);
             // new row of B: <e_k, e_head>
@@ -221,7 +226,10 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
                 return out;
             }
         }
-        if (!diis && in.alpha != 1.0) mix_kernel<<<nblk(nn), 256, 0, st>>>(nn, in.alpha, Pold.p, dP);
+        if (!diis && in.alpha != 1.0) {
+            mix_kernel<<<nblk(nn), 256, 0, st>>>(nn, in.alpha, Pold.p, dP);
+            count_launch();
+        }
     }
     HF_CUDA(cudaMemcpyAsync(dC, Fw.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
     HF_CUDA(cudaStreamSynchronize(st));

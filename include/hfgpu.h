@@ -40,6 +40,17 @@ enum {
 const char *hfgpu_last_error(void);
 int hfgpu_version(void);
 
+/* Run subsequent calls on the current device on the given cudaStream_t (NULL:
+ * the library's own stream); calls stay synchronous with respect to the host. */
+int hfgpu_set_stream(void *cuda_stream);
+/* number of libhfgpu kernels launched by this process so far (CUDA library
+ * kernels such as cuBLAS/cuSOLVER are not counted) */
+int64_t hfgpu_kernel_launches(void);
+/* Measured FP64 FMA throughput of the current GPU in TFLOP/s (a register-only
+ * kernel of independent fma chains over all SMs), the denominator used for
+ * the FP64-bound integral kernels' roofline. */
+int hfgpu_probe_fp64_tflops(double *tflops);
+
 /* ---- Integral drivers: same arguments as hfsolver's C drivers --------------
  * nbf functions; function i has nprim[i] primitives starting at the 0-based
  * offset istart[i] in coef/alpha (n2 entries), centre (xcenter[i], ycenter[i],
@@ -126,8 +137,11 @@ typedef struct {
     int64_t n_bf_quartets;   /* unique contracted basis-function quartets evaluated */
     int64_t n_prim_quartets; /* primitive shell quartets evaluated */
     double eri_flops;        /* McMurchie-Davidson reference flop count of those */
-    double ms_eri, ms_scf, ms_mp2, ms_total; /* device time of each stage */
-    double reserved[8];
+    double ms_eri;           /* ERI class kernels */
+    double ms_scf, ms_mp2;   /* SCF loop; AO->MO transform + MBPT2 */
+    double ms_total;         /* the whole call */
+    double ms_setup;         /* basis, one-electron integrals, pairs, Schwarz bounds */
+    double reserved[7];
 } hfgpu_result;
 
 void hfgpu_default_options(hfgpu_options *opt);

@@ -79,6 +79,8 @@ def _bind(L, prefix="oracle_"):
         L.oracle_eri_list.restype = None
         L.oracle_ijkl.argtypes = [ctypes.c_int64] * 4
         L.oracle_ijkl.restype = ctypes.c_int64
+        L.oracle_formG_entries.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_int64, _ip, _dp]
+        L.oracle_formG_entries.restype = None
 
 
 def _d(a):
@@ -403,3 +405,37 @@ def mp2_semidirect(int2, C, lam, nocc, block=8):
     den = e_o[:, None, None, None] - e_v[None, :, None, None] + e_o[None, None, :, None] \
         - e_v[None, None, None, :]
     return float(np.sum((2 * iajb ** 2 - iajb * iajb.transpose(0, 3, 2, 1)) / den))
+
+
+# --------------------------------------------------------------------------
+# bounded samples of the reference's cost (for CPU-baseline timing)
+
+
+def random_unique_quartets(n, count, rng):
+    """Uniform sample of unique (i>=j, k>=l, ij>=kl) function quartets."""
+    m = n * (n + 1) // 2
+    total = m * (m + 1) // 2
+    p = rng.integers(0, total, size=count)
+    ij = ((np.sqrt(8.0 * p + 1) - 1) // 2).astype(np.int64)
+    ij -= (ij * (ij + 1) // 2 > p)
+    ij += ((ij + 1) * (ij + 2) // 2 <= p)
+    kl = p - ij * (ij + 1) // 2
+
+    def split(x):
+        i = ((np.sqrt(8.0 * x + 1) - 1) // 2).astype(np.int64)
+        i -= (i * (i + 1) // 2 > x)
+        i += ((i + 1) * (i + 2) // 2 <= x)
+        return i, x - i * (i + 1) // 2
+
+    i, j = split(ij)
+    k, l = split(kl)
+    return np.stack([i, j, k, l], axis=1).astype(np.int32)
+
+
+def formG_entries(P, int2, entries):
+    n = P.shape[0]
+    Pf = np.asfortranarray(P)
+    e = np.ascontiguousarray(np.asarray(entries, dtype=np.int32).reshape(-1, 2))
+    out = np.zeros(len(e))
+    lib().oracle_formG_entries(n, _d(Pf), _d(int2), len(e), _i(e), _d(out))
+    return out

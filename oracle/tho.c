@@ -343,3 +343,21 @@ void oracle_formG(int n, const double *P, const double *int2, double *G)
             G[i + (int64_t)j * n] = acc;
         }
 }
+
+/* G(i,j) of formG2 for a list of (i,j) entries only (bounded timing samples of
+ * the Fock build at sizes where the full n^4 sweep is too slow). */
+void oracle_formG_entries(int n, const double *P, const double *int2, int64_t ne, const int *ij,
+                          double *out)
+{
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t e = 0; e < ne; e++) {
+        int i = ij[2 * e], j = ij[2 * e + 1];
+        double acc = 0.;
+        for (int l = 0; l < n; l++)
+            for (int k = 0; k < n; k++) {
+                double tt = int2[oracle_ijkl(i, j, k, l)] - 0.5 * int2[oracle_ijkl(i, l, k, j)];
+                acc += P[k + (int64_t)l * n] * tt;
+            }
+        out[e] = acc;
+    }
+}

@@ -37,8 +37,8 @@ def test_single_water_config(oracle):
     from hfsolver_gb300.clusters import water
 
     atno, xyz = water()
-    r = hf.rhf(atno, xyz, hf.RHFOptions(tolP=1e-10, tolE=1e-12))
-    ref = oracle.rhf_gauss(atno, xyz, nscf=40, tolE=1e-12, tolP=1e-10)
+    r = hf.rhf(atno, xyz, hf.RHFOptions(nscf=100, tolP=1e-10, tolE=1e-12))
+    ref = oracle.rhf_gauss(atno, xyz, nscf=100, tolE=1e-12, tolP=1e-10)
     e2 = oracle.mbpt2(oracle.transform_int2(ref["int2"], ref["C"]), ref["lam"], 5)
     assert abs(r["Etot"] - ref["Etot"]) < 1e-10
     assert abs(r["E2"] - e2) < 1e-8
