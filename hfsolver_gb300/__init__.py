@@ -4,9 +4,9 @@ The compute path is libhfgpu.so (hand-written CUDA for sm_103a, C ABI in
 include/hfgpu.h); this package is its Python face, with the reference's
 routine names (see hfsolver_gb300.api).
 """
-from .api import (HFGPUError, RHFOptions, SCFNotConverged, basis_size, doscf, getints2, getInts, getS, getT,
+from .api import (HFGPUError, RHFOptions, SCFNotConverged, basis_size, doscf, formG, getints2, getInts, getS, getT,
                   getV, mbpt2, packed_size, rhf, rhf_gauss, transform_int2)
 from ._lib import LIB_PATH
 
-__all__ = ["HFGPUError", "RHFOptions", "SCFNotConverged", "basis_size", "doscf", "getints2", "getInts", "getS",
+__all__ = ["HFGPUError", "RHFOptions", "SCFNotConverged", "basis_size", "doscf", "formG", "getints2", "getInts", "getS",
            "getT", "getV", "mbpt2", "packed_size", "rhf", "rhf_gauss", "transform_int2", "LIB_PATH"]

@@ -52,8 +52,10 @@ SIGNATURES = {
                                       ctypes.c_int64]),
     "hfgpu_doscf": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp, _ip]),
+    "hfgpu_formG": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
     "hfgpu_transform_int2": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
     "hfgpu_mbpt2": (ctypes.c_int, [ctypes.c_int, _dp, _dp, ctypes.c_int, _dp]),
+    "hfgpu_dgemm_sliced": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]),
     "hfgpu_default_options": (None, [ctypes.POINTER(Options)]),
     "hfgpu_basis_size": (ctypes.c_int, [ctypes.c_int, _ip]),
     "hfgpu_rhf": (ctypes.c_int, [ctypes.c_int, _ip, _dp, ctypes.POINTER(Options), ctypes.POINTER(Result), _dp,

@@ -9,6 +9,7 @@ getS, getT, getV       src/qc.c:6-93 (C drivers)                       hfgpu_get
 getInts                src/qc.c:95-131                                 hfgpu_getInts
 getints2               src/gaussians_hfsolver.f90:13-34 (plugin)       hfgpu_getints2
 doscf                  src/scf.f90:72-136                              hfgpu_doscf
+formG                  src/scf.f90:26-58                               hfgpu_formG
 transform_int2         src/mbpt.f90:11-79                              hfgpu_transform_int2
 mbpt2                  src/mbpt.f90:154-159, src/mbpt2.f90:8-31        hfgpu_mbpt2
 rhf_gauss / rhf        src/drivers.f90:12-51 (+ MBPT2)                 hfgpu_rhf
@@ -132,6 +133,18 @@ def doscf(H, int2, S, Noccupied, Nscf, tolE, tolP, alpha):
                                   int(Nscf), float(tolE), float(tolP), float(alpha), C.ctypes.data_as(_dp),
                                   P.ctypes.data_as(_dp), _d(lam), _d(E0), _i(it)))
     return C, P, lam, float(E0[0]), int(it[0])
+
+
+def formG(P, int2):
+    """G = J - K/2 from the packed integrals (scf.f90:26-58)."""
+    P = np.asfortranarray(P, dtype=np.float64)
+    int2 = _f64(int2)
+    n = P.shape[0]
+    if int2.size != packed_size(n):
+        raise ValueError("int2 has the wrong length")
+    G = np.zeros((n, n), order="F")
+    _check(_lib.lib().hfgpu_formG(n, P.ctypes.data_as(_dp), _d(int2), G.ctypes.data_as(_dp)))
+    return G
 
 
 def transform_int2(int2, C):

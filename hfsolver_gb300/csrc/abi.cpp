@@ -7,6 +7,7 @@
 
 #include "internal.h"
 #include "scf.h"
+#include "tcgemm.h"
 
 using namespace hfgpu;
 
@@ -191,6 +192,22 @@ int hfgpu_doscf(int n, const double* H, const double* int2, const double* S, int
     return rc;
 }
 
+int hfgpu_formG(int n, const double* P, const double* int2, double* G)
+{
+    return guard([&] {
+        HF_CHECK(n >= 1, HFGPU_ERR_INVALID, "n must be >= 1");
+        check_ptr(P, "P"); check_ptr(int2, "int2"); check_ptr(G, "G");
+        Context& ctx = context();
+        const size_t nn = (size_t)n * n;
+        DBuf<double> dP(nn, ctx.stream), dI(packed_size(n), ctx.stream), dG(nn, ctx.stream);
+        dP.upload(P, nn);
+        dI.upload(int2, packed_size(n));
+        jk_from_packed(ctx, n, dI.p, dP.p, dG.p);
+        dG.download(G, nn);
+        HF_CUDA(cudaStreamSynchronize(ctx.stream));
+    });
+}
+
 int hfgpu_transform_int2(int n, const double* int2, const double* C, double* moint2)
 {
     return guard([&] {
@@ -218,6 +235,24 @@ int hfgpu_mbpt2(int n, const double* moint2, const double* lam, int nocc, double
         dM.upload(moint2, np);
         dL.upload(lam, n);
         *E2 = mbpt2_packed(ctx, n, dM.p, dL.p, nocc);
+    });
+}
+
+int hfgpu_dgemm_sliced(int64_t M, int N, int K, const double* A, const double* Bt, double* C)
+{
+    return guard([&] {
+        HF_CHECK(M >= 1 && N >= 1 && K >= 1 && K <= 512, HFGPU_ERR_INVALID, "need M, N >= 1 and 1 <= K <= 512");
+        check_ptr(A, "A"); check_ptr(Bt, "Bt"); check_ptr(C, "C");
+        Context& ctx = context();
+        DBuf<double> dA((size_t)M * K, ctx.stream), dB((size_t)N * K, ctx.stream), dC((size_t)M * N, ctx.stream);
+        dA.upload(A, (size_t)M * K);
+        dB.upload(Bt, (size_t)N * K);
+        Sliced sa, sb;
+        slice_dense(ctx, dA.p, M, K, K, sa, SLICE_TILE_A);
+        slice_dense(ctx, dB.p, N, K, K, sb, SLICE_TILE_B);
+        sliced_gemm(ctx, sa, sb, dC.p, OutMap{0, N}, false);
+        dC.download(C, (size_t)M * N);
+        HF_CUDA(cudaStreamSynchronize(ctx.stream));
     });
 }
 
@@ -271,8 +306,8 @@ int hfgpu_rhf(int natoms, const int* atno, const double* xyz, const hfgpu_option
         if (opt_in) opt = *opt_in; else hfgpu_default_options(&opt);
         nscf = opt.nscf;
         HF_CHECK(opt.nscf >= 1, HFGPU_ERR_INVALID, "nscf must be >= 1");
-        HF_CHECK(opt.mp2 >= HFGPU_MP2_NONE && opt.mp2 <= HFGPU_MP2_FP64, HFGPU_ERR_UNSUPPORTED,
-                 "requested MP2 precision is not available");
+        HF_CHECK(opt.mp2 >= HFGPU_MP2_NONE && opt.mp2 <= HFGPU_MP2_SPLIT_BF16, HFGPU_ERR_INVALID,
+                 "unknown MP2 precision");
         std::memset(res, 0, sizeof(*res));
         Basis b = build_basis(natoms, atno, xyz);  // validates the input before any device work
         Context& ctx = context();
@@ -341,7 +376,9 @@ int hfgpu_rhf(int natoms, const int* atno, const double* xyz, const hfgpu_option
             const int mo = opt.mp2_nocc > 0 ? opt.mp2_nocc : nocc;
             HF_CHECK(mo <= n, HFGPU_ERR_INVALID, "mp2_nocc larger than the basis");
             const int mv = n - mo;
-            if (mo > 0 && mv > 0) {
+            if (mo > 0 && mv > 0 && opt.mp2 == HFGPU_MP2_SPLIT_BF16) {
+                res->E2 = mp2_energy_mixed(ctx, n, dI.p, dC.p, mo, dL.p);
+            } else if (mo > 0 && mv > 0) {
                 DBuf<double> iajb((size_t)mo * mv * mo * mv, st);
                 ao2mo_fp64(ctx, n, dI.p, dC.p, mo, dC.p + (size_t)n * mo, mv, iajb.p);
                 res->E2 = mp2_energy(ctx, mo, mv, iajb.p, dL.p);

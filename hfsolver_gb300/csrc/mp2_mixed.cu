@@ -1,0 +1,103 @@
+// Mixed-precision AO -> MO transform on the tensor cores, for MBPT2.
+//
+// Same (ia|jb) as ao2mo_fp64 (the quantity transform_int2, src/mbpt.f90:11-79,
+// feeds to term1, src/mbpt2.f90:8-31), ordered as a half transform so that
+// every contraction is one "tall A times coefficient block" GEMM in the exact
+// bf16-sliced form of tcgemm.cu (FP64 inputs and outputs):
+//   1. Y[p][j][la]  = sum_si (mu nu|la si) C1[si, j]     p = pair(mu >= nu)
+//   2. Z[p][j][b]   = sum_la Y[p][j][la] C2[la, b]
+//   3. W[q][i][mu]  = sum_nu Z[pair(mu, nu)][q] C1[nu, i]    q = (j, b)
+//   4. T[q][i][a]   = sum_mu W[q][i][mu] C2[mu, a]       T[j][b][i][a] = (ia|jb)
+// Steps 1-2 run over blocks of pairs and steps 3-4 over blocks of q, so each
+// sliced operand stays within a fixed device-memory budget.
+#include <algorithm>
+#include <vector>
+
+#include "internal.h"
+#include "scf.h"
+#include "tcgemm.h"
+
+namespace hfgpu {
+
+static const int64_t SLICE_BUDGET_ROWS = 1 << 20;  // rows per sliced operand (x K_pad x 10 bytes)
+
+void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, int n1, const double* C2, int n2,
+                  double* T)
+{
+    cudaStream_t st = ctx.stream;
+    HF_CHECK(n <= 512, HFGPU_ERR_UNSUPPORTED, "mixed-precision transform supports up to 512 functions");
+    const int64_t npair = (int64_t)n * (n + 1) / 2;
+    std::vector<int2> hp(npair);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j <= i; j++) hp[(size_t)i * (i + 1) / 2 + j] = make_int2(i, j);
+    DBuf<int2> pairs = to_device(hp, st);
+    Sliced B1, B2, A;
+    slice_dense(ctx, C1, n1, n, n, B1, SLICE_TILE_B);  // rows of B^T = columns of C1
+    slice_dense(ctx, C2, n2, n, n, B2, SLICE_TILE_B);
+    const int64_t nq = (int64_t)n1 * n2;
+    DBuf<double> Z((size_t)npair * nq, st);
+    // steps 1-2 over blocks of pairs
+    const int64_t pb = std::max<int64_t>(1, SLICE_BUDGET_ROWS / n);
+    DBuf<double> Y((size_t)std::min(pb, npair) * n1 * n, st);
+    for (int64_t p0 = 0; p0 < npair; p0 += pb) {
+        const int64_t np = std::min(pb, npair - p0);
+        slice_packed(ctx, d_int2, pairs.p, p0, np, n, A);
+        sliced_gemm(ctx, A, B1, Y.p, OutMap{n, n1}, false);  // rows (p, la) -> Y[p][j][la]
+        slice_dense(ctx, Y.p, np * n1, n, n, A, SLICE_TILE_A);
+        sliced_gemm(ctx, A, B2, Z.p + p0 * nq, OutMap{0, n2}, false);  // rows (p, j) -> Z[p][j][b]
+    }
+    // steps 3-4 over blocks of q
+    const int64_t qb = std::max<int64_t>(1, SLICE_BUDGET_ROWS / std::max(n, n1));
+    DBuf<double> W((size_t)std::min(qb, nq) * n1 * n, st);
+    for (int64_t q0 = 0; q0 < nq; q0 += qb) {
+        const int64_t nqb = std::min(qb, nq - q0);
+        // rows (q, mu) over nu of Z[pair(mu, nu)][q0 + q]
+        slice_sympair(ctx, Z.p + q0, nq, nqb, n, A);
+        sliced_gemm(ctx, A, B1, W.p, OutMap{n, n1}, false);  // rows (q, mu) -> W[q][i][mu]
+        slice_dense(ctx, W.p, nqb * n1, n, n, A, SLICE_TILE_A);
+        sliced_gemm(ctx, A, B2, T + q0 * n1 * n2, OutMap{0, n2}, false);  // rows (q, i) -> T[q][i][a]
+    }
+}
+
+// one block per (i, j): sum_ab (ia|jb) [2 (ia|jb) - (ib|ja)] / (e_i + e_j - e_a - e_b), T[j][b][i][a]
+__global__ void mp2_jbia_kernel(int o, int v, const double* __restrict__ T, const double* __restrict__ eps,
+                                double* partial)
+{
+    const int i = blockIdx.x % o, j = blockIdx.x / o;
+    const double eij = eps[i] + eps[j];
+    double s = 0.0;
+    for (int e = threadIdx.x; e < v * v; e += blockDim.x) {
+        const int a = e % v, b = e / v;
+        const double x = T[(((int64_t)j * v + b) * o + i) * v + a];
+        const double y = T[(((int64_t)j * v + a) * o + i) * v + b];
+        s += x * (2 * x - y) / (eij - eps[o + a] - eps[o + b]);
+    }
+    __shared__ double sh[256];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+double mp2_energy_mixed(Context& ctx, int n, const double* d_int2, const double* dC, int o, const double* d_eps)
+{
+    const int v = n - o;
+    if (o <= 0 || v <= 0) return 0.0;
+    DBuf<double> T((size_t)o * v * o * v, ctx.stream);
+    ao2mo_sliced(ctx, n, d_int2, dC, o, dC + (size_t)n * o, v, T.p);
+    DBuf<double> part((size_t)o * o, ctx.stream);
+    mp2_jbia_kernel<<<o * o, 256, 0, ctx.stream>>>(o, v, T.p, d_eps, part.p);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+    std::vector<double> h((size_t)o * o);
+    part.download(h.data(), h.size());
+    HF_CUDA(cudaStreamSynchronize(ctx.stream));
+    double E = 0;
+    for (double x : h) E += x;
+    return E;
+}
+
+}  // namespace hfgpu

@@ -40,6 +40,8 @@ double mp2_energy(Context& ctx, int nocc, int nvir, const double* d_iajb, const 
 namespace hfgpu {
 // full (ij|kl) over all orbitals into the packed layout (transform_int2 drop-in)
 void transform_packed(Context& ctx, int n, const double* d_int2, const double* dC, double* d_mo);
+// MBPT2 energy with the tensor-core (exactly sliced bf16) transform (mp2_mixed.cu)
+double mp2_energy_mixed(Context& ctx, int n, const double* d_int2, const double* dC, int nocc, const double* d_eps);
 // term1 of src/mbpt2.f90 on packed MO integrals (mbpt2 drop-in)
 double mbpt2_packed(Context& ctx, int n, const double* d_mo, const double* d_lam, int nocc);
 }  // namespace hfgpu

@@ -1,0 +1,449 @@
+// FP64-accurate GEMM on the tcgen05 tensor cores (sm_103a) by exact bf16 slicing.
+//
+// C[r, c] = sum_k A[r, k] B[k, c] for FP64 A and B, as used by the mixed-
+// precision AO->MO transform.  Each row of A (and each column of B) is scaled
+// by a power of two 2^e so that |x| < 2^e, rounded to a 35-bit fixed-point
+// integer and cut into five 7-bit digits d_0..d_4 (x ~ 2^e sum_t d_t 2^{-7(t+1)}),
+// stored as bf16 "slice planes" (integers <= 128 are exact in bf16).  This is
+// the error-free splitting of Ozaki, Ogita, Oishi and Rump (Numer. Algorithms
+// 59, 95 (2012)) with bf16 tensor-core products:
+//   * a product of two digits is < 2^14, so a K-sum of one digit pair over
+//     K <= 1024 stays below 2^24 and the FP32 tensor-core accumulation is exact;
+//   * digit pairs (i, j) with i + j = t share the weight 2^{-7(t+2)} and are
+//     accumulated together in TMEM accumulator t (t = 0..4, 15 products);
+//     groups t = 0, 1 stay exact for K <= 512, and the rounding of the later
+//     groups is below 2^{-24} of terms that are already 2^{-28} smaller;
+//   * the epilogue recombines sum_t acc_t 2^{-7(t+2)} in FP64 and applies the
+//     row and column scales.
+// The result matches an FP64 GEMM to about 2^-35 of sum_k |A||B| per element.
+//
+// Kernel: one CTA (128 threads) per 128 x 64 output tile; per K step of 64 one
+// thread issues the TMA loads of the 5 A and 5 B slice tiles (128B swizzle)
+// and then the 15 x 4 tcgen05.mma (M=128, N=64, K=16, BF16 in, FP32 out);
+// every wait on an mbarrier is bounded and reports a timeout through an error
+// flag instead of spinning forever.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "internal.h"
+#include "tcgemm.h"
+
+namespace hfgpu {
+
+constexpr int NSL = 5, SL_BITS = 7;
+constexpr int BM = 128, BN = 64, BK = 64;
+constexpr int A_TILE = BM * BK * 2;  // 16 KiB
+constexpr int B_TILE = BN * BK * 2;  // 8 KiB
+constexpr int SMEM_BYTES = NSL * (A_TILE + B_TILE) + 1024 + 64;
+constexpr uint32_t TMEM_COLS = 512;  // 5 accumulators x 64 columns, rounded to a power of two
+constexpr int WAIT_SPINS = 1 << 22;
+
+// ------------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(su32(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait on an mbarrier phase; false after WAIT_SPINS polls
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase)
+{
+    for (int i = 0; i < WAIT_SPINS; ++i) {
+        if (mbar_try_wait(bar, phase)) return true;
+        if (i > 32) __nanosleep(64);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            su32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(su32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// K-major operand tile written by TMA with 128-byte swizzle: 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
+{
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;              // leading byte offset (not used by swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
+    d |= (uint64_t)1 << 46;              // descriptor version
+    d |= (uint64_t)2 << 61;              // 128-byte swizzle
+    return d;
+}
+
+// kind::f16 instruction descriptor: BF16 x BF16 -> FP32, both K-major, M = 128, N = BN
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void umma(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t acc)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
+        "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ double pow2(int e) { return __longlong_as_double((int64_t)(e + 1023) << 52); }
+
+// ------------------------------------------------------------------ GEMM kernel
+__device__ __forceinline__ int64_t out_index(const OutMap& om, int64_t r, int64_t c)
+{
+    return om.R > 0 ? (r / om.R) * (om.R * om.ld) + c * om.R + (r % om.R) : r * om.ld + c;
+}
+
+__global__ void __launch_bounds__(128, 1)
+    sliced_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                       int64_t a_rows_pad, int b_rows_pad, int ksteps, const int* __restrict__ ea,
+                       const int* __restrict__ eb, int64_t M, int N, double* out, OutMap om, int accumulate,
+                       int* err)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* sA = smem;                       // NSL tiles of BM x BK bf16
+    unsigned char* sB = smem + NSL * A_TILE;        // NSL tiles of BN x BK bf16
+    uint64_t* bars = (uint64_t*)(sB + NSL * B_TILE);  // [0] TMA, [1] MMA
+    uint32_t* tslot = (uint32_t*)(bars + 2);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t m0 = (int64_t)blockIdx.x * BM;
+    const int n0 = blockIdx.y * BN;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tslot)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+
+    bool ok = true;
+    int stuck = -1;  // barrier whose wait timed out
+    uint32_t phase = 0;
+    for (int ks = 0; ks < ksteps && ok; ++ks) {
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(&bars[0], NSL * (A_TILE + B_TILE));
+#pragma unroll
+            for (int t = 0; t < NSL; ++t) {
+                tma_load_2d(sA + t * A_TILE, &tmA, ks * BK, (int)(t * a_rows_pad + m0), &bars[0]);
+                tma_load_2d(sB + t * B_TILE, &tmB, ks * BK, t * b_rows_pad + n0, &bars[0]);
+            }
+        }
+        ok = mbar_wait(&bars[0], phase);
+        if (!ok) stuck = 0;
+        if (ok && threadIdx.x == 0) {
+            fence_after();
+#pragma unroll
+            for (int i = 0; i < NSL; ++i)
+#pragma unroll
+                for (int j = 0; j < NSL - i; ++j) {
+                    const uint32_t dt = tmem + (uint32_t)((i + j) * BN);
+#pragma unroll
+                    for (int kk = 0; kk < BK / 16; ++kk) {
+                        const uint64_t ad = sdesc(su32(sA + i * A_TILE) + kk * 32);
+                        const uint64_t bd = sdesc(su32(sB + j * B_TILE) + kk * 32);
+                        // group t = i + j is first written by (i = 0, j = t) at ks = 0, kk = 0
+                        umma(dt, ad, bd, (ks == 0 && i == 0 && kk == 0) ? 0u : 1u);
+                    }
+                }
+            umma_commit(&bars[1]);
+        }
+        if (ok) {
+            ok = mbar_wait(&bars[1], phase);
+            if (!ok) stuck = 1;
+        }
+        if (ok) phase ^= 1;
+        __syncthreads();
+    }
+    if (!ok) {
+        if (lane == 0) atomicExch(err, 1);
+        // let the copies or products still in flight land before TMEM is freed (bounded)
+        mbar_wait(&bars[stuck], phase);
+    } else {
+        fence_after();
+        // epilogue: warp w owns TMEM lanes (rows) 32w .. 32w+31
+        const int64_t r = m0 + warp * 32 + lane;
+        const double er = (r < M) ? pow2(ea[r]) : 0.0;
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            double v[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[i] = 0.0;
+#pragma unroll
+            for (int t = 0; t < NSL; ++t) {
+                float f[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(t * BN + c0), f);
+                const double w = pow2(-SL_BITS * (t + 2));
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[i] = fma((double)f[i], w, v[i]);
+            }
+            if (r < M) {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int c = n0 + c0 + i;
+                    if (c < N) {
+                        const double x = v[i] * er * pow2(eb[c]);
+                        const int64_t o = out_index(om, r, c);
+                        out[o] = accumulate ? out[o] + x : x;
+                    }
+                }
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+}
+
+// ------------------------------------------------------------------ slicing
+// digits of |x| * 2^(35 - e) (rounded), with the sign of x applied
+__device__ __forceinline__ void digits5(double x, int e, float (&d)[NSL])
+{
+    const uint64_t bits = (uint64_t)__double_as_longlong(x);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    uint64_t Y = 0;
+    if (ex != 0) {
+        const uint64_t m = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+        const int sh = ex - 1075 + NSL * SL_BITS - e;  // |x| < 2^e gives sh < -17
+        if (sh >= 0)
+            Y = m << sh;
+        else if (sh > -63)
+            Y = (m + (1ull << (-sh - 1))) >> (-sh);
+    }
+    const float sgn = (bits >> 63) ? -1.0f : 1.0f;
+#pragma unroll
+    for (int t = 0; t < NSL; ++t) {
+        const int shift = SL_BITS * (NSL - 1 - t);
+        const uint64_t dig = (t == 0) ? (Y >> shift) : ((Y >> shift) & ((1u << SL_BITS) - 1));
+        d[t] = sgn * (float)dig;
+    }
+}
+
+// row exponent: |x| < 2^e for every x in the row (0 for an all-zero row)
+__device__ __forceinline__ int row_exponent(double amax)
+{
+    if (!(amax > 0)) return 0;
+    return (int)((((uint64_t)__double_as_longlong(amax)) >> 52) & 0x7FF) - 1022;
+}
+
+// One warp per row.  Element (r, k) of the source is fetched by Src::get(r, k).
+template <class Src>
+__global__ void slice_kernel(Src src, int64_t rows, int K, int64_t rows_pad, int K_pad, __nv_bfloat16* planes,
+                             int* rexp)
+{
+    constexpr int KMAX = 16;  // K <= 512
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += nwarp) {
+        double x[KMAX];
+        double amax = 0.0;
+#pragma unroll
+        for (int q = 0; q < KMAX; ++q) {
+            const int k = lane + 32 * q;
+            x[q] = (k < K) ? src.get(r, k) : 0.0;
+            amax = fmax(amax, fabs(x[q]));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+        const int e = row_exponent(amax);
+        if (lane == 0) rexp[r] = e;
+#pragma unroll
+        for (int q = 0; q < KMAX; ++q) {
+            const int k = lane + 32 * q;
+            if (k < K) {
+                float d[NSL];
+                digits5(x[q], e, d);
+#pragma unroll
+                for (int t = 0; t < NSL; ++t) planes[((int64_t)t * rows_pad + r) * K_pad + k] = __float2bfloat16_rn(d[t]);
+            }
+        }
+    }
+}
+
+struct DenseRows {  // row-major rows with stride ld
+    const double* p;
+    int64_t ld;
+    __device__ double get(int64_t r, int k) const { return p[r * ld + k]; }
+};
+
+struct PackedRows {  // rows (pair p, la), k = si of the packed (mu nu|la si), pairs mu >= nu from p0
+    const double* ints;
+    const int2* pairs;
+    int64_t p0;
+    int n;
+    __device__ double get(int64_t r, int k) const
+    {
+        const int2 mn = pairs[p0 + r / n];
+        const int64_t la = r % n, si = k;
+        const int64_t a = mn.x, b = mn.y;
+        const int64_t c = la > si ? la : si, d = la > si ? si : la;
+        const int64_t ij = a * (a + 1) / 2 + b, kl = c * (c + 1) / 2 + d;
+        return ints[ij >= kl ? ij * (ij + 1) / 2 + kl : kl * (kl + 1) / 2 + ij];
+    }
+};
+
+struct SymPairRows {  // rows (q, mu), k = nu of Z[pair(mu, nu) * ldz + q]
+    const double* Z;
+    int64_t ldz;
+    int n;
+    __device__ double get(int64_t r, int k) const
+    {
+        const int64_t q = r / n, mu = r % n, nu = k;
+        const int64_t a = mu > nu ? mu : nu, b = mu > nu ? nu : mu;
+        return Z[(a * (a + 1) / 2 + b) * ldz + q];
+    }
+};
+
+// ------------------------------------------------------------------ host side
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    });
+    HF_CHECK(fn != nullptr, HFGPU_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    return fn;
+}
+
+static CUtensorMap make_map(const Sliced& s, int box_rows)
+{
+    CUtensorMap m;
+    cuuint64_t dims[2] = {(cuuint64_t)s.K_pad, (cuuint64_t)(NSL * s.rows_pad)};
+    cuuint64_t strides[1] = {(cuuint64_t)s.K_pad * 2};
+    cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)s.planes.p, dims, strides, box, es,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    HF_CHECK(r == CUDA_SUCCESS, HFGPU_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return m;
+}
+
+static int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+void Sliced::alloc(Context& ctx, int64_t r, int k, int row_tile)
+{
+    HF_CHECK(k >= 1 && k <= 512, HFGPU_ERR_UNSUPPORTED, "sliced GEMM supports 1 <= K <= 512");
+    rows = r;
+    K = k;
+    rows_pad = round_up(r, row_tile);
+    K_pad = (int)round_up(k, BK);
+    const size_t need = (size_t)NSL * rows_pad * K_pad;
+    if (planes.n < need) planes.alloc(need, ctx.stream);
+    if (rexp.n < (size_t)rows_pad) rexp.alloc(rows_pad, ctx.stream);
+    HF_CUDA(cudaMemsetAsync(planes.p, 0, need * sizeof(__nv_bfloat16), ctx.stream));
+}
+
+template <class Src>
+static void launch_slice(Context& ctx, const Src& src, Sliced& s)
+{
+    const int64_t warps = std::min<int64_t>(s.rows, (int64_t)ctx.num_sms * 64);
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, (warps * 32 + 255) / 256);
+    slice_kernel<Src><<<blocks, 256, 0, ctx.stream>>>(src, s.rows, s.K, s.rows_pad, s.K_pad, s.planes.p, s.rexp.p);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+}
+
+void slice_dense(Context& ctx, const double* A, int64_t rows, int K, int64_t ld, Sliced& s, int row_tile)
+{
+    s.alloc(ctx, rows, K, row_tile);
+    launch_slice(ctx, DenseRows{A, ld}, s);
+}
+
+void slice_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n, Sliced& s)
+{
+    s.alloc(ctx, npairs * n, n, BM);
+    launch_slice(ctx, PackedRows{ints, pairs, p0, n}, s);
+}
+
+void slice_sympair(Context& ctx, const double* Z, int64_t ldz, int64_t nq, int n, Sliced& s)
+{
+    s.alloc(ctx, nq * n, n, BM);
+    launch_slice(ctx, SymPairRows{Z, ldz, n}, s);
+}
+
+void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, OutMap om, bool accumulate)
+{
+    HF_CHECK(A.K == B.K && A.K_pad == B.K_pad, HFGPU_ERR_INVALID, "sliced GEMM: K mismatch");
+    HF_CHECK(B.rows_pad % BN == 0 && A.rows_pad % BM == 0, HFGPU_ERR_INVALID, "sliced GEMM: padding");
+    static bool attr = false;
+    if (!attr) {
+        HF_CUDA(cudaFuncSetAttribute(sliced_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        attr = true;
+    }
+    const CUtensorMap ta = make_map(A, BM), tb = make_map(B, BN);
+    DBuf<int> err(1, ctx.stream);
+    err.zero();
+    dim3 grid((unsigned)(A.rows_pad / BM), (unsigned)(B.rows_pad / BN));
+    HF_CHECK(grid.x > 0 && grid.y > 0 && A.rows_pad / BM < 2147483647LL, HFGPU_ERR_INVALID, "sliced GEMM: grid");
+    sliced_gemm_kernel<<<grid, 128, SMEM_BYTES, ctx.stream>>>(ta, tb, A.rows_pad, (int)B.rows_pad, A.K_pad / BK,
+                                                               A.rexp.p, B.rexp.p, A.rows, (int)B.rows, out, om,
+                                                               accumulate ? 1 : 0, err.p);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+    int h = 0;
+    err.download(&h, 1);
+    HF_CUDA(cudaStreamSynchronize(ctx.stream));
+    HF_CHECK(h == 0, HFGPU_ERR_CUDA, "sliced GEMM: an mbarrier wait timed out");
+}
+
+}  // namespace hfgpu

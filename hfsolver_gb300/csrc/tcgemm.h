@@ -1,0 +1,37 @@
+// Exactly sliced FP64 GEMM on tcgen05 tensor cores (tcgemm.cu).
+#pragma once
+#include <cuda_bf16.h>
+
+#include "internal.h"
+
+namespace hfgpu {
+
+// Output placement: element (r, c) goes to r*ld + c (R == 0), or, with R > 0,
+// to (r/R)*(R*ld) + c*R + r%R (the rows transposed within blocks of R).
+struct OutMap {
+    int64_t R;
+    int64_t ld;
+};
+
+// A matrix cut into five bf16 planes of 7-bit digits plus one power-of-two
+// exponent per row; rows and K padded to the tile sizes.
+struct Sliced {
+    DBuf<__nv_bfloat16> planes;
+    DBuf<int> rexp;
+    int64_t rows = 0, rows_pad = 0;
+    int K = 0, K_pad = 0;
+    void alloc(Context& ctx, int64_t rows, int K, int row_tile);
+};
+
+constexpr int SLICE_TILE_A = 128, SLICE_TILE_B = 64;
+
+// rows of a row-major FP64 matrix (stride ld)
+void slice_dense(Context& ctx, const double* A, int64_t rows, int K, int64_t ld, Sliced& s, int row_tile);
+// rows (pair p, la) over si of the packed (mu nu|la si), pairs[p0 .. p0+npairs)
+void slice_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n, Sliced& s);
+// rows (q, mu), q < nq, over nu of Z[pair(mu, nu) * ldz + q]
+void slice_sympair(Context& ctx, const double* Z, int64_t ldz, int64_t nq, int n, Sliced& s);
+// out (+)= A B^T for slices A (M x K) and B (N x K)
+void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, OutMap om, bool accumulate);
+
+}  // namespace hfgpu

@@ -102,6 +102,11 @@ int hfgpu_doscf(int n, const double *H, const double *int2, const double *S, int
                 double tolE, double tolP, double alpha, double *C, double *P, double *lam,
                 double *E0, int *niter);
 
+/* replaces formG / formG2, src/scf.f90:26-58: G(i,j) = sum_kl P(k,l) [(ij|kl) - (il|kj)/2]
+ * from the packed integrals, without the reference's dense TT(n,n,n,n)
+ * (src/scf.f90:79-105); P and G column-major n x n. */
+int hfgpu_formG(int n, const double *P, const double *int2, double *G);
+
 /* replaces transform_int2, src/mbpt.f90:11-79: (mu nu|la si) -> (ij|kl) over
  * all orbitals, both arrays packed.  FP64. */
 int hfgpu_transform_int2(int n, const double *int2, const double *C, double *moint2);
@@ -110,6 +115,13 @@ int hfgpu_transform_int2(int n, const double *int2, const double *C, double *moi
  * E2 = sum_{a,b<nocc; r,s>=nocc} [2 (ar|bs)^2 - (ar|bs)(as|br)] / (lam_a+lam_b-lam_r-lam_s)
  * from the packed MO integrals. */
 int hfgpu_mbpt2(int n, const double *moint2, const double *lam, int nocc, double *E2);
+
+/* FP64-accurate C = A B on the tcgen05 tensor cores (the kernel behind the
+ * mixed-precision transform): A row-major M x K, Bt = B^T row-major N x K
+ * (B column-major), C row-major M x N; 1 <= K <= 512.  Rows of A and columns
+ * of B are split exactly into five 7-bit bf16 digits with a power-of-two
+ * scale; the result agrees with an FP64 GEMM to about 2^-35 sum_k |A||B|. */
+int hfgpu_dgemm_sliced(int64_t M, int N, int K, const double *A, const double *Bt, double *C);
 
 /* ---- Whole pipeline: rhf_gauss (src/drivers.f90:12-51) + MBPT2 ------------ */
 

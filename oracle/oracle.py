@@ -299,11 +299,16 @@ def eigh(F, S):
     return scipy.linalg.eigh(F, S, lower=True, driver="gvd")
 
 
-def doscf(H, int2, S, nocc, nscf, tolE, tolP, alpha, verbose=False):
-    """Restates scf.f90:72-136 (P = 0 start, linear mixing, 4-energy window)."""
+def doscf(H, int2, S, nocc, nscf, tolE, tolP, alpha, verbose=False, diis=0):
+    """Restates scf.f90:72-136 (P = 0 start, linear mixing, 4-energy window).
+
+    diis > 0 replaces the linear mixing by Pulay DIIS with that many vectors
+    (error F P S - S P F, iterations with P = 0 excluded); it is used only to
+    reach the same converged solution faster on the larger fixture molecules."""
     n = H.shape[0]
     P = np.zeros((n, n))
     Escf = []
+    hist_F, hist_e = [], []
     for it in range(nscf):
         G = formG(P, int2)
         F = H + G
@@ -311,7 +316,25 @@ def doscf(H, int2, S, nocc, nscf, tolE, tolP, alpha, verbose=False):
         Escf.append(E0)
         if verbose:
             print(it + 1, E0)
-        lam, C = eigh(F, S)
+        Fs = F
+        if diis and it > 0:
+            err = F @ P @ S - S @ P @ F
+            hist_F.append(F)
+            hist_e.append(err)
+            hist_F, hist_e = hist_F[-diis:], hist_e[-diis:]
+            k = len(hist_F)
+            if k >= 2:
+                B = np.zeros((k + 1, k + 1))
+                for a in range(k):
+                    for b in range(k):
+                        B[a, b] = np.sum(hist_e[a] * hist_e[b])
+                B[:k, :k] /= np.max(np.abs(np.diag(B[:k, :k])))
+                B[k, :k] = B[:k, k] = -1
+                rhs = np.zeros(k + 1)
+                rhs[k] = -1
+                c = np.linalg.solve(B, rhs)[:k]
+                Fs = sum(ci * Fi for ci, Fi in zip(c, hist_F))
+        lam, C = eigh(Fs, S)
         Pold = P
         P = formP(C, nocc)
         dP = np.sqrt(np.sum((P - Pold) ** 2) / 4)
@@ -319,7 +342,8 @@ def doscf(H, int2, S, nocc, nscf, tolE, tolP, alpha, verbose=False):
             w = Escf[it - 3:it + 1]
             if dP < tolP and max(w) - min(w) < tolE:
                 return dict(C=C, P=P, lam=lam, E0=E0, niter=it + 1, dP=dP)
-        P = (1 - alpha) * Pold + alpha * P
+        if not diis:
+            P = (1 - alpha) * Pold + alpha * P
     raise SCFNotConverged(f"SCF did not converge in {nscf} iterations.")
 
 
@@ -333,7 +357,7 @@ def nuclear_energy(atno, xyz):
     return E
 
 
-def rhf_gauss(atno, xyz, nscf=40, alpha=1.0, tolE=1e-10, tolP=1e-8, verbose=False):
+def rhf_gauss(atno, xyz, nscf=40, alpha=1.0, tolE=1e-10, tolP=1e-8, verbose=False, diis=0):
     """drivers.f90:12-51: integrals, H = T + V, SCF with Nocc = sum(atno)/2."""
     b = Basis(atno, xyz)
     S = one_electron(b, "S")
@@ -341,7 +365,7 @@ def rhf_gauss(atno, xyz, nscf=40, alpha=1.0, tolE=1e-10, tolP=1e-8, verbose=Fals
     V = one_electron(b, "V")
     int2 = getInts(b)
     H = T + V
-    r = doscf(H, int2, S, int(sum(atno)) // 2, nscf, tolE, tolP, alpha, verbose)
+    r = doscf(H, int2, S, int(sum(atno)) // 2, nscf, tolE, tolP, alpha, verbose, diis)
     Enuc = nuclear_energy(b.atno, b.xyz)
     r.update(basis=b, S=S, T=T, V=V, H=H, int2=int2, Enuc=Enuc, Ekin=float(np.sum(r["P"] * T)),
              Etot=r["E0"] + Enuc)

@@ -55,6 +55,14 @@ def test_doscf_dropin(oracle):
     assert_close(P, ref["P"], 1e-8, 0, "P")
 
 
+def test_formG_dropin(oracle):
+    c = CASES["NH3"]
+    ref = oracle.rhf_gauss(c["atno"], np.array(c["xyz"], float))
+    for P in (ref["P"], np.random.default_rng(2).standard_normal(ref["P"].shape)):
+        P = 0.5 * (P + P.T)
+        assert_close(hf.formG(P, ref["int2"]), oracle.formG(P, ref["int2"]), 1e-11, 1e-11, "G")
+
+
 def test_doscf_nonconvergence_is_reported(oracle):
     c = CASES["H2O"]
     ref = oracle.rhf_gauss(c["atno"], np.array(c["xyz"], float))
