@@ -98,10 +98,10 @@ def workload(rank):
     return water_cluster(8, box=8.0, seed=rank)
 
 
-def options():
+def options(mp2="fp64"):
     import hfsolver_gb300 as hf
 
-    return hf.RHFOptions(nscf=60, diis=True, diis_size=8, schwarz=1e-12, tolE=1e-10, tolP=1e-8, mp2="fp64")
+    return hf.RHFOptions(nscf=60, diis=True, diis_size=8, schwarz=1e-12, tolE=1e-10, tolP=1e-8, mp2=mp2)
 
 
 # ---------------------------------------------------------------- CPU baseline
@@ -198,7 +198,7 @@ def run_gpu(args):
     stream = torch.cuda.Stream()
     _lib.check(L.hfgpu_set_stream(ctypes.c_void_p(stream.cuda_stream)))
     atno, xyz = workload(rank)
-    opt = options()
+    opt = options(args.mp2)
     peak = ctypes.c_double(0)
     _lib.check(L.hfgpu_probe_fp64_tflops(ctypes.byref(peak)))
 
@@ -254,7 +254,7 @@ def run_gpu(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "molecule": "8 H2O, seed=rank, 8 A cube", "nbf": n, "nocc": r["nocc"],
-                   "global_batch": world, "scf": "DIIS", "schwarz": 1e-12, "mp2": "fp64",
+                   "global_batch": world, "scf": "DIIS", "schwarz": 1e-12, "mp2": args.mp2,
                    "l2": "no flush: each step rebuilds a 1.6 GB packed ERI array (> 129 MB L2)",
                    "parallelism": f"replicas x{world}"},
         "results": {"Etot": r["Etot"], "E2": r["E2"], "niter": r["niter"]},
@@ -286,6 +286,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mp2", default="fp64", choices=["fp64", "split_bf16"])
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the CPU-baseline sample (profiling runs)")
     args = ap.parse_args()

@@ -30,9 +30,11 @@ __global__ void jk_packed_kernel(int n, int64_t m, const double* __restrict__ in
         const double* row = ints + ij * (ij + 1) / 2;
         double gij = 0.0;
         for (int64_t kl = lane; kl <= ij; kl += 32) {
+            const double v = row[kl];
+            if (v == 0.0) continue;  // screened-out quartets contribute nothing
             const int2 pkl = pairs[kl];
             const int k = pkl.x, l = pkl.y;
-            double w = row[kl] * fij;
+            double w = v * fij;
             if (k == l) w *= 0.5;
             if (kl == ij) w *= 0.5;
             gij = fma(2.0 * w, P[k + (int64_t)l * n], gij);
