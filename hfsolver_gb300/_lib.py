@@ -53,6 +53,8 @@ SIGNATURES = {
     "hfgpu_doscf": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp, _ip]),
     "hfgpu_formG": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
+    "hfgpu_formG_device_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p]),
     "hfgpu_transform_int2": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
     "hfgpu_mbpt2": (ctypes.c_int, [ctypes.c_int, _dp, _dp, ctypes.c_int, _dp]),
     "hfgpu_dgemm_sliced": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]),

@@ -107,6 +107,22 @@ int hfgpu_doscf(int n, const double *H, const double *int2, const double *S, int
  * (src/scf.f90:79-105); P and G column-major n x n. */
 int hfgpu_formG(int n, const double *P, const double *int2, double *G);
 
+/* Allocation-free variant of hfgpu_formG; it has no counterpart in the
+ * reference.  For callers that cannot let a library allocate device memory:
+ * code whose device memory is all owned by its own allocator (for example a
+ * framework's caching allocator that has reserved the GPU) or by a fixed
+ * quota, or a latency-critical loop where a cudaMalloc would synchronise the
+ * device.  Inputs and output are DEVICE pointers owned by the caller:
+ * d_int2 (packed, m(m+1)/2 doubles), d_P and d_G (n x n, column-major).  The
+ * work is enqueued on cuda_stream (a cudaStream_t; NULL = the legacy default
+ * stream) and the call returns without waiting for it.  The only scratch is a
+ * fixed array of 512 x 512 doubles (2 MiB) per device that is created when the
+ * library is loaded and kept until the process exits, so n <= 512 (larger n
+ * returns HFGPU_ERR_INVALID).  The first call on a device looks up that
+ * array's device address, so make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race. */
+int hfgpu_formG_device_noalloc(int n, const double *d_int2, const double *d_P, double *d_G, void *cuda_stream);
+
 /* replaces transform_int2, src/mbpt.f90:11-79: (mu nu|la si) -> (ij|kl) over
  * all orbitals, both arrays packed.  FP64. */
 int hfgpu_transform_int2(int n, const double *int2, const double *C, double *moint2);
