@@ -5,9 +5,11 @@ Workload (one step = one molecule through the whole pipeline): 8 rigid H2O
 (0.9572 A, 104.52 deg) with random orientations, oxygens in an 8 A cube
 (O-O >= 2.7 A, seed = rank), 6-31G** Cartesian basis (200 functions, 40
 occupied); FP64 McMurchie-Davidson ERIs with a Schwarz cut of 1e-12, kept in
-HBM; RHF with DIIS (dP < 1e-8, 4-energy window < 1e-10); FP64 AO->MO
-transform and MBPT2.  Everything is rebuilt each step (the 1.6 GB packed ERI
-array is larger than L2, so no L2 flush is needed between steps).
+HBM; RHF with DIIS and SP2 density purification (dP < 1e-8, 4-energy window
+< 1e-10); AO->MO transform and MBPT2 on the tensor cores (exact 7-bit bf16
+slicing, tcgen05), with the plain FP64 transform timed beside it on the same
+molecule ("mixed_vs_plain").  Everything is rebuilt each step (the 1.6 GB
+packed ERI array is larger than L2, so no L2 flush is needed between steps).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -92,16 +94,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def workload(rank):
+def workload(rank, waters=8):
     from hfsolver_gb300.clusters import water_cluster
 
-    return water_cluster(8, box=8.0, seed=rank)
+    # 8 waters in an 8 A cube; other sizes at the same density (16 waters: 10.08 A)
+    return water_cluster(waters, seed=rank)
 
 
-def options(mp2="fp64"):
+def options(mp2="split_bf16"):
     import hfsolver_gb300 as hf
 
-    return hf.RHFOptions(nscf=60, diis=True, diis_size=8, schwarz=1e-12, tolE=1e-10, tolP=1e-8, mp2=mp2)
+    return hf.RHFOptions(nscf=60, diis=True, diis_size=8, schwarz=1e-12, tolE=1e-10, tolP=1e-8, mp2=mp2,
+                         purify=True)
 
 
 # ---------------------------------------------------------------- CPU baseline
@@ -180,6 +184,28 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------- GPU run
+def measured_peaks():
+    """Peaks measured on this GPU pool (generated file), else the stated fallback."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return d["hbm_gbs"], d["bf16_tflops"], "measured (MEASURED_PEAKS.json)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 1900.0, "fallback (6.8 TB/s, 1.9 PFLOP/s bf16)"
+
+
+def timed_steps(L, stream, steps, fn):
+    import torch
+
+    torch.cuda.synchronize()
+    n0 = L.hfgpu_kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    out = [fn() for _ in range(steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), out, L.hfgpu_kernel_launches() - n0
+
+
 def run_gpu(args):
     import ctypes
 
@@ -197,76 +223,98 @@ def run_gpu(args):
     L = _lib.lib()
     stream = torch.cuda.Stream()
     _lib.check(L.hfgpu_set_stream(ctypes.c_void_p(stream.cuda_stream)))
-    atno, xyz = workload(rank)
-    opt = options(args.mp2)
+    atno, xyz = workload(rank, args.waters)
+    main_mp2 = args.mp2
+    other_mp2 = "fp64" if main_mp2 == "split_bf16" else "split_bf16"
+    opt, opt_other = options(main_mp2), options(other_mp2)
     peak = ctypes.c_double(0)
     _lib.check(L.hfgpu_probe_fp64_tflops(ctypes.byref(peak)))
-
-    def step():
-        return hf.rhf(atno, xyz, opt)
-
-    for _ in range(args.warmup):
-        r = step()
+    hbm_peak, bf16_peak, peak_src = measured_peaks()
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
-    # device-timed region
+    for _ in range(args.warmup):
+        hf.rhf(atno, xyz, opt)
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
-    torch.cuda.synchronize()
-    n0 = L.hfgpu_kernel_launches()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    results = [step() for _ in range(args.steps)]
-    e1.record(stream)
-    torch.cuda.synchronize()
+    ms, results, launches = timed_steps(L, stream, args.steps, lambda: hf.rhf(atno, xyz, opt))
     barrier()
-    launches = L.hfgpu_kernel_launches() - n0
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    # end-to-end through the C ABI with host buffers (coordinates in, orbitals out)
-    n = results[-1]["nbf"]
+    # end to end through the C ABI with host buffers (coordinates in, orbitals out)
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        rr = hf.rhf(atno, xyz, opt, want_orbitals=True)
+        hf.rhf(atno, xyz, opt, want_orbitals=True)
     torch.cuda.synchronize()
     ms_e2e = (time.perf_counter() - t0) * 1e3
+    # the other MBPT2 precision on the same molecule, for the mixed-vs-plain comparison
+    hf.rhf(atno, xyz, opt_other)
+    ms_o, res_o, _ = timed_steps(L, stream, max(1, args.steps // 2), lambda: hf.rhf(atno, xyz, opt_other))
     barrier()
     if world > 1:
-        t = torch.tensor([ms, ms_e2e], dtype=torch.float64, device="cuda")
+        t = torch.tensor([ms, ms_e2e, ms_o], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, ms_e2e = float(t[0]), float(t[1])
+        ms, ms_e2e, ms_o = (float(x) for x in t)
     if rank != 0:
         return 0
     r = results[-1]
-    eri_ms = float(np.mean([x["ms_eri"] for x in results]))
-    achieved = r["eri_flops"] / (eri_ms * 1e-3) / 1e12
+    n = r["nbf"]
+    avg = lambda k: float(np.mean([x[k] for x in results]))  # noqa: E731
+    eri_ms, fock_ms, tc_ms = avg("ms_eri"), avg("ms_fock"), avg("ms_tcgemm")
+    # the Fock build reads each surviving quartet block once: 8 bytes per computed integral
+    block_bytes = 8.0 * r["n_block_elems"] if r.get("n_block_elems") else 8.0 * r["n_bf_quartets"]
+    roof = {
+        "eri": {"kernel": "eri_class_kernel (21 classes, one ERI pass)", "bound": "fp64",
+                "achieved": r["eri_flops"] / (eri_ms * 1e-3) / 1e12, "peak": peak.value, "unit": "TFLOP/s",
+                "peak_source": "measured on this GPU by hfgpu_probe_fp64_tflops", "ms": eri_ms},
+        "fock": {"kernel": "digest_kernel (21 classes, + symmetrize), per SCF iteration", "bound": "hbm",
+                 "achieved": block_bytes / (fock_ms / r["niter"] * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                 "peak_source": peak_src, "ms": fock_ms},
+    }
+    if r["tc_flops"] > 0:
+        roof["tcgemm"] = {"kernel": "sliced_gemm_kernel (tcgen05, 21 bf16 products per FP64 multiply-add)",
+                          "bound": "tensor", "achieved": r["tc_flops"] / (tc_ms * 1e-3) / 1e12, "peak": bf16_peak,
+                          "unit": "TFLOP/s", "peak_source": peak_src, "ms": tc_ms}
+    for v in roof.values():
+        v["frac"] = v["achieved"] / v["peak"]
+    top = max(roof, key=lambda k: roof[k]["ms"])
+    dominant = dict(roof[top])
+    dominant["traffic"] = None
     cpu_t, cpu_desc = (None, None)
     if world == 1 and not args.no_cpu_baseline:
         cpu_t, cpu_desc = cpu_sample(atno, xyz, r["niter"], budget_s=8.0)
+    ro = res_o[-1]
+    mixed = r if main_mp2 == "split_bf16" else ro
+    plain = ro if main_mp2 == "split_bf16" else r
     line = {
         "metric": METRIC, "value": world * args.steps / (ms * 1e-3), "unit": "molecules/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "molecule": "8 H2O, seed=rank, 8 A cube", "nbf": n, "nocc": r["nocc"],
-                   "global_batch": world, "scf": "DIIS", "schwarz": 1e-12, "mp2": args.mp2,
-                   "l2": "no flush: each step rebuilds a 1.6 GB packed ERI array (> 129 MB L2)",
+        "config": {"workload": WORKLOAD if args.waters == 8 else f"water{args.waters}_631gss_rhf_diis_schwarz1e-12_mp2",
+                   "molecule": f"{args.waters} H2O, seed=rank, {8.0 * (args.waters / 8) ** (1 / 3):.2f} A cube",
+                   "nbf": n, "nocc": r["nocc"],
+                   "global_batch": world, "scf": "DIIS + SP2 purification", "schwarz": 1e-12, "mp2": main_mp2,
+                   "l2": f"no flush: each step rebuilds the {8 * (n * (n + 1) // 2) * (n * (n + 1) // 2 + 1) // 2 / 1e9:.1f} GB "
+                         "packed ERI array (> 129 MB L2)",
                    "parallelism": f"replicas x{world}"},
         "results": {"Etot": r["Etot"], "E2": r["E2"], "niter": r["niter"]},
-        "stages_ms": {"setup": r["ms_setup"], "eri": eri_ms, "scf": r["ms_scf"], "mp2": r["ms_mp2"],
-                      "total": r["ms_total"]},
+        "mixed_vs_plain": {"plain_fp64_molecules_per_s": world * len(res_o) / (ms_o * 1e-3)
+                           if main_mp2 == "split_bf16" else world * args.steps / (ms * 1e-3),
+                           "mixed_molecules_per_s": world * args.steps / (ms * 1e-3)
+                           if main_mp2 == "split_bf16" else world * len(res_o) / (ms_o * 1e-3),
+                           "dE2": abs(mixed["E2"] - plain["E2"]), "dEtot": abs(mixed["Etot"] - plain["Etot"]),
+                           "mp2_ms": {"mixed": mixed["ms_mp2"], "plain_fp64": plain["ms_mp2"]}},
+        "stages_ms": {"setup": avg("ms_setup"), "eri": eri_ms, "scf": avg("ms_scf"), "fock": fock_ms,
+                      "mp2": avg("ms_mp2"), "tcgemm": tc_ms, "total": avg("ms_total")},
         "eri": {"quartets_per_s": r["n_bf_quartets"] / (eri_ms * 1e-3), "bf_quartets": r["n_bf_quartets"],
                 "shell_quartets": r["n_quartets"], "prim_quartets": r["n_prim_quartets"],
                 "md_flops": r["eri_flops"]},
-        "roofline": {"kernel": "eri_class_kernel (all classes of one ERI pass)", "bound": "fp64",
-                     "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s", "frac": achieved / peak.value,
-                     "peak_source": "measured: hfgpu_probe_fp64_tflops (FP64 FMA, this GPU)",
-                     "traffic": None},
+        "roofline": dominant,
+        "rooflines": roof,
         "e2e": {"value": world * args.steps / (ms_e2e * 1e-3), "unit": "molecules/s",
                 "h2d_bytes_per_step": int(xyz.size * 8 + len(atno) * 4),
                 "d2h_bytes_per_step": int((n * n + n) * 8 + ctypes.sizeof(_lib.Result))},
@@ -286,7 +334,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mp2", default="fp64", choices=["fp64", "split_bf16"])
+    ap.add_argument("--mp2", default="split_bf16", choices=["fp64", "split_bf16"],
+                    help="MBPT2 precision of the headline pipeline (the other one is timed beside it)")
+    ap.add_argument("--waters", type=int, default=8,
+                    help="cluster size (8: 200 functions, the headline workload; 16: 400 functions)")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the CPU-baseline sample (profiling runs)")
     args = ap.parse_args()

@@ -22,7 +22,7 @@ class Options(ctypes.Structure):
     _fields_ = [("nscf", ctypes.c_int), ("mix_alpha", ctypes.c_double), ("tolE", ctypes.c_double),
                 ("tolP", ctypes.c_double), ("scf_accel", ctypes.c_int), ("diis_size", ctypes.c_int),
                 ("schwarz", ctypes.c_double), ("mp2", ctypes.c_int), ("mp2_nocc", ctypes.c_int),
-                ("reserved", ctypes.c_int * 8)]
+                ("purify", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
 
 class Result(ctypes.Structure):
@@ -33,7 +33,8 @@ class Result(ctypes.Structure):
                 ("n_bf_quartets", ctypes.c_int64), ("n_prim_quartets", ctypes.c_int64),
                 ("eri_flops", ctypes.c_double), ("ms_eri", ctypes.c_double), ("ms_scf", ctypes.c_double),
                 ("ms_mp2", ctypes.c_double), ("ms_total", ctypes.c_double), ("ms_setup", ctypes.c_double),
-                ("reserved", ctypes.c_double * 7)]
+                ("ms_fock", ctypes.c_double), ("ms_tcgemm", ctypes.c_double), ("tc_flops", ctypes.c_double),
+                ("ms_grad", ctypes.c_double), ("reserved", ctypes.c_double * 3)]
 
 
 # name -> (restype, argtypes); the list every test of the ABI checks against
@@ -53,6 +54,8 @@ SIGNATURES = {
     "hfgpu_doscf": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp, _ip]),
     "hfgpu_formG": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
+    "hfgpu_jk": (ctypes.c_int, _BASIS + [_dp, ctypes.c_double, _dp, _dp]),
+    "hfgpu_mp2_energy": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, ctypes.c_int, _dp]),
     "hfgpu_formG_device_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                   ctypes.c_void_p]),
     "hfgpu_transform_int2": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
@@ -60,8 +63,12 @@ SIGNATURES = {
     "hfgpu_dgemm_sliced": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]),
     "hfgpu_default_options": (None, [ctypes.POINTER(Options)]),
     "hfgpu_basis_size": (ctypes.c_int, [ctypes.c_int, _ip]),
+    "hfgpu_rhf_batch": (ctypes.c_int, [ctypes.c_int, _ip, _ip, _dp, ctypes.POINTER(Options),
+                                       ctypes.POINTER(Result)]),
     "hfgpu_rhf": (ctypes.c_int, [ctypes.c_int, _ip, _dp, ctypes.POINTER(Options), ctypes.POINTER(Result), _dp,
                                  _dp]),
+    "hfgpu_rhf_gradient": (ctypes.c_int, [ctypes.c_int, _ip, _dp, ctypes.POINTER(Options), ctypes.POINTER(Result),
+                                          _dp]),
 }
 
 _LIB = None

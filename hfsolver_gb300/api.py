@@ -10,6 +10,9 @@ getInts                src/qc.c:95-131                                 hfgpu_get
 getints2               src/gaussians_hfsolver.f90:13-34 (plugin)       hfgpu_getints2
 doscf                  src/scf.f90:72-136                              hfgpu_doscf
 formG                  src/scf.f90:26-58                               hfgpu_formG
+jk                     J and K of TT, src/scf.f90:84-105               hfgpu_jk
+mp2_energy             transform_int2 + mbpt2 (E2 only)                hfgpu_mp2_energy
+rhf_batch              rhf_gauss over many molecules                   hfgpu_rhf_batch
 transform_int2         src/mbpt.f90:11-79                              hfgpu_transform_int2
 mbpt2                  src/mbpt.f90:154-159, src/mbpt2.f90:8-31        hfgpu_mbpt2
 rhf_gauss / rhf        src/drivers.f90:12-51 (+ MBPT2)                 hfgpu_rhf
@@ -135,6 +138,30 @@ def doscf(H, int2, S, Noccupied, Nscf, tolE, tolP, alpha):
     return C, P, lam, float(E0[0]), int(it[0])
 
 
+def jk(nprim, istart, xcenter, ycenter, zcenter, lpower, mpower, npower, coef, alpha, P, schwarz=0.0):
+    """(J, K) of density P for a basis in the C-driver layout (integrals stay on the device)."""
+    n, args, keep = _basis_args(nprim, istart, xcenter, ycenter, zcenter, lpower, mpower, npower, coef, alpha)
+    P = np.asfortranarray(P, dtype=np.float64)
+    J = np.zeros((n, n), order="F")
+    K = np.zeros((n, n), order="F")
+    _check(_lib.lib().hfgpu_jk(*args, P.ctypes.data_as(_dp), float(schwarz), J.ctypes.data_as(_dp),
+                               K.ctypes.data_as(_dp)))
+    return J, K
+
+
+def mp2_energy(int2, C, lam, Noccupied, precision="fp64"):
+    """E2 of transform_int2 + mbpt2 without the packed MO array (only (ia|jb))."""
+    C = np.asfortranarray(C, dtype=np.float64)
+    int2, lam = _f64(int2), _f64(lam)
+    n = C.shape[0]
+    if int2.size != packed_size(n):
+        raise ValueError("int2 has the wrong length")
+    E2 = np.zeros(1)
+    prec = {"fp64": _lib.MP2_FP64, "split_bf16": _lib.MP2_SPLIT_BF16}[precision]
+    _check(_lib.lib().hfgpu_mp2_energy(n, _d(int2), C.ctypes.data_as(_dp), _d(lam), int(Noccupied), prec, _d(E2)))
+    return float(E2[0])
+
+
 def formG(P, int2):
     """G = J - K/2 from the packed integrals (scf.f90:26-58)."""
     P = np.asfortranarray(P, dtype=np.float64)
@@ -174,6 +201,7 @@ class RHFOptions:
     schwarz: float = 0.0
     mp2: str = "fp64"          # "none" | "fp64" | "split_bf16"
     mp2_nocc: int = 0          # <= 0: sum(Z)/2
+    purify: bool = False       # SP2 density purification instead of an eigensolve per iteration
 
     def to_c(self):
         o = _lib.Options()
@@ -184,6 +212,7 @@ class RHFOptions:
         o.schwarz = self.schwarz
         o.mp2 = {"none": _lib.MP2_NONE, "fp64": _lib.MP2_FP64, "split_bf16": _lib.MP2_SPLIT_BF16}[self.mp2]
         o.mp2_nocc = self.mp2_nocc
+        o.purify = 1 if self.purify else 0
         return o
 
 
@@ -211,6 +240,36 @@ def rhf(atno, xyz, options=None, want_orbitals=False):
     out = {k: getattr(res, k) for k, _ in _lib.Result._fields_ if k != "reserved"}
     if want_orbitals:
         out["C"], out["lam"] = C, lam
+    return out
+
+
+def rhf_gradient(atno, xyz, options=None):
+    """Analytic RHF nuclear gradient dE_tot/dR (Ha/bohr, natoms x 3) at the
+    converged SCF of rhf(atno, xyz, options); returns (result dict, gradient).
+    Forces for the md.f90 integrators are -gradient (src/md.f90:13-20)."""
+    opt = (options or RHFOptions(mp2="none")).to_c()
+    at = _i32(atno)
+    xyz = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64).reshape(len(at), 3))
+    res = _lib.Result()
+    g = np.zeros((len(at), 3))
+    code = _lib.lib().hfgpu_rhf_gradient(len(at), _i(at), _d(xyz), opt, res, _d(g))
+    _check(code)
+    out = {k: getattr(res, k) for k, _ in _lib.Result._fields_ if k != "reserved"}
+    return out, g
+
+
+def rhf_batch(molecules, options=None):
+    """hfgpu_rhf over a list of (atno, xyz) molecules in one call; returns a list
+    of result dicts (a failed molecule has niter = -status)."""
+    opt = (options or RHFOptions()).to_c()
+    natoms = _i32([len(a) for a, _ in molecules])
+    atno = _i32(np.concatenate([np.asarray(a) for a, _ in molecules]))
+    xyz = _f64(np.concatenate([np.asarray(x, dtype=np.float64).reshape(-1, 3) for _, x in molecules]).ravel())
+    res = (_lib.Result * len(molecules))()
+    code = _lib.lib().hfgpu_rhf_batch(len(molecules), _i(natoms), _i(atno), _d(xyz), opt, res)
+    out = [{k: getattr(r, k) for k, _ in _lib.Result._fields_ if k != "reserved"} for r in res]
+    if code not in (_lib.OK, _lib.ERR_NOT_CONVERGED):
+        _check(code)
     return out
 
 

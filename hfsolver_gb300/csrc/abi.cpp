@@ -1,5 +1,6 @@
 // extern "C" entry points of libhfgpu (declared in include/hfgpu.h).
 #include <chrono>
+#include <memory>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -94,6 +95,105 @@ void ints_dropin(const Basis& b, double* Ints, double schwarz, EriStats* st)
 }
 
 }  // namespace
+
+static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu_options* opt_in, hfgpu_result* res,
+                     double* C, double* lam, int& conv, int& nscf, double* grad = nullptr)
+{
+        check_ptr(atno, "atno"); check_ptr(xyz, "xyz"); check_ptr(res, "res");
+        hfgpu_options opt;
+        if (opt_in) opt = *opt_in; else hfgpu_default_options(&opt);
+        nscf = opt.nscf;
+        HF_CHECK(opt.nscf >= 1, HFGPU_ERR_INVALID, "nscf must be >= 1");
+        HF_CHECK(opt.mp2 >= HFGPU_MP2_NONE && opt.mp2 <= HFGPU_MP2_SPLIT_BF16, HFGPU_ERR_INVALID,
+                 "unknown MP2 precision");
+        std::memset(res, 0, sizeof(*res));
+        Basis b = build_basis(natoms, atno, xyz);  // validates the input before any device work
+        Context& ctx = context();
+        cudaStream_t st = ctx.stream;
+        ctx.stat_fock_ms = ctx.stat_tc_ms = ctx.stat_tc_flops = 0;
+        Timer total(st);
+        const int n = b.nbf;
+        int nelec = 0;
+        for (int i = 0; i < natoms; i++) nelec += atno[i];
+        const int nocc = nelec / 2;
+        const size_t nn = (size_t)n * n;
+        res->nbf = n;
+        res->nocc = nocc;
+        res->nshell = (int)b.shells.size();
+        std::vector<double> x(natoms), y(natoms), z(natoms);
+        for (int i = 0; i < natoms; i++) { x[i] = xyz[3 * i]; y[i] = xyz[3 * i + 1]; z[i] = xyz[3 * i + 2]; }
+        DBuf<double> dS(nn, st), dT(nn, st), dV(nn, st), dH(nn, st);
+        onee_compute(ctx, b, natoms, atno, x.data(), y.data(), z.data(), dS.p, dT.p, dV.p);
+        {
+            const double one = 1.0;
+            HF_CUBLAS(cublasDgeam(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, &one, dT.p, n, &one, dV.p, n, dH.p, n));
+        }
+        // integrals, resident in HBM for the whole SCF
+        DBuf<double> dI(packed_size(n), st);
+        dI.zero();
+        EriStats es;
+        std::unique_ptr<EriPlan, void (*)(EriPlan*)> plan(eri_plan_create(ctx, b, opt.schwarz), eri_plan_destroy);
+        res->ms_setup = total.ms();
+        // the packed array feeds MBPT2; the screened quartet blocks feed every Fock build
+        eri_compute(ctx, plan.get(), dI.p, true, &es);
+        res->ms_eri = es.ms;
+        res->n_quartets = es.n_quartets;
+        res->n_bf_quartets = es.n_bf_quartets;
+        res->n_prim_quartets = es.n_prim_quartets;
+        res->eri_flops = es.flops;
+        // SCF
+        Timer ts(st);
+        DBuf<double> dC(nn, st), dP(nn, st), dL(n, st);
+        ScfIn in;
+        in.n = n; in.nocc = nocc; in.nscf = opt.nscf; in.dH = dH.p; in.dS = dS.p; in.d_int2 = dI.p;
+        in.tolE = opt.tolE; in.tolP = opt.tolP; in.alpha = opt.mix_alpha;
+        in.accel = opt.scf_accel; in.diis_size = opt.diis_size > 0 ? opt.diis_size : 8;
+        in.purify = opt.purify != 0;
+        in.direct_jk = [](Context& c, void* user, const double* P, double* G) {
+            eri_digest(c, (EriPlan*)user, P, G);
+        };
+        in.direct_ctx = plan.get();
+        ScfOut so = run_scf(ctx, in, dC.p, dP.p, dL.p);
+        res->ms_scf = ts.ms();
+        conv = so.converged;
+        double Enuc = 0;
+        for (int i = 0; i < natoms; i++)
+            for (int j = 0; j < i; j++) {
+                double dx = xyz[3 * i] - xyz[3 * j], dy = xyz[3 * i + 1] - xyz[3 * j + 1],
+                       dz = xyz[3 * i + 2] - xyz[3 * j + 2];
+                Enuc += atno[i] * atno[j] / std::sqrt(dx * dx + dy * dy + dz * dz);
+            }
+        res->E0 = so.E0;
+        res->Enuc = Enuc;
+        res->Etot = so.E0 + Enuc;
+        res->Ekin = device_dot(ctx, (int64_t)nn, dP.p, dT.p);
+        res->dP = so.dP;
+        res->niter = so.niter;
+        // MBPT2
+        if (conv && opt.mp2 != HFGPU_MP2_NONE) {
+            Timer tm(st);
+            const int mo = opt.mp2_nocc > 0 ? opt.mp2_nocc : nocc;
+            HF_CHECK(mo <= n, HFGPU_ERR_INVALID, "mp2_nocc larger than the basis");
+            const int mv = n - mo;
+            if (mo > 0 && mv > 0 && opt.mp2 == HFGPU_MP2_SPLIT_BF16) {
+                res->E2 = mp2_energy_mixed(ctx, n, dI.p, dC.p, mo, dL.p);
+            } else if (mo > 0 && mv > 0) {
+                DBuf<double> iajb((size_t)mo * mv * mo * mv, st);
+                ao2mo_fp64(ctx, n, dI.p, dC.p, mo, dC.p + (size_t)n * mo, mv, iajb.p);
+                res->E2 = mp2_energy(ctx, mo, mv, iajb.p, dL.p);
+            }
+            res->ms_mp2 = tm.ms();
+        }
+        // analytic nuclear gradient at the converged orbitals
+        if (conv && grad) rhf_gradient(ctx, plan.get(), natoms, atno, xyz, dC.p, dL.p, nocc, grad, &res->ms_grad);
+        if (C) dC.download(C, nn);
+        if (lam) dL.download(lam, n);
+        HF_CUDA(cudaStreamSynchronize(st));
+        res->ms_total = total.ms();
+        res->ms_fock = ctx.stat_fock_ms;
+        res->ms_tcgemm = ctx.stat_tc_ms;
+        res->tc_flops = ctx.stat_tc_flops;
+}
 
 extern "C" {
 
@@ -208,6 +308,63 @@ int hfgpu_formG(int n, const double* P, const double* int2, double* G)
     });
 }
 
+int hfgpu_jk(int nbf, const int* nprim, const int* istart, const double* xc, const double* yc, const double* zc,
+             const int* lp, const int* mp, const int* np, int n2, const double* coef, const double* alpha,
+             const double* P, double schwarz, double* J, double* K)
+{
+    return guard([&] {
+        check_ptr(P, "P"); check_ptr(J, "J"); check_ptr(K, "K");
+        HF_CHECK(schwarz >= 0, HFGPU_ERR_INVALID, "schwarz must be >= 0");
+        Basis b = basis_from_functions(nbf, nprim, istart, xc, yc, zc, lp, mp, np, n2, coef, alpha);
+        Context& ctx = context();
+        const size_t nn = (size_t)nbf * nbf;
+        DBuf<double> dI(packed_size(nbf), ctx.stream), dP(nn, ctx.stream), dJ(nn, ctx.stream), dK(nn, ctx.stream);
+        dI.zero();
+        dP.upload(P, nn);
+        EriPlan* plan = eri_plan_create(ctx, b, schwarz);
+        try {
+            eri_compute_packed(ctx, plan, dI.p, nullptr);
+        } catch (...) {
+            eri_plan_destroy(plan);
+            throw;
+        }
+        eri_plan_destroy(plan);
+        jk_separate_from_packed(ctx, nbf, dI.p, dP.p, dJ.p, dK.p);
+        dJ.download(J, nn);
+        dK.download(K, nn);
+        HF_CUDA(cudaStreamSynchronize(ctx.stream));
+    });
+}
+
+int hfgpu_mp2_energy(int n, const double* int2, const double* C, const double* lam, int nocc, int precision,
+                     double* E2)
+{
+    return guard([&] {
+        HF_CHECK(n >= 1 && nocc >= 0 && nocc <= n, HFGPU_ERR_INVALID, "invalid sizes");
+        HF_CHECK(precision == HFGPU_MP2_FP64 || precision == HFGPU_MP2_SPLIT_BF16, HFGPU_ERR_INVALID,
+                 "precision must be HFGPU_MP2_FP64 or HFGPU_MP2_SPLIT_BF16");
+        check_ptr(int2, "int2"); check_ptr(C, "C"); check_ptr(lam, "lam"); check_ptr(E2, "E2");
+        Context& ctx = context();
+        const size_t nn = (size_t)n * n;
+        DBuf<double> dI(packed_size(n), ctx.stream), dC(nn, ctx.stream), dL(n, ctx.stream);
+        dI.upload(int2, packed_size(n));
+        dC.upload(C, nn);
+        dL.upload(lam, n);
+        const int v = n - nocc;
+        double e = 0.0;
+        if (nocc > 0 && v > 0) {
+            if (precision == HFGPU_MP2_SPLIT_BF16) {
+                e = mp2_energy_mixed(ctx, n, dI.p, dC.p, nocc, dL.p);
+            } else {
+                DBuf<double> iajb((size_t)nocc * v * nocc * v, ctx.stream);
+                ao2mo_fp64(ctx, n, dI.p, dC.p, nocc, dC.p + (size_t)n * nocc, v, iajb.p);
+                e = mp2_energy(ctx, nocc, v, iajb.p, dL.p);
+            }
+        }
+        *E2 = e;
+    });
+}
+
 int hfgpu_transform_int2(int n, const double* int2, const double* C, double* moint2)
 {
     return guard([&] {
@@ -298,103 +455,48 @@ int hfgpu_basis_size(int natoms, const int* atno)
 int hfgpu_rhf(int natoms, const int* atno, const double* xyz, const hfgpu_options* opt_in, hfgpu_result* res,
               double* C, double* lam)
 {
-    int conv = 1;
-    int nscf = 0;
+    int conv = 1, nscf = 0;
+    int rc = guard([&] { rhf_impl(natoms, atno, xyz, opt_in, res, C, lam, conv, nscf); });
+    if (rc == HFGPU_OK && !conv) {
+        set_last_error("SCF did not converge in " + std::to_string(nscf) + " iterations.");
+        return HFGPU_ERR_NOT_CONVERGED;
+    }
+    return rc;
+}
+
+int hfgpu_rhf_gradient(int natoms, const int* atno, const double* xyz, const hfgpu_options* opt_in,
+                       hfgpu_result* res, double* grad)
+{
+    int conv = 1, nscf = 0;
     int rc = guard([&] {
-        check_ptr(atno, "atno"); check_ptr(xyz, "xyz"); check_ptr(res, "res");
-        hfgpu_options opt;
-        if (opt_in) opt = *opt_in; else hfgpu_default_options(&opt);
-        nscf = opt.nscf;
-        HF_CHECK(opt.nscf >= 1, HFGPU_ERR_INVALID, "nscf must be >= 1");
-        HF_CHECK(opt.mp2 >= HFGPU_MP2_NONE && opt.mp2 <= HFGPU_MP2_SPLIT_BF16, HFGPU_ERR_INVALID,
-                 "unknown MP2 precision");
-        std::memset(res, 0, sizeof(*res));
-        Basis b = build_basis(natoms, atno, xyz);  // validates the input before any device work
-        Context& ctx = context();
-        cudaStream_t st = ctx.stream;
-        Timer total(st);
-        const int n = b.nbf;
-        int nelec = 0;
-        for (int i = 0; i < natoms; i++) nelec += atno[i];
-        const int nocc = nelec / 2;
-        const size_t nn = (size_t)n * n;
-        res->nbf = n;
-        res->nocc = nocc;
-        res->nshell = (int)b.shells.size();
-        std::vector<double> x(natoms), y(natoms), z(natoms);
-        for (int i = 0; i < natoms; i++) { x[i] = xyz[3 * i]; y[i] = xyz[3 * i + 1]; z[i] = xyz[3 * i + 2]; }
-        DBuf<double> dS(nn, st), dT(nn, st), dV(nn, st), dH(nn, st);
-        onee_compute(ctx, b, natoms, atno, x.data(), y.data(), z.data(), dS.p, dT.p, dV.p);
-        {
-            const double one = 1.0;
-            HF_CUBLAS(cublasDgeam(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, &one, dT.p, n, &one, dV.p, n, dH.p, n));
-        }
-        // integrals, resident in HBM for the whole SCF
-        DBuf<double> dI(packed_size(n), st);
-        dI.zero();
-        EriStats es;
-        EriPlan* plan = eri_plan_create(ctx, b, opt.schwarz);
-        res->ms_setup = total.ms();
-        try {
-            eri_compute_packed(ctx, plan, dI.p, &es);
-        } catch (...) {
-            eri_plan_destroy(plan);
-            throw;
-        }
-        eri_plan_destroy(plan);
-        res->ms_eri = es.ms;
-        res->n_quartets = es.n_quartets;
-        res->n_bf_quartets = es.n_bf_quartets;
-        res->n_prim_quartets = es.n_prim_quartets;
-        res->eri_flops = es.flops;
-        // SCF
-        Timer ts(st);
-        DBuf<double> dC(nn, st), dP(nn, st), dL(n, st);
-        ScfIn in;
-        in.n = n; in.nocc = nocc; in.nscf = opt.nscf; in.dH = dH.p; in.dS = dS.p; in.d_int2 = dI.p;
-        in.tolE = opt.tolE; in.tolP = opt.tolP; in.alpha = opt.mix_alpha;
-        in.accel = opt.scf_accel; in.diis_size = opt.diis_size > 0 ? opt.diis_size : 8;
-        ScfOut so = run_scf(ctx, in, dC.p, dP.p, dL.p);
-        res->ms_scf = ts.ms();
-        conv = so.converged;
-        double Enuc = 0;
-        for (int i = 0; i < natoms; i++)
-            for (int j = 0; j < i; j++) {
-                double dx = xyz[3 * i] - xyz[3 * j], dy = xyz[3 * i + 1] - xyz[3 * j + 1],
-                       dz = xyz[3 * i + 2] - xyz[3 * j + 2];
-                Enuc += atno[i] * atno[j] / std::sqrt(dx * dx + dy * dy + dz * dz);
-            }
-        res->E0 = so.E0;
-        res->Enuc = Enuc;
-        res->Etot = so.E0 + Enuc;
-        res->Ekin = device_dot(ctx, (int64_t)nn, dP.p, dT.p);
-        res->dP = so.dP;
-        res->niter = so.niter;
-        // MBPT2
-        if (conv && opt.mp2 != HFGPU_MP2_NONE) {
-            Timer tm(st);
-            const int mo = opt.mp2_nocc > 0 ? opt.mp2_nocc : nocc;
-            HF_CHECK(mo <= n, HFGPU_ERR_INVALID, "mp2_nocc larger than the basis");
-            const int mv = n - mo;
-            if (mo > 0 && mv > 0 && opt.mp2 == HFGPU_MP2_SPLIT_BF16) {
-                res->E2 = mp2_energy_mixed(ctx, n, dI.p, dC.p, mo, dL.p);
-            } else if (mo > 0 && mv > 0) {
-                DBuf<double> iajb((size_t)mo * mv * mo * mv, st);
-                ao2mo_fp64(ctx, n, dI.p, dC.p, mo, dC.p + (size_t)n * mo, mv, iajb.p);
-                res->E2 = mp2_energy(ctx, mo, mv, iajb.p, dL.p);
-            }
-            res->ms_mp2 = tm.ms();
-        }
-        if (C) dC.download(C, nn);
-        if (lam) dL.download(lam, n);
-        HF_CUDA(cudaStreamSynchronize(st));
-        res->ms_total = total.ms();
+        check_ptr(grad, "grad");
+        rhf_impl(natoms, atno, xyz, opt_in, res, nullptr, nullptr, conv, nscf, grad);
     });
     if (rc == HFGPU_OK && !conv) {
         set_last_error("SCF did not converge in " + std::to_string(nscf) + " iterations.");
         return HFGPU_ERR_NOT_CONVERGED;
     }
     return rc;
+}
+
+int hfgpu_rhf_batch(int nmol, const int* natoms, const int* atno, const double* xyz, const hfgpu_options* opt,
+                    hfgpu_result* res)
+{
+    if (nmol < 0 || (nmol > 0 && (!natoms || !atno || !xyz || !res))) {
+        set_last_error("hfgpu_rhf_batch: invalid arguments");
+        return HFGPU_ERR_INVALID;
+    }
+    int64_t a0 = 0;
+    int first = HFGPU_OK;
+    for (int m = 0; m < nmol; ++m) {
+        int rc = hfgpu_rhf(natoms[m], atno + a0, xyz + 3 * a0, opt, &res[m], nullptr, nullptr);
+        if (rc != HFGPU_OK) {
+            res[m].niter = -rc;
+            if (first == HFGPU_OK) first = rc;
+        }
+        a0 += natoms[m] > 0 ? natoms[m] : 0;
+    }
+    return first;
 }
 
 }  // extern "C"

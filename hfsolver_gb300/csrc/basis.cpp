@@ -79,6 +79,7 @@ Basis build_basis(int natoms, const int* atno, const double* xyz)
             sh.L = k631_shell_l[s];
             HF_CHECK(sh.L <= 2, HFGPU_ERR_UNSUPPORTED, "angular momentum above d is not supported");
             sh.nprim = k631_shell_nprim[s];
+            sh.atom = i;
             sh.x = xyz[3 * i];
             sh.y = xyz[3 * i + 1];
             sh.z = xyz[3 * i + 2];

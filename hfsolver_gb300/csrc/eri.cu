@@ -32,6 +32,8 @@
 #include "boys.cuh"
 #include "eri_kernel.cuh"
 #include "internal.h"
+#include "eri_plan.h"
+#include "jk_blocks.cuh"
 #include "md.cuh"
 
 namespace hfgpu {
@@ -156,6 +158,15 @@ static KernelFn get_kernel(int tb, int tk, int mode)
     return f;
 }
 
+// lanes per quartet for kb x kk primitive quartets: enough independent work per
+// lane (about 16 primitive quartets) without idling the rest of the warp
+static int pick_split(int64_t kprod)
+{
+    int s = 1;
+    while (s < 32 && kprod >= 32 * s) s <<= 1;
+    return s;
+}
+
 static int class_G(int tb, int tk)
 {
     int nab = ncart(ptype_la(tb)) * ncart(ptype_lb(tb));
@@ -173,42 +184,13 @@ double md_flops(int la, int lb, int lc, int ld)
            2.0 * ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) * nherm(Lp);
 }
 
-struct ClassPlan {
-    int tb, tk;
-    std::vector<Seg> segs;
-    int64_t nwarps = 0;
-    DBuf<Seg> dsegs;
-};
-
-struct EriPlan {
-    Basis basis;
-    int npair = 0;
-    // device basis
-    DBuf<int> sL, snp, sp0, sc0, scf, cfn;
-    DBuf<double> sxyz, alpha, coef;
-    // pairs
-    std::vector<int> pA, pB, pK, pT;
-    std::vector<int64_t> poff;
-    DBuf<int> dA, dB, dK;
-    DBuf<int64_t> doff;
-    DBuf<double> pdata;
-    // screening
-    std::vector<double> Q;
-    DBuf<int> gpairs;
-    DBuf<int64_t> prefix;
-    std::vector<ClassPlan> classes;
-    EriStats stats;
-    ShellDev shdev() const
-    {
-        return ShellDev{sL.p, snp.p, sxyz.p, sp0.p, sc0.p, scf.p, alpha.p, coef.p, cfn.p};
-    }
-    PairDev prdev() const { return PairDev{dA.p, dB.p, dK.p, doff.p, pdata.p}; }
-};
-
-static void launch_class(Context& ctx, EriPlan* P, ClassPlan& c, int mode, double* out, const int2* list)
+static void launch_class(Context& ctx, EriPlan* P, ClassPlan& c, int mode, double* out, const int2* list,
+                         double* blocks = nullptr)
 {
     if (c.nwarps == 0) return;
     EriArgs a;
+    a.blocks = blocks;
+    a.nq_class = c.nq;
     a.sh = P->shdev();
     a.pr = P->prdev();
     a.boys = ctx.boys;
@@ -219,8 +201,8 @@ static void launch_class(Context& ctx, EriPlan* P, ClassPlan& c, int mode, doubl
     a.nseg = (int)c.segs.size();
     a.nwarps = c.nwarps;
     a.out = out;
-    int64_t blocks = (c.nwarps + ERI_BLOCK / 32 - 1) / (ERI_BLOCK / 32);
-    get_kernel(c.tb, c.tk, mode)<<<(unsigned)blocks, ERI_BLOCK, 0, ctx.stream>>>(a);
+    const int64_t nblocks = (c.nwarps + ERI_BLOCK / 32 - 1) / (ERI_BLOCK / 32);
+    get_kernel(c.tb, c.tk, mode)<<<(unsigned)nblocks, ERI_BLOCK, 0, ctx.stream>>>(a);
     count_launch();
     HF_CUDA(cudaGetLastError());
 }
@@ -297,18 +279,21 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
                 Seg s{};
                 s.warp0 = 0; s.nq = (int64_t)g.second.size(); s.pref0 = (int64_t)dl.size();
                 s.list = 1;
+                s.qoff = 0;
+                s.split = pick_split((int64_t)g.first.second * g.first.second);
+                const int64_t qpw = 32 / s.split;
                 for (int id : g.second) dl.push_back(make_int2(id, id));
                 bool merged = false;
                 for (auto& dc : dcls)
                     if (dc.tb == t) {
                         s.warp0 = dc.nwarps;
                         dc.segs.push_back(s);
-                        dc.nwarps += (s.nq + 31) / 32 * class_G(t, t);
+                        dc.nwarps += (s.nq + qpw - 1) / qpw * class_G(t, t);
                         merged = true;
                     }
                 if (!merged) {
                     c.segs.push_back(s);
-                    c.nwarps = (s.nq + 31) / 32 * class_G(t, t);
+                    c.nwarps = (s.nq + qpw - 1) / qpw * class_G(t, t);
                     dcls.push_back(std::move(c));
                 }
             }
@@ -400,7 +385,11 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
                         }
                         s.nq = acc;
                         s.warp0 = c.nwarps;
-                        c.nwarps += (acc + 31) / 32 * G_;
+                        s.qoff = c.nq;
+                        s.split = pick_split((int64_t)A_.k * B_.k);
+                        const int64_t qpw = 32 / s.split;
+                        c.nq += acc;
+                        c.nwarps += (acc + qpw - 1) / qpw * G_;
                         c.segs.push_back(s);
                         stt.n_quartets += acc;
                         stt.n_bf_quartets += nbf;
@@ -424,17 +413,86 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
 }
 
 void eri_plan_destroy(EriPlan* p) { delete p; }
+
+__global__ void sym_kernel(int n, const double* __restrict__ Gh, double* G)
+{
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * n) return;
+    const int i = idx % n, j = idx / n;
+    G[idx] = Gh[idx] + Gh[j + (int64_t)i * n];
+}
+
+void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG)
+{
+    HF_CHECK(P->blocks.p != nullptr, HFGPU_ERR_INVALID, "eri_digest: integrals were not kept");
+    const int n = P->basis.nbf;
+    const int64_t nn = (int64_t)n * n;
+    DBuf<double> Gh(nn, ctx.stream);
+    Gh.zero();
+    cudaEvent_t e0, e1;
+    HF_CUDA(cudaEventCreate(&e0));
+    HF_CUDA(cudaEventCreate(&e1));
+    HF_CUDA(cudaEventRecord(e0, ctx.stream));
+    for (auto& c : P->classes) {
+        if (c.nq == 0) continue;
+        DigestArgs a;
+        a.sh = P->shdev();
+        a.pr = P->prdev();
+        a.gpairs = P->gpairs.p;
+        a.prefix = P->prefix.p;
+        a.list = nullptr;
+        a.segs = c.dsegs.p;
+        a.nseg = (int)c.segs.size();
+        a.nq = c.nq;
+        a.blocks = P->blocks.p + c.boff;
+        a.P = dP;
+        a.n = n;
+        a.Gh = Gh.p;
+        digest_fn(c.tb, c.tk)<<<(unsigned)((c.nq + 127) / 128), 128, 0, ctx.stream>>>(a);
+        count_launch();
+        HF_CUDA(cudaGetLastError());
+    }
+    sym_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, ctx.stream>>>(n, Gh.p, dG);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+    HF_CUDA(cudaEventRecord(e1, ctx.stream));
+    HF_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    HF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    ctx.stat_fock_ms += ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+}
 EriStats eri_plan_stats(const EriPlan* p) { return p->stats; }
 
 void eri_compute_packed(Context& ctx, EriPlan* P, double* d_out, EriStats* st)
 {
+    eri_compute(ctx, P, d_out, false, st);
+}
+
+static int block_size(int tb, int tk)
+{
+    return ncart(ptype_la(tb)) * ncart(ptype_lb(tb)) * ncart(ptype_la(tk)) * ncart(ptype_lb(tk));
+}
+
+void eri_compute(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks, EriStats* st)
+{
+    if (keep_blocks) {
+        int64_t total = 0;
+        for (auto& c : P->classes) {
+            c.boff = total;
+            total += c.nq * block_size(c.tb, c.tk);
+        }
+        P->blocks.alloc(std::max<int64_t>(total, 1), ctx.stream);
+    }
     cudaEvent_t e0, e1;
     HF_CUDA(cudaEventCreate(&e0));
     HF_CUDA(cudaEventCreate(&e1));
     HF_CUDA(cudaEventRecord(e0, ctx.stream));
     // heaviest classes first so the tail of the launch sequence is short
     for (int i = (int)P->classes.size() - 1; i >= 0; --i)
-        launch_class(ctx, P, P->classes[i], MODE_PACKED, d_out, nullptr);
+        launch_class(ctx, P, P->classes[i], MODE_PACKED, d_out, nullptr,
+                     keep_blocks ? P->blocks.p + P->classes[i].boff : nullptr);
     HF_CUDA(cudaEventRecord(e1, ctx.stream));
     HF_CUDA(cudaEventSynchronize(e1));
     float ms = 0;

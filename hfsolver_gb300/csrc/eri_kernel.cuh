@@ -35,9 +35,11 @@ struct Seg {
     int64_t warp0;   // first warp of the segment within its class launch
     int64_t nq;      // quartets
     int64_t pref0;   // prefix-sum offset (prefix mode) or list offset (list mode)
+    int64_t qoff;    // index of the segment's first quartet within its class
     int bra0, ket0;  // offsets into the grouped, sorted pair-id array
     int nbra;
     int list;        // 1: explicit (bra, ket) list
+    int split;       // lanes per quartet (power of two): they share its primitive pairs
 };
 
 enum { MODE_PACKED = 0, MODE_DIAG = 1 };
@@ -52,7 +54,9 @@ struct EriArgs {
     const Seg* segs;
     int nseg;
     int64_t nwarps;
-    double* out;  // packed integrals, or diagonal buffer [pair][36]
+    double* out;     // packed integrals (may be null), or diagonal buffer [pair][36]
+    double* blocks;  // class-wise quartet blocks [element][quartet] (may be null)
+    int64_t nq_class;
 };
 
 using KernelFn = void (*)(EriArgs);
@@ -80,7 +84,8 @@ template <int TB, int TK, int CH>
 struct EriBody;  // generated
 
 template <int TB, int TK, int MODE, int CH>
-__device__ __forceinline__ void run_chunk(const EriArgs& a, int bra, int ket, bool active)
+__device__ __forceinline__ void run_chunk(const EriArgs& a, int bra, int ket, bool active, int64_t qg, int sub,
+                                          int split)
 {
     using CI = ClassInfo<TB, TK>;
     double acc[CI::NAB * CI::NCD];
@@ -89,22 +94,27 @@ __device__ __forceinline__ void run_chunk(const EriArgs& a, int bra, int ket, bo
     const int kb = a.pr.K[bra], kk = a.pr.K[ket];
     const double* pb0 = a.pr.pdata + a.pr.off[bra];
     const double* pk0 = a.pr.pdata + a.pr.off[ket];
-    for (int ib = 0; ib < kb; ++ib) {
+    // the split lanes of a quartet take its primitive pairs in turn
+    for (int pp = sub; pp < kb * kk; pp += split) {
+        const int ib = pp / kk, ik = pp - ib * kk;
         const double* pb = pb0 + (int64_t)ib * CI::SB;
+        const double* pk = pk0 + (int64_t)ik * CI::SK;
         const double p = __ldg(pb), px = __ldg(pb + 1), py = __ldg(pb + 2), pz = __ldg(pb + 3);
-        for (int ik = 0; ik < kk; ++ik) {
-            const double* pk = pk0 + (int64_t)ik * CI::SK;
-            const double q = __ldg(pk), qx = __ldg(pk + 1), qy = __ldg(pk + 2), qz = __ldg(pk + 3);
-            const double r = rsqrt_nr(p + q);
-            const double alpha = p * q * (r * r);
-            const double X = px - qx, Y = py - qy, Z = pz - qz;
-            const double T = alpha * (X * X + Y * Y + Z * Z);
-            double F[CI::L + 1];
-            boys_scaled<CI::L>(T, TWO_PI_2_5 * r, -2.0 * alpha, a.boys, F);
-            EriBody<TB, TK, CH>::prim(acc, pb + PAIR_HDR, pk + PAIR_HDR, F, X, Y, Z);
-        }
+        const double q = __ldg(pk), qx = __ldg(pk + 1), qy = __ldg(pk + 2), qz = __ldg(pk + 3);
+        const double r = rsqrt_nr(p + q);
+        const double alpha = p * q * (r * r);
+        const double X = px - qx, Y = py - qy, Z = pz - qz;
+        const double T = alpha * (X * X + Y * Y + Z * Z);
+        double F[CI::L + 1];
+        boys_scaled<CI::L>(T, TWO_PI_2_5 * r, -2.0 * alpha, a.boys, F);
+        EriBody<TB, TK, CH>::prim(acc, pb + PAIR_HDR, pk + PAIR_HDR, F, X, Y, Z);
     }
-    if (!active) return;
+    if (split > 1) {  // sum the partial accumulators of the split lanes (aligned groups)
+#pragma unroll
+        for (int i = 0; i < CI::NAB * CI::NCD; ++i)
+            for (int o = split >> 1; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+    }
+    if (!active || sub != 0) return;
     if constexpr (MODE == MODE_DIAG) {
         // bra == ket: keep the diagonal values (ab|ab) for the Schwarz bound
 #pragma unroll
@@ -113,6 +123,14 @@ __device__ __forceinline__ void run_chunk(const EriArgs& a, int bra, int ket, bo
             a.out[(int64_t)ket * 36 + icd] = acc[icd * CI::NCD + s];
         }
     } else {
+        if (a.blocks) {  // the whole block, one element plane per component quartet (coalesced in q)
+#pragma unroll
+            for (int s = 0; s < CI::NCD; ++s)
+#pragma unroll
+                for (int ab = 0; ab < CI::NAB; ++ab)
+                    a.blocks[(int64_t)(ab * CI::NCDT + CH * CI::NCD + s) * a.nq_class + qg] = acc[ab * CI::NCD + s];
+        }
+        if (!a.out) return;
         const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
         const int* fa = a.sh.comp_fn + a.sh.cfn0[A];
         const int* fb = a.sh.comp_fn + a.sh.cfn0[B];
@@ -139,17 +157,19 @@ __device__ __forceinline__ void run_chunk(const EriArgs& a, int bra, int ket, bo
 }
 
 template <int TB, int TK, int MODE, int G, int CH>
-__device__ __forceinline__ void dispatch_chunk(const EriArgs& a, int chunk, int bra, int ket, bool active)
+__device__ __forceinline__ void dispatch_chunk(const EriArgs& a, int chunk, int bra, int ket, bool active, int64_t qg,
+                                               int sub, int split)
 {
     if constexpr (CH < G) {
         if (chunk == CH)
-            run_chunk<TB, TK, MODE, CH>(a, bra, ket, active);
+            run_chunk<TB, TK, MODE, CH>(a, bra, ket, active, qg, sub, split);
         else
-            dispatch_chunk<TB, TK, MODE, G, CH + 1>(a, chunk, bra, ket, active);
+            dispatch_chunk<TB, TK, MODE, G, CH + 1>(a, chunk, bra, ket, active, qg, sub, split);
     }
 }
 
-// One warp = 32 quartets of one segment for one ket chunk (warp-uniform).
+// One warp = 32/split quartets of one segment for one ket chunk (warp-uniform);
+// split lanes share each quartet's primitive pairs.
 template <int TB, int TK, int MODE>
 __global__ void __launch_bounds__(ERI_BLOCK) eri_class_kernel(EriArgs a)
 {
@@ -165,7 +185,9 @@ __global__ void __launch_bounds__(ERI_BLOCK) eri_class_kernel(EriArgs a)
     const Seg sg = a.segs[lo];
     const int64_t lw = w - sg.warp0;
     const int chunk = (int)(lw % CI::G);
-    int64_t q = (lw / CI::G) * 32 + lane;
+    const int split = sg.split;
+    const int sub = lane & (split - 1);
+    int64_t q = (lw / CI::G) * (32 / split) + lane / split;
     const bool active = q < sg.nq;
     if (!active) q = sg.nq - 1;
     int bra, ket;
@@ -183,7 +205,7 @@ __global__ void __launch_bounds__(ERI_BLOCK) eri_class_kernel(EriArgs a)
         bra = a.gpairs[sg.bra0 + l2];
         ket = a.gpairs[sg.ket0 + (int)(q - pf[l2])];
     }
-    dispatch_chunk<TB, TK, MODE, CI::G, 0>(a, chunk, bra, ket, active);
+    dispatch_chunk<TB, TK, MODE, CI::G, 0>(a, chunk, bra, ket, active, sg.qoff + q, sub, split);
 }
 
 template <int TB, int TK>

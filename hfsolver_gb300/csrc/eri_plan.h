@@ -1,0 +1,47 @@
+// Device-side integral plan of one molecule: basis, shell pairs with their
+// primitive-pair records, Schwarz bounds and the screened quartet segments of
+// every class.  Shared by the ERI, Fock-digest and gradient translation units.
+#pragma once
+#include <vector>
+
+#include "eri_kernel.cuh"
+#include "internal.h"
+
+namespace hfgpu {
+
+struct ClassPlan {
+    int tb, tk;
+    std::vector<Seg> segs;
+    int64_t nwarps = 0;
+    int64_t nq = 0;     // quartets of the class
+    int64_t boff = 0;   // offset of the class's blocks in EriPlan::blocks
+    DBuf<Seg> dsegs;
+};
+
+struct EriPlan {
+    Basis basis;
+    int npair = 0;
+    // device basis
+    DBuf<int> sL, snp, sp0, sc0, scf, cfn;
+    DBuf<double> sxyz, alpha, coef;
+    // pairs
+    std::vector<int> pA, pB, pK, pT;
+    std::vector<int64_t> poff;
+    DBuf<int> dA, dB, dK;
+    DBuf<int64_t> doff;
+    DBuf<double> pdata;
+    // screening
+    std::vector<double> Q;
+    DBuf<int> gpairs;
+    DBuf<int64_t> prefix;
+    std::vector<ClassPlan> classes;
+    DBuf<double> blocks;  // class-wise quartet blocks, kept for the SCF's Fock builds
+    EriStats stats;
+    ShellDev shdev() const
+    {
+        return ShellDev{sL.p, snp.p, sxyz.p, sp0.p, sc0.p, scf.p, alpha.p, coef.p, cfn.p};
+    }
+    PairDev prdev() const { return PairDev{dA.p, dB.p, dK.p, doff.p, pdata.p}; }
+};
+
+}  // namespace hfgpu

@@ -115,6 +115,8 @@ struct Context {
     cusolverDnHandle_t solver = nullptr;
     double* boys = nullptr;  // device copy of the Boys grid
     int num_sms = 0;
+    // kernel-time counters, reset by the pipeline entry points
+    double stat_fock_ms = 0, stat_tc_ms = 0, stat_tc_flops = 0;
 };
 Context& context();  // for the current device
 void count_launch(int n = 1);  // bookkeeping for hfgpu_kernel_launches
@@ -129,6 +131,7 @@ struct Shell {
     int prim0 = 0;   // offset of the exponents in Basis::alpha
     int coef0 = 0;   // offset of the ncart(L) x nprim coefficient block (component-major)
     int cfn0 = 0;    // offset in Basis::comp_fn
+    int atom = -1;   // index of the nucleus it sits on (-1: not built from atoms)
 };
 
 struct Basis {
@@ -163,6 +166,11 @@ void eri_plan_destroy(EriPlan* p);
 EriStats eri_plan_stats(const EriPlan* p);
 // all unique (ij|kl) into the packed array d_out (device, zeroed by the caller)
 void eri_compute_packed(Context& ctx, EriPlan* p, double* d_out, EriStats* st);
+// the same, d_out may be null; keep_blocks also keeps the screened quartet blocks
+// in HBM for eri_digest
+void eri_compute(Context& ctx, EriPlan* p, double* d_out, bool keep_blocks, EriStats* st);
+// G = J - K/2 of density dP from the kept quartet blocks (n x n)
+void eri_digest(Context& ctx, EriPlan* p, const double* dP, double* dG);
 
 // one-electron integrals (onee.cu): S, T, V on the device (n x n, symmetric)
 void onee_compute(Context& ctx, const Basis& b, int natoms, const int* atno, const double* x,
@@ -170,8 +178,15 @@ void onee_compute(Context& ctx, const Basis& b, int natoms, const int* atno, con
 
 // J/K (jk.cu): G = J - K/2 from packed integrals and density P (device)
 void jk_from_packed(Context& ctx, int n, const double* d_int2, const double* dP, double* dG);
+// J and K separately: J(i,j) = sum_kl (ij|kl) P(k,l), K(i,j) = sum_kl (ik|jl) P(k,l)
+void jk_separate_from_packed(Context& ctx, int n, const double* d_int2, const double* dP, double* dJ, double* dK);
 
 int64_t packed_size(int64_t n);
+
+// analytic RHF nuclear gradient (grad.cu) at converged orbitals dC, energies dL
+// (device, n x n and n); grad gets 3 values per atom (Ha/bohr), host memory
+void rhf_gradient(Context& ctx, EriPlan* plan, int natoms, const int* atno, const double* xyz, const double* dC,
+                  const double* dL, int nocc, double* grad, double* ms_grad);
 
 // probe.cu: measured FP64 FMA rate (TFLOP/s)
 double probe_fp64_tflops(Context& ctx);

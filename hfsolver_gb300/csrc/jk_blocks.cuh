@@ -1,0 +1,170 @@
+// Fock two-electron term G = J - K/2 from the class-wise quartet blocks that
+// the ERI kernels leave in HBM (EriArgs::blocks).
+//
+// Same G as formG (src/scf.f90:26-58) and as jk_packed_kernel, but only the
+// quartets that survived Schwarz screening are read (no zeros), reads are
+// coalesced (block element e of quartet q is at e * nq + q), and each thread
+// folds its whole quartet block into J/K partial sums before the atomics.
+//
+// Degeneracy: a block holds every component quartet of the shell quartet,
+// including both orders when A == B, C == D or bra pair == ket pair; weighting
+// every element by 1/2 per coincidence of shells makes the sum over the block
+// equal to the sum over unique integrals with the usual 8-fold weights.  The
+// half-matrix updates are those of jk.cu:
+//   Gh[a][b] += 2 w P_cd, Gh[c][d] += 2 w P_ab,
+//   Gh[a][c] -= w P_bd/2, Gh[b][c] -= w P_ad/2, Gh[a][d] -= w P_bc/2, Gh[b][d] -= w P_ac/2,
+// and G = Gh + Gh^T.
+#pragma once
+#include "eri_kernel.cuh"
+
+namespace hfgpu {
+
+struct DigestArgs {
+    ShellDev sh;
+    PairDev pr;
+    const int* gpairs;
+    const int64_t* prefix;
+    const int2* list;
+    const Seg* segs;
+    int nseg;
+    int64_t nq;
+    const double* blocks;
+    const double* P;
+    int n;
+    double* Gh;
+};
+
+template <int TB, int TK>
+__global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
+{
+    using CI = ClassInfo<TB, TK>;
+    constexpr int NA = ncart(CI::LA), NB = ncart(CI::LB), NC = ncart(CI::LC), ND = ncart(CI::LD);
+    const int64_t qg = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (qg >= a.nq) return;
+    int lo = 0, hi = a.nseg - 1;  // last segment with qoff <= qg
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.segs[mid].qoff <= qg) lo = mid; else hi = mid - 1;
+    }
+    const Seg sg = a.segs[lo];
+    const int64_t q = qg - sg.qoff;
+    int bra, ket;
+    if (sg.list) {
+        const int2 e = a.list[sg.pref0 + q];
+        bra = e.x;
+        ket = e.y;
+    } else {
+        const int64_t* pf = a.prefix + sg.pref0;
+        int l2 = 0, h2 = sg.nbra - 1;
+        while (l2 < h2) {
+            const int mid = (l2 + h2 + 1) >> 1;
+            if (pf[mid] <= q) l2 = mid; else h2 = mid - 1;
+        }
+        bra = a.gpairs[sg.bra0 + l2];
+        ket = a.gpairs[sg.ket0 + (int)(q - pf[l2])];
+    }
+    const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
+    int fa[NA], fb[NB], fc[NC], fd[ND];
+#pragma unroll
+    for (int i = 0; i < NA; ++i) fa[i] = a.sh.comp_fn[a.sh.cfn0[A] + i];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) fb[i] = a.sh.comp_fn[a.sh.cfn0[B] + i];
+#pragma unroll
+    for (int i = 0; i < NC; ++i) fc[i] = a.sh.comp_fn[a.sh.cfn0[C] + i];
+#pragma unroll
+    for (int i = 0; i < ND; ++i) fd[i] = a.sh.comp_fn[a.sh.cfn0[D] + i];
+    const int n = a.n;
+    auto Pv = [&](int x, int y) { return (x < 0 || y < 0) ? 0.0 : __ldg(a.P + x + (int64_t)y * n); };
+    const double f = (A == B ? 0.5 : 1.0) * (C == D ? 0.5 : 1.0) * (bra == ket ? 0.5 : 1.0);
+    // accumulators indexed by the rolled (a, b) loop live in local memory and are
+    // touched once per (a, b); everything indexed by (c, d) stays in registers
+    double jab[NA * NB], kac[NA * NC], kbc[NB * NC], kad[NA * ND], kbd[NB * ND];
+    double jcd[NC * ND], Pcd[NC * ND];
+#pragma unroll
+    for (int i = 0; i < NA * NB; ++i) jab[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < NA * NC; ++i) kac[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < NB * NC; ++i) kbc[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < NA * ND; ++i) kad[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < NB * ND; ++i) kbd[i] = 0.0;
+#pragma unroll
+    for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+        for (int id = 0; id < ND; ++id) {
+            jcd[ic * ND + id] = 0.0;
+            Pcd[ic * ND + id] = Pv(fc[ic], fd[id]);
+        }
+#pragma unroll 1
+    for (int ia = 0; ia < NA; ++ia)
+#pragma unroll 1
+        for (int ib = 0; ib < NB; ++ib) {
+            const double Pab = Pv(fa[ia], fb[ib]);
+            double Pac[NC], Pbc[NC], Pad[ND], Pbd[ND];
+#pragma unroll
+            for (int ic = 0; ic < NC; ++ic) {
+                Pac[ic] = Pv(fa[ia], fc[ic]);
+                Pbc[ic] = Pv(fb[ib], fc[ic]);
+            }
+#pragma unroll
+            for (int id = 0; id < ND; ++id) {
+                Pad[id] = Pv(fa[ia], fd[id]);
+                Pbd[id] = Pv(fb[ib], fd[id]);
+            }
+            double s_ab = 0.0, s_ad[ND], s_bd[ND];
+#pragma unroll
+            for (int id = 0; id < ND; ++id) s_ad[id] = s_bd[id] = 0.0;
+            const double* blk = a.blocks + (int64_t)((ia * NB + ib) * CI::NCDT) * a.nq + qg;
+#pragma unroll
+            for (int ic = 0; ic < NC; ++ic) {
+                double s_ac = 0.0, s_bc = 0.0;
+#pragma unroll
+                for (int id = 0; id < ND; ++id) {
+                    const double v = __ldg(blk + (int64_t)(ic * ND + id) * a.nq) * f;
+                    s_ab = fma(v, Pcd[ic * ND + id], s_ab);
+                    jcd[ic * ND + id] = fma(v, Pab, jcd[ic * ND + id]);
+                    s_ac = fma(v, Pbd[id], s_ac);
+                    s_bc = fma(v, Pad[id], s_bc);
+                    s_ad[id] = fma(v, Pbc[ic], s_ad[id]);
+                    s_bd[id] = fma(v, Pac[ic], s_bd[id]);
+                }
+                kac[ia * NC + ic] += s_ac;
+                kbc[ib * NC + ic] += s_bc;
+            }
+            jab[ia * NB + ib] += s_ab;
+#pragma unroll
+            for (int id = 0; id < ND; ++id) {
+                kad[ia * ND + id] += s_ad[id];
+                kbd[ib * ND + id] += s_bd[id];
+            }
+        }
+    double* Gh = a.Gh;
+    auto add = [&](int x, int y, double v) {
+        if (x >= 0 && y >= 0 && v != 0.0) atomicAdd(Gh + x + (int64_t)y * n, v);
+    };
+#pragma unroll 1
+    for (int ia = 0; ia < NA; ++ia)
+        for (int ib = 0; ib < NB; ++ib) add(fa[ia], fb[ib], 2.0 * jab[ia * NB + ib]);
+#pragma unroll 1
+    for (int ic = 0; ic < NC; ++ic)
+        for (int id = 0; id < ND; ++id) add(fc[ic], fd[id], 2.0 * jcd[ic * ND + id]);
+#pragma unroll 1
+    for (int ia = 0; ia < NA; ++ia)
+        for (int ic = 0; ic < NC; ++ic) add(fa[ia], fc[ic], -0.5 * kac[ia * NC + ic]);
+#pragma unroll 1
+    for (int ib = 0; ib < NB; ++ib)
+        for (int ic = 0; ic < NC; ++ic) add(fb[ib], fc[ic], -0.5 * kbc[ib * NC + ic]);
+#pragma unroll 1
+    for (int ia = 0; ia < NA; ++ia)
+        for (int id = 0; id < ND; ++id) add(fa[ia], fd[id], -0.5 * kad[ia * ND + id]);
+#pragma unroll 1
+    for (int ib = 0; ib < NB; ++ib)
+        for (int id = 0; id < ND; ++id) add(fb[ib], fd[id], -0.5 * kbd[ib * ND + id]);
+}
+
+using DigestFn = void (*)(DigestArgs);
+DigestFn digest_fn(int tb, int tk);  // jk_blocks.cu
+
+}  // namespace hfgpu

@@ -53,13 +53,13 @@ __device__ static void e1d(double (&E)[OE_LA + 1][OE_LB + 1][OE_T], int la, int 
 
 constexpr int OE_L = 4;  // largest l_a + l_b for s, p, d
 
-// R_tuv(p, PC) for t+u+v <= OE_L (Helgaker et al. eqs. 9.9.18-9.9.20)
-__device__ static void r_aux(double (&R)[OE_L + 1][nherm(OE_L)], const double (&F)[OE_L + 1], double X, double Y,
+// R_tuv(p, PC) for t+u+v <= L <= OE_L (Helgaker et al. eqs. 9.9.18-9.9.20)
+__device__ static void r_aux(int L, double (&R)[OE_L + 1][nherm(OE_L)], const double (&F)[OE_L + 1], double X, double Y,
                              double Z)
 {
-    for (int n = 0; n <= OE_L; ++n) R[n][0] = F[n];
-    for (int n = OE_L - 1; n >= 0; --n)
-        for (int s = 1; s <= OE_L - n; ++s)
+    for (int n = 0; n <= L; ++n) R[n][0] = F[n];
+    for (int n = L - 1; n >= 0; --n)
+        for (int s = 1; s <= L - n; ++s)
             for (int t = s; t >= 0; --t)
                 for (int v = 0; v <= s - t; ++v) {
                     int u = s - t - v;
@@ -82,9 +82,13 @@ __global__ void onee_kernel(FnDev f, int n, int nat, const int* __restrict__ Z, 
                             const double* __restrict__ boys, double* S, double* T, double* V)
 {
     const double PI = 3.14159265358979323846;
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n * n) return;
-    int i = idx % n, j = idx / n;
+    // one thread per lower-triangle element (i >= j), mirrored on output
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * (n + 1) / 2) return;
+    int i = (int)((sqrtf(8.0f * (float)idx + 1.0f) - 1.0f) * 0.5f);
+    while ((int64_t)i * (i + 1) / 2 > idx) --i;
+    while ((int64_t)(i + 1) * (i + 2) / 2 <= idx) ++i;
+    const int j = (int)(idx - (int64_t)i * (i + 1) / 2);
     int l1 = f.lmn[3 * i], m1 = f.lmn[3 * i + 1], n1 = f.lmn[3 * i + 2];
     int l2 = f.lmn[3 * j], m2 = f.lmn[3 * j + 1], n2 = f.lmn[3 * j + 2];
     double ax = f.xyz[3 * i], ay = f.xyz[3 * i + 1], az = f.xyz[3 * i + 2];
@@ -120,9 +124,17 @@ __global__ void onee_kernel(FnDev f, int n, int nat, const int* __restrict__ Z, 
             for (int c = 0; c < nat; ++c) {
                 double X = px - C[3 * c], Y = py - C[3 * c + 1], Zc = pz - C[3 * c + 2];
                 double F[OE_L + 1];
-                boys_scaled<OE_L>(p * (X * X + Y * Y + Zc * Zc), 1.0, -2.0 * p, boys, F);
+                const double Tc = p * (X * X + Y * Y + Zc * Zc);
+                const int L = l1 + l2 + m1 + m2 + n1 + n2;
+                switch (L) {  // Boys values up to the order this pair needs
+                    case 0: { double f[1]; boys_scaled<0>(Tc, 1.0, -2.0 * p, boys, f); F[0] = f[0]; break; }
+                    case 1: { double f[2]; boys_scaled<1>(Tc, 1.0, -2.0 * p, boys, f); for (int k = 0; k < 2; ++k) F[k] = f[k]; break; }
+                    case 2: { double f[3]; boys_scaled<2>(Tc, 1.0, -2.0 * p, boys, f); for (int k = 0; k < 3; ++k) F[k] = f[k]; break; }
+                    case 3: { double f[4]; boys_scaled<3>(Tc, 1.0, -2.0 * p, boys, f); for (int k = 0; k < 4; ++k) F[k] = f[k]; break; }
+                    default: boys_scaled<OE_L>(Tc, 1.0, -2.0 * p, boys, F); break;
+                }
                 double R[OE_L + 1][nherm(OE_L)];
-                r_aux(R, F, X, Y, Zc);
+                r_aux(L, R, F, X, Y, Zc);
                 double acc = 0;
                 for (int t = 0; t <= l1 + l2; ++t)
                     for (int u = 0; u <= m1 + m2; ++u)
@@ -132,9 +144,10 @@ __global__ void onee_kernel(FnDev f, int n, int nat, const int* __restrict__ Z, 
             }
             v_acc += cc * K * 2 * PI * ip * vsum;
         }
-    if (S) S[idx] = s_acc;
-    if (T) T[idx] = t_acc;
-    if (V) V[idx] = v_acc;
+    const int64_t o1 = i + (int64_t)j * n, o2 = j + (int64_t)i * n;
+    if (S) S[o1] = S[o2] = s_acc;
+    if (T) T[o1] = T[o2] = t_acc;
+    if (V) V[o1] = V[o2] = v_acc;
 }
 
 void onee_compute(Context& ctx, const Basis& b, int nat, const int* atno, const double* x, const double* y,
@@ -171,7 +184,8 @@ void onee_compute(Context& ctx, const Basis& b, int nat, const int* atno, const 
     auto dZ = to_device(Z, st);
     auto dC = to_device(C, st);
     FnDev f{dl.p, dn.p, da.p, dc.p, dx.p, dal.p, dco.p};
-    int blocks = (n * n + 127) / 128;
+    const int64_t npair = (int64_t)n * (n + 1) / 2;
+    const int blocks = (int)((npair + 127) / 128);
     onee_kernel<<<blocks, 128, 0, st>>>(f, n, nat, dZ.p, dC.p, ctx.boys, dS, dT, dV);
     count_launch();
     HF_CUDA(cudaGetLastError());

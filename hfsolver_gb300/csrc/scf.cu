@@ -78,6 +78,176 @@ static void reduce(Context& ctx, int mode, int64_t nn, const double* A, const do
 
 static unsigned nblk(int64_t n) { return (unsigned)((n + 255) / 256); }
 
+// ---- density by purification (SP2, Niklasson, Phys. Rev. B 66, 155115 (2002)) ----
+// Gershgorin bounds of a symmetric matrix: b[0] <= lowest, b[1] >= highest eigenvalue
+__global__ void gersh_kernel(int n, const double* __restrict__ A, double* b)
+{
+    __shared__ double lo[256], hi[256];
+    double l = 1e300, h = -1e300;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double r = 0;
+        for (int j = 0; j < n; ++j)
+            if (j != i) r += fabs(A[i + (int64_t)j * n]);
+        const double d = A[i + (int64_t)i * n];
+        l = fmin(l, d - r);
+        h = fmax(h, d + r);
+    }
+    lo[threadIdx.x] = l;
+    hi[threadIdx.x] = h;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            lo[threadIdx.x] = fmin(lo[threadIdx.x], lo[threadIdx.x + o]);
+            hi[threadIdx.x] = fmax(hi[threadIdx.x], hi[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        b[0] = lo[0];
+        b[1] = hi[0];
+    }
+}
+
+__global__ void scale_cols_kernel(int n, const double* __restrict__ U, const double* __restrict__ w, double* V)
+{
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * n) return;
+    V[idx] = U[idx] / sqrt(w[idx / n]);
+}
+
+// X2 = X X for symmetric X (n <= 1024), upper-triangle 16x16 tiles mirrored;
+// the diagonal of X2 is added to trX2 (one SP2 step's tr X^2).
+constexpr int SQ_T = 16;
+__global__ void __launch_bounds__(SQ_T* SQ_T) sym_square_kernel(int n, const double* __restrict__ X, double* X2,
+                                                                double* trX2)
+{
+    __shared__ double As[SQ_T][SQ_T + 1], Bs[SQ_T][SQ_T + 1];
+    // blockIdx.x -> tile pair (ti <= tj), row-major over the upper triangle
+    const int nt = (n + SQ_T - 1) / SQ_T;
+    int b = blockIdx.x, ti = 0;
+    while (b >= nt - ti) {
+        b -= nt - ti;
+        ++ti;
+    }
+    const int tj = ti + b;
+    const int ty = threadIdx.x / SQ_T, tx = threadIdx.x % SQ_T;
+    const int i = ti * SQ_T + ty, j = tj * SQ_T + tx;
+    double acc = 0.0;
+    for (int k0 = 0; k0 < n; k0 += SQ_T) {
+        const int ka = k0 + tx, kb = k0 + ty;
+        As[ty][tx] = (i < n && ka < n) ? X[i + (int64_t)ka * n] : 0.0;  // X[i][k]
+        Bs[ty][tx] = (kb < n && j < n) ? X[kb + (int64_t)j * n] : 0.0;  // X[k][j]
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < SQ_T; ++k) acc = fma(As[ty][k], Bs[k][tx], acc);
+        __syncthreads();
+    }
+    if (i < n && j < n) {
+        X2[i + (int64_t)j * n] = acc;
+        if (ti != tj) X2[j + (int64_t)i * n] = acc;
+        if (i == j) atomicAdd(trX2, acc);
+    }
+}
+
+// X = (emax I - F) / (emax - emin): spectrum mapped into [0, 1], occupied states
+// near 1; trX = tr X of this initial iterate
+__global__ void sp2_init2_kernel(int n, const double* __restrict__ F, const double* __restrict__ b, double* X,
+                                 double* trX)
+{
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * n) return;
+    const int i = idx % n, j = idx / n;
+    const double x = ((i == j ? b[1] : 0.0) - F[idx]) / (b[1] - b[0]);
+    X[idx] = x;
+    if (i == j) atomicAdd(trX, x);
+}
+
+// one SP2 step from the traces of this step (t[0] = tr X, t[1] = tr X^2);
+// accumulates tr of the new iterate into tnext[0]
+__global__ void sp2_step_kernel(int n, int nocc, const double* __restrict__ t, const double* __restrict__ X2,
+                                double* X, double* tnext)
+{
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * n) return;
+    const bool square = fabs(t[1] - nocc) <= fabs(2 * t[0] - t[1] - nocc);
+    const double x = square ? X2[idx] : 2 * X[idx] - X2[idx];
+    X[idx] = x;
+    const int i = idx % n, j = idx / n;
+    if (i == j) atomicAdd(tnext, x);
+}
+
+struct Purifier {
+    int n = 0, nocc = 0;
+    DBuf<double> X, T1, T2, B, tr;  // orthogonaliser S^-1/2 and work
+    void setup(Context& ctx, int n_, int nocc_, const double* dS)
+    {
+        n = n_;
+        nocc = nocc_;
+        const int64_t nn = (int64_t)n * n;
+        cudaStream_t st = ctx.stream;
+        X.alloc(nn, st);
+        T1.alloc(nn, st);
+        T2.alloc(nn, st);
+        B.alloc(4, st);
+        tr.alloc(4, st);
+        DBuf<double> U(nn, st), w(n, st);
+        DBuf<int> info(1, st);
+        HF_CUDA(cudaMemcpyAsync(U.p, dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+        int lwork = 0;
+        HF_CUSOLVER(cusolverDnDsyevd_bufferSize(ctx.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, U.p,
+                                                n, w.p, &lwork));
+        DBuf<double> work(std::max(lwork, 1), st);
+        HF_CUSOLVER(cusolverDnDsyevd(ctx.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, U.p, n, w.p,
+                                     work.p, lwork, info.p));
+        std::vector<double> hw(n);
+        int hinfo = 0;
+        w.download(hw.data(), n);
+        info.download(&hinfo, 1);
+        HF_CUDA(cudaStreamSynchronize(st));
+        HF_CHECK(hinfo == 0 && hw[0] > 0, HFGPU_ERR_LINALG, "S is not positive definite");
+        scale_cols_kernel<<<nblk(nn), 256, 0, st>>>(n, U.p, w.p, T1.p);  // U w^-1/2
+        count_launch();
+        const double one = 1.0, zero = 0.0;
+        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, n, &one, T1.p, n, U.p, n, &zero, X.p, n));
+    }
+    // P = 2 X proj(X F X) X: the closed-shell density of F without diagonalising it
+    void density(Context& ctx, const double* dF, double* dP)
+    {
+        const int64_t nn = (int64_t)n * n;
+        cudaStream_t st = ctx.stream;
+        const double one = 1.0, zero = 0.0, two = 2.0;
+        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, X.p, n, dF, n, &zero, T1.p, n));
+        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, T1.p, n, X.p, n, &zero, T2.p, n));
+        gersh_kernel<<<1, 256, 0, st>>>(n, T2.p, B.p);
+        count_launch();
+        // per-step trace slots [step][tr X, tr X^2], zeroed once
+        const int MAXS = 160, CHECK = 8;
+        if (tr.n < (size_t)2 * (MAXS + 1)) tr.alloc(2 * (MAXS + 1), st);
+        HF_CUDA(cudaMemsetAsync(tr.p, 0, sizeof(double) * 2 * (MAXS + 1), st));
+        sp2_init2_kernel<<<nblk(nn), 256, 0, st>>>(n, T2.p, B.p, T1.p, tr.p);  // T1 = iterate
+        count_launch();
+        const int nt = (n + SQ_T - 1) / SQ_T;
+        const unsigned tiles = (unsigned)(nt * (nt + 1) / 2);
+        double h[2] = {0, 1};
+        bool done = false;
+        for (int it = 0; it < MAXS && !done; ++it) {
+            sym_square_kernel<<<tiles, SQ_T * SQ_T, 0, st>>>(n, T1.p, T2.p, tr.p + 2 * it + 1);
+            count_launch();
+            sp2_step_kernel<<<nblk(nn), 256, 0, st>>>(n, nocc, tr.p + 2 * it, T2.p, T1.p, tr.p + 2 * (it + 1));
+            count_launch();
+            if (it % CHECK == CHECK - 1) {
+                // traces of step it (tr X, tr X^2) are complete once its kernels ran
+                HF_CUDA(cudaMemcpyAsync(h, tr.p + 2 * it, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+                HF_CUDA(cudaStreamSynchronize(st));
+                done = fabs(h[0] - h[1]) < 1e-13 * n && fabs(h[0] - nocc) < 1e-6;
+            }
+        }
+        HF_CHECK(fabs(h[0] - nocc) < 1e-6, HFGPU_ERR_LINALG, "density purification did not converge (no gap?)");
+        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, X.p, n, T1.p, n, &zero, T2.p, n));
+        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &two, T2.p, n, X.p, n, &zero, dP, n));
+    }
+};
+
 // P = 2 C_occ C_occ^T
 static void form_density(Context& ctx, int n, int nocc, const double* C, double* P)
 {
@@ -141,6 +311,9 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
     std::vector<double> B((size_t)nd * nd, 0.0);
     int nhist = 0, head = 0;
 
+    Purifier pur;
+    if (in.purify) pur.setup(ctx, n, in.nocc, in.dS);
+
     std::vector<double> Escf;
     ScfOut out;
     for (int it = 1; it <= in.nscf; ++it) {
@@ -196,12 +369,18 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
             }
             head = (head + 1) % nd;
         }
-        HF_CUDA(cudaMemcpyAsync(Fw.p, Fsolve, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
-        HF_CUDA(cudaMemcpyAsync(Sw.p, in.dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
-        HF_CUSOLVER(cusolverDnDsygvd(ctx.solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
-                                     CUBLAS_FILL_MODE_LOWER, n, Fw.p, n, Sw.p, n, dLam, work.p, lwork, info.p));
         HF_CUDA(cudaMemcpyAsync(Pold.p, dP, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
-        form_density(ctx, n, in.nocc, Fw.p, dP);
+        if (in.purify) {
+            HF_CUDA(cudaMemcpyAsync(Fw.p, Fsolve, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+            pur.density(ctx, Fw.p, dP);
+            HF_CUDA(cudaMemsetAsync(info.p, 0, sizeof(int), st));
+        } else {
+            HF_CUDA(cudaMemcpyAsync(Fw.p, Fsolve, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+            HF_CUDA(cudaMemcpyAsync(Sw.p, in.dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+            HF_CUSOLVER(cusolverDnDsygvd(ctx.solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                                         CUBLAS_FILL_MODE_LOWER, n, Fw.p, n, Sw.p, n, dLam, work.p, lwork, info.p));
+            form_density(ctx, n, in.nocc, Fw.p, dP);
+        }
         reduce(ctx, 1, nn, dP, Pold.p, nullptr, scal.p + 1);  // dP
         double h[2];
         int hinfo = 0;
@@ -220,6 +399,17 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
             double emax = *std::max_element(Escf.end() - 4, Escf.end());
             double emin = *std::min_element(Escf.end() - 4, Escf.end());
             if (dPv < in.tolP && emax - emin < in.tolE) {
+                if (in.purify) {
+                    // orbitals and orbital energies of the last Fock matrix, as the reference returns them
+                    HF_CUDA(cudaMemcpyAsync(Sw.p, in.dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+                    HF_CUSOLVER(cusolverDnDsygvd(ctx.solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                                                 CUBLAS_FILL_MODE_LOWER, n, Fw.p, n, Sw.p, n, dLam, work.p, lwork,
+                                                 info.p));
+                    form_density(ctx, n, in.nocc, Fw.p, dP);
+                    info.download(&hinfo, 1);
+                    HF_CUDA(cudaStreamSynchronize(st));
+                    HF_CHECK(hinfo == 0, HFGPU_ERR_LINALG, "eigh: dsygvd returned info = " + std::to_string(hinfo));
+                }
                 HF_CUDA(cudaMemcpyAsync(dC, Fw.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
                 HF_CUDA(cudaStreamSynchronize(st));
                 out.converged = true;
@@ -230,6 +420,11 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
             mix_kernel<<<nblk(nn), 256, 0, st>>>(nn, in.alpha, Pold.p, dP);
             count_launch();
         }
+    }
+    if (in.purify) {  // orbitals of the last Fock matrix
+        HF_CUDA(cudaMemcpyAsync(Sw.p, in.dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+        HF_CUSOLVER(cusolverDnDsygvd(ctx.solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                                     CUBLAS_FILL_MODE_LOWER, n, Fw.p, n, Sw.p, n, dLam, work.p, lwork, info.p));
     }
     HF_CUDA(cudaMemcpyAsync(dC, Fw.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
     HF_CUDA(cudaStreamSynchronize(st));

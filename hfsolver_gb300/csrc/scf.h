@@ -16,6 +16,7 @@ struct ScfIn {
     double tolE = 1e-10, tolP = 1e-8, alpha = 1.0;
     int accel = HFGPU_SCF_MIXING;
     int diis_size = 8;
+    bool purify = false;  // density by SP2 purification instead of dsygvd each iteration
 };
 
 struct ScfOut {

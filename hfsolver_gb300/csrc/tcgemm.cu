@@ -2,24 +2,24 @@
 //
 // C[r, c] = sum_k A[r, k] B[k, c] for FP64 A and B, as used by the mixed-
 // precision AO->MO transform.  Each row of A (and each column of B) is scaled
-// by a power of two 2^e so that |x| < 2^e, rounded to a 35-bit fixed-point
-// integer and cut into five 7-bit digits d_0..d_4 (x ~ 2^e sum_t d_t 2^{-7(t+1)}),
+// by a power of two 2^e so that |x| < 2^e, rounded to a 42-bit fixed-point
+// integer and cut into six 7-bit digits d_0..d_5 (x ~ 2^e sum_t d_t 2^{-7(t+1)}),
 // stored as bf16 "slice planes" (integers <= 128 are exact in bf16).  This is
 // the error-free splitting of Ozaki, Ogita, Oishi and Rump (Numer. Algorithms
 // 59, 95 (2012)) with bf16 tensor-core products:
 //   * a product of two digits is < 2^14, so a K-sum of one digit pair over
 //     K <= 1024 stays below 2^24 and the FP32 tensor-core accumulation is exact;
 //   * digit pairs (i, j) with i + j = t share the weight 2^{-7(t+2)} and are
-//     accumulated together in TMEM accumulator t (t = 0..4, 15 products);
+//     accumulated together in TMEM accumulator t (t = 0..5, 21 products);
 //     groups t = 0, 1 stay exact for K <= 512, and the rounding of the later
 //     groups is below 2^{-24} of terms that are already 2^{-28} smaller;
-//   * the epilogue recombines sum_t acc_t 2^{-7(t+2)} in FP64 and applies the
-//     row and column scales.
-// The result matches an FP64 GEMM to about 2^-35 of sum_k |A||B| per element.
+//   * the epilogue recombines sum_t acc_t 2^{-7(t+2)} exactly in int64 and
+//     applies the row and column scales with one FP64 multiply.
+// The result matches an FP64 GEMM to about 2^-42 K max|A_r.| max|B_.c| per element.
 //
 // Kernel: one CTA (128 threads) per 128 x 64 output tile; per K step of 64 one
-// thread issues the TMA loads of the 5 A and 5 B slice tiles (128B swizzle)
-// and then the 15 x 4 tcgen05.mma (M=128, N=64, K=16, BF16 in, FP32 out);
+// thread issues the TMA loads of the 6 A and 6 B slice tiles (128B swizzle)
+// and then the 21 x 4 tcgen05.mma (M=128, N=64, K=16, BF16 in, FP32 out);
 // every wait on an mbarrier is bounded and reports a timeout through an error
 // flag instead of spinning forever.
 #include <cuda.h>
@@ -33,12 +33,12 @@
 
 namespace hfgpu {
 
-constexpr int NSL = 5, SL_BITS = 7;
+constexpr int NSL = 6, SL_BITS = 7;
 constexpr int BM = 128, BN = 64, BK = 64;
 constexpr int A_TILE = BM * BK * 2;  // 16 KiB
 constexpr int B_TILE = BN * BK * 2;  // 8 KiB
 constexpr int SMEM_BYTES = NSL * (A_TILE + B_TILE) + 1024 + 64;
-constexpr uint32_t TMEM_COLS = 512;  // 5 accumulators x 64 columns, rounded to a power of two
+constexpr uint32_t TMEM_COLS = 512;  // 6 accumulators x 64 columns, rounded to a power of two
 constexpr int WAIT_SPINS = 1 << 22;
 
 // ------------------------------------------------------------------ PTX helpers
@@ -127,7 +127,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ double pow2(int e) { return __longlong_as_double((int64_t)(e + 1023) << 52); }
+// 2^e for any integer e (0 below the normal range, where the scaled values of
+// the transform are far below anything that matters)
+__device__ __forceinline__ double pow2(int e)
+{
+    if (e < -1022) return 0.0;
+    if (e > 1023) e = 1023;
+    return __longlong_as_double((int64_t)(e + 1023) << 52);
+}
 
 // ------------------------------------------------------------------ GEMM kernel
 __device__ __forceinline__ int64_t out_index(const OutMap& om, int64_t r, int64_t c)
@@ -212,26 +219,28 @@ __global__ void __launch_bounds__(128, 1)
     } else {
         fence_after();
         // epilogue: warp w owns TMEM lanes (rows) 32w .. 32w+31
+        // Every group sum is an integer-valued FP32 (sums of digit products), so the
+        // groups recombine exactly in int64: S = sum_t acc_t 2^{7(NSL-1-t)} < 2^59,
+        // and the value is S 2^{-7(NSL+1)} times the row and column scales.
         const int64_t r = m0 + warp * 32 + lane;
-        const double er = (r < M) ? pow2(ea[r]) : 0.0;
-        for (int c0 = 0; c0 < BN; c0 += 16) {
-            double v[16];
+        const int er = (r < M) ? ea[r] : 0;
+        for (int c0 = 0; c0 < BN && n0 + c0 < N; c0 += 16) {
+            long long S[16];
 #pragma unroll
-            for (int i = 0; i < 16; ++i) v[i] = 0.0;
+            for (int i = 0; i < 16; ++i) S[i] = 0;
 #pragma unroll
             for (int t = 0; t < NSL; ++t) {
                 float f[16];
                 tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(t * BN + c0), f);
-                const double w = pow2(-SL_BITS * (t + 2));
 #pragma unroll
-                for (int i = 0; i < 16; ++i) v[i] = fma((double)f[i], w, v[i]);
+                for (int i = 0; i < 16; ++i) S[i] += __float2ll_rn(f[i]) << (SL_BITS * (NSL - 1 - t));
             }
             if (r < M) {
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
                     const int c = n0 + c0 + i;
                     if (c < N) {
-                        const double x = v[i] * er * pow2(eb[c]);
+                        const double x = (double)S[i] * pow2(er + eb[c] - SL_BITS * (NSL + 1));
                         const int64_t o = out_index(om, r, c);
                         out[o] = accumulate ? out[o] + x : x;
                     }
@@ -253,7 +262,7 @@ __device__ __forceinline__ void digits5(double x, int e, float (&d)[NSL])
     uint64_t Y = 0;
     if (ex != 0) {
         const uint64_t m = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-        const int sh = ex - 1075 + NSL * SL_BITS - e;  // |x| < 2^e gives sh < -17
+        const int sh = ex - 1075 + NSL * SL_BITS - e;  // |x| < 2^e gives sh < -10
         if (sh >= 0)
             Y = m << sh;
         else if (sh > -63)
@@ -433,6 +442,10 @@ void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, Ou
     const CUtensorMap ta = make_map(A, BM), tb = make_map(B, BN);
     DBuf<int> err(1, ctx.stream);
     err.zero();
+    cudaEvent_t e0, e1;
+    HF_CUDA(cudaEventCreate(&e0));
+    HF_CUDA(cudaEventCreate(&e1));
+    HF_CUDA(cudaEventRecord(e0, ctx.stream));
     dim3 grid((unsigned)(A.rows_pad / BM), (unsigned)(B.rows_pad / BN));
     HF_CHECK(grid.x > 0 && grid.y > 0 && A.rows_pad / BM < 2147483647LL, HFGPU_ERR_INVALID, "sliced GEMM: grid");
     sliced_gemm_kernel<<<grid, 128, SMEM_BYTES, ctx.stream>>>(ta, tb, A.rows_pad, (int)B.rows_pad, A.K_pad / BK,
@@ -440,9 +453,16 @@ void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, Ou
                                                                accumulate ? 1 : 0, err.p);
     count_launch();
     HF_CUDA(cudaGetLastError());
+    HF_CUDA(cudaEventRecord(e1, ctx.stream));
     int h = 0;
     err.download(&h, 1);
     HF_CUDA(cudaStreamSynchronize(ctx.stream));
+    float ms = 0;
+    HF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx.stat_tc_ms += ms;
+    ctx.stat_tc_flops += 2.0 * (NSL * (NSL + 1) / 2) * (double)A.rows * (double)B.rows * (double)A.K;
     HF_CHECK(h == 0, HFGPU_ERR_CUDA, "sliced GEMM: an mbarrier wait timed out");
 }
 

@@ -13,7 +13,7 @@ struct OutMap {
     int64_t ld;
 };
 
-// A matrix cut into five bf16 planes of 7-bit digits plus one power-of-two
+// A matrix cut into six bf16 planes of 7-bit digits plus one power-of-two
 // exponent per row; rows and K padded to the tile sizes.
 struct Sliced {
     DBuf<__nv_bfloat16> planes;

@@ -102,6 +102,16 @@ int hfgpu_doscf(int n, const double *H, const double *int2, const double *S, int
                 double tolE, double tolP, double alpha, double *C, double *P, double *lam,
                 double *E0, int *niter);
 
+/* Coulomb and exchange matrices of a density, J(i,j) = sum_kl (ij|kl) P(k,l) and
+ * K(i,j) = sum_kl (ik|jl) P(k,l) (the two parts of TT, src/scf.f90:84-105), for a
+ * basis in the C-driver layout above, with quartets whose Schwarz bound
+ * sqrt((ab|ab)(cd|cd)) is below schwarz left out (0: none).  The integrals are
+ * built and digested on the device; no two-electron array is returned. */
+int hfgpu_jk(int nbf, const int *nprim, const int *istart, const double *xcenter,
+             const double *ycenter, const double *zcenter, const int *lpower, const int *mpower,
+             const int *npower, int n2, const double *coef, const double *alpha, const double *P,
+             double schwarz, double *J, double *K);
+
 /* replaces formG / formG2, src/scf.f90:26-58: G(i,j) = sum_kl P(k,l) [(ij|kl) - (il|kj)/2]
  * from the packed integrals, without the reference's dense TT(n,n,n,n)
  * (src/scf.f90:79-105); P and G column-major n x n. */
@@ -135,9 +145,17 @@ int hfgpu_mbpt2(int n, const double *moint2, const double *lam, int nocc, double
 /* FP64-accurate C = A B on the tcgen05 tensor cores (the kernel behind the
  * mixed-precision transform): A row-major M x K, Bt = B^T row-major N x K
  * (B column-major), C row-major M x N; 1 <= K <= 512.  Rows of A and columns
- * of B are split exactly into five 7-bit bf16 digits with a power-of-two
- * scale; the result agrees with an FP64 GEMM to about 2^-35 sum_k |A||B|. */
+ * of B are split exactly into six 7-bit bf16 digits with a power-of-two scale;
+ * the result agrees with an FP64 GEMM to about 2^-42 K max|A_r.| max|B_.c|. */
 int hfgpu_dgemm_sliced(int64_t M, int N, int K, const double *A, const double *Bt, double *C);
+
+/* MBPT2 energy from the packed AO integrals and the orbitals: the
+ * transform_int2 + mbpt2 sequence of the reference's tests
+ * (src/mbpt.f90:11-79, :154-159) without the packed MO array; only (ia|jb) is
+ * formed.  precision: HFGPU_MP2_FP64 (cuBLAS DGEMM) or HFGPU_MP2_SPLIT_BF16
+ * (tensor cores, exact 7-bit bf16 slicing). */
+int hfgpu_mp2_energy(int n, const double *int2, const double *C, const double *lam, int nocc,
+                     int precision, double *E2);
 
 /* ---- Whole pipeline: rhf_gauss (src/drivers.f90:12-51) + MBPT2 ------------ */
 
@@ -154,7 +172,9 @@ typedef struct {
     double schwarz;      /* quartet cut on sqrt((ab|ab)(cd|cd)); 0 = none (reference) */
     int mp2;             /* HFGPU_MP2_* */
     int mp2_nocc;        /* occupied orbitals passed to MBPT2; <= 0: sum(Z)/2 */
-    int reserved[8];
+    int purify;          /* 1: density by SP2 purification (GEMMs only) in each iteration and one
+                            final dsygvd for the orbitals; 0: dsygvd every iteration (reference) */
+    int reserved[7];
 } hfgpu_options;
 
 typedef struct {
@@ -169,7 +189,11 @@ typedef struct {
     double ms_scf, ms_mp2;   /* SCF loop; AO->MO transform + MBPT2 */
     double ms_total;         /* the whole call */
     double ms_setup;         /* basis, one-electron integrals, pairs, Schwarz bounds */
-    double reserved[7];
+    double ms_fock;          /* Fock two-electron kernels summed over the SCF iterations */
+    double ms_tcgemm;        /* tensor-core sliced GEMM kernels (mixed MBPT2) */
+    double tc_flops;         /* bf16 tensor flops those kernels performed (2 M N K per product) */
+    double ms_grad;          /* analytic gradient (hfgpu_rhf_gradient) */
+    double reserved[3];
 } hfgpu_result;
 
 void hfgpu_default_options(hfgpu_options *opt);
@@ -180,6 +204,25 @@ void hfgpu_default_options(hfgpu_options *opt);
  * given they must hold nbf*nbf and nbf doubles (nbf from hfgpu_basis_size). */
 int hfgpu_rhf(int natoms, const int *atno, const double *xyz, const hfgpu_options *opt,
               hfgpu_result *res, double *C, double *lam);
+
+/* Analytic RHF nuclear gradient dE_tot/dR (Ha/bohr) at the converged SCF of
+ * hfgpu_rhf with the same arguments: grad holds 3 x natoms doubles (x, y, z
+ * of each atom, the layout of xyz).  The reference has no gradient; this is
+ * the force callback its md.f90 integrators take (src/md.f90:13-20, forces =
+ * -grad).  One- and two-electron derivative integrals are contracted with the
+ * density and energy-weighted density on the GPU and never stored; the
+ * two-electron part runs over the quartets that survive opt->schwarz.
+ * res gets the energies (and E2 if opt->mp2 asks for it).  Returns
+ * HFGPU_ERR_NOT_CONVERGED, with grad untouched, if the SCF did not converge. */
+int hfgpu_rhf_gradient(int natoms, const int *atno, const double *xyz, const hfgpu_options *opt,
+                       hfgpu_result *res, double *grad);
+
+/* hfgpu_rhf for nmol molecules in one call: molecule m has natoms[m] atoms, its
+ * charges and coordinates follow those of molecule m-1 in atno and xyz; res[m]
+ * gets its results (res[m].niter = -status if it failed).  Returns the first
+ * failure's status, or HFGPU_OK. */
+int hfgpu_rhf_batch(int nmol, const int *natoms, const int *atno, const double *xyz,
+                    const hfgpu_options *opt, hfgpu_result *res);
 
 /* number of basis functions hfgpu_rhf will use for these atoms (0 on error) */
 int hfgpu_basis_size(int natoms, const int *atno);

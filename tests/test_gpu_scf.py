@@ -110,3 +110,57 @@ def test_gpu_errors_are_statuses():
     atno, xyz = water()
     with pytest.raises(hf.SCFNotConverged):
         hf.rhf(atno, xyz, hf.RHFOptions(nscf=2))
+
+
+@pytest.mark.parametrize("nw,seed", [(2, 3), (4, 0)])
+def test_purification_matches_diagonalisation(nw, seed):
+    """SP2 purification of the density each iteration reaches the same SCF
+    solution (and the same final orbitals) as an eigensolve each iteration."""
+    from hfsolver_gb300.clusters import water_cluster
+
+    atno, xyz = water_cluster(nw, seed=seed)
+    o = dict(diis=True, tolP=1e-10, tolE=1e-12, schwarz=1e-12)
+    a = hf.rhf(atno, xyz, hf.RHFOptions(**o), want_orbitals=True)
+    b = hf.rhf(atno, xyz, hf.RHFOptions(purify=True, **o), want_orbitals=True)
+    assert abs(a["Etot"] - b["Etot"]) < 1e-10
+    assert abs(a["E2"] - b["E2"]) < 1e-9
+    assert np.max(np.abs(a["lam"] - b["lam"])) < 1e-7
+
+
+def test_jk_direct_entry(oracle):
+    from tests.gpu_common import basis_args
+
+    c = CASES["NH3"]
+    ref = oracle.rhf_gauss(c["atno"], np.array(c["xyz"], float))
+    b = ref["basis"]
+    I = oracle.unpack(ref["int2"], b.n)
+    P = ref["P"]
+    J_ref = np.einsum("ijkl,kl->ij", I, P)
+    K_ref = np.einsum("ikjl,kl->ij", I, P)
+    J, K = hf.jk(*basis_args(b), P)
+    assert_close(J, J_ref, 1e-11, 1e-11, "J")
+    assert_close(K, K_ref, 1e-11, 1e-11, "K")
+    assert_close(J - 0.5 * K, oracle.formG(P, ref["int2"]), 1e-11, 1e-11, "G")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split_bf16"])
+def test_mp2_energy_entry(oracle, precision):
+    c = CASES["CH4_1"]
+    ref = oracle.rhf_gauss(c["atno"], np.array(c["xyz"], float))
+    e2 = oracle.mbpt2(oracle.transform_int2(ref["int2"], ref["C"]), ref["lam"], 5)
+    got = hf.mp2_energy(ref["int2"], ref["C"], ref["lam"], 5, precision)
+    assert abs(got - e2) < (1e-12 if precision == "fp64" else 1e-9)
+
+
+def test_rhf_batch_matches_single_calls():
+    from hfsolver_gb300.clusters import water, water_cluster
+
+    mols = [water(), (np.array(CASES["CH4_1"]["atno"]), np.array(CASES["CH4_1"]["xyz"], float)),
+            water_cluster(2, seed=1)]
+    o = hf.RHFOptions(diis=True, tolP=1e-9, tolE=1e-11)
+    batch = hf.rhf_batch(mols, o)
+    for (a, x), r in zip(mols, batch):
+        single = hf.rhf(a, x, o)
+        assert r["niter"] == single["niter"]
+        assert abs(r["Etot"] - single["Etot"]) < 1e-11
+        assert abs(r["E2"] - single["E2"]) < 1e-11

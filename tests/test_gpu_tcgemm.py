@@ -1,8 +1,8 @@
 """The tcgen05 sliced-bf16 GEMM (hfgpu_dgemm_sliced) against an FP64 GEMM, and
 the mixed-precision MBPT2 against the FP64 one.
 
-GEMM tolerance: |C - A B| <= 2^-33 K max|A_r.| max|B_.c| per element (each
-entry is kept to 2^-35 of its row's or column's power-of-two scale, which is at
+GEMM tolerance: |C - A B| <= 2^-40 K max|A_r.| max|B_.c| per element (each
+entry is kept to 2^-42 of its row's or column's power-of-two scale, which is at
 most twice the row's or column's largest entry).  MBPT2: |dE2| <= 1e-8 Ha."""
 import ctypes
 
@@ -36,7 +36,7 @@ def test_sliced_gemm_matches_fp64(M, N, K):
     B = rng.standard_normal((K, N)) * 10.0 ** rng.uniform(-2, 2, size=(1, N))
     C = sliced(A, B)
     ref = A @ B
-    bound = 2.0 ** -33 * K * np.max(np.abs(A), axis=1)[:, None] * np.max(np.abs(B), axis=0)[None, :] + 1e-300
+    bound = 2.0 ** -40 * K * np.max(np.abs(A), axis=1)[:, None] * np.max(np.abs(B), axis=0)[None, :] + 1e-300
     assert np.all(np.abs(C - ref) <= bound), float(np.max(np.abs(C - ref) / bound))
 
 
@@ -56,4 +56,19 @@ def test_mixed_mp2_matches_fp64(nw, seed):
     e64 = hf.rhf(atno, xyz, hf.RHFOptions(mp2="fp64", **o))
     emx = hf.rhf(atno, xyz, hf.RHFOptions(mp2="split_bf16", **o))
     assert abs(e64["Etot"] - emx["Etot"]) < 1e-12
+    assert abs(e64["E2"] - emx["E2"]) < 1e-8
+
+
+def test_sixteen_water_mixed_vs_fp64():
+    """16 waters, 400 functions, 80 occupied: the tensor-core MBPT2 against the
+    FP64 transform on the same SCF solution (the FP64 path itself matches the
+    oracle fixtures up to 200 functions)."""
+    from hfsolver_gb300.clusters import water_cluster
+
+    atno, xyz = water_cluster(16, seed=0)
+    o = dict(diis=True, purify=True, schwarz=1e-12, tolP=1e-8, tolE=1e-10)
+    emx = hf.rhf(atno, xyz, hf.RHFOptions(mp2="split_bf16", **o))
+    e64 = hf.rhf(atno, xyz, hf.RHFOptions(mp2="fp64", **o))
+    assert emx["nbf"] == 400 and emx["nocc"] == 80
+    assert abs(e64["Etot"] - emx["Etot"]) < 1e-10
     assert abs(e64["E2"] - emx["E2"]) < 1e-8
