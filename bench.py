@@ -97,8 +97,9 @@ class ClockSampler:
 def workload(rank, waters=8):
     from hfsolver_gb300.clusters import water_cluster
 
-    # 8 waters in an 8 A cube; other sizes at the same density (16 waters: 10.08 A)
-    return water_cluster(waters, seed=rank)
+    # 8 waters in an 8 A cube, 16 waters in an 11 A cube; other sizes at the
+    # density of the 8-water cube
+    return water_cluster(waters, box=11.0 if waters == 16 else None, seed=rank)
 
 
 def options(mp2="split_bf16"):
@@ -295,7 +296,8 @@ def run_gpu(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD if args.waters == 8 else f"water{args.waters}_631gss_rhf_diis_schwarz1e-12_mp2",
-                   "molecule": f"{args.waters} H2O, seed=rank, {8.0 * (args.waters / 8) ** (1 / 3):.2f} A cube",
+                   "molecule": f"{args.waters} H2O, seed=rank, "
+                               f"{11.0 if args.waters == 16 else 8.0 * (args.waters / 8) ** (1 / 3):.2f} A cube",
                    "nbf": n, "nocc": r["nocc"],
                    "global_batch": world, "scf": "DIIS + SP2 purification", "schwarz": 1e-12, "mp2": main_mp2,
                    "l2": f"no flush: each step rebuilds the {8 * (n * (n + 1) // 2) * (n * (n + 1) // 2 + 1) // 2 / 1e9:.1f} GB "
@@ -328,6 +330,108 @@ def run_gpu(args):
     return 0
 
 
+def run_batch(args):
+    """Batched molecules/s: args.batch seeded water clusters of 1-12 waters with
+    Gaussian atom jitter (0.05 A), all through hfgpu_rhf_batch (mixed MBPT2,
+    several molecules in flight on their own streams), against the same
+    molecules one at a time through the plain FP64 path (every 8th molecule)."""
+    import torch
+
+    import hfsolver_gb300 as hf
+    from hfsolver_gb300.clusters import water_batch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    mols = water_batch(args.batch, seed=rank)
+    opt = options("split_bf16")
+    opt.batch_streams = args.streams
+    for w in range(args.warmup):
+        hf.rhf_batch(mols[w * 4:(w + 1) * 4], opt)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = []
+    for _ in range(args.steps):
+        res = hf.rhf_batch(mols, opt)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    # the same molecules one at a time, plain FP64 MBPT2, on a fixed subset
+    sub = list(range(0, len(mols), 8))
+    plain = options("fp64")
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ref = [hf.rhf(mols[i][0], mols[i][1], plain) for i in sub]
+    torch.cuda.synchronize()
+    wall_plain = time.perf_counter() - t1
+    if world > 1:
+        t = torch.tensor([wall, wall_plain], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        wall, wall_plain = (float(x) for x in t)
+    if rank != 0:
+        return 0
+    failed = sum(1 for r in res if r["niter"] <= 0)
+    dE2 = max(abs(res[i]["E2"] - r["E2"]) for i, r in zip(sub, ref))
+    dEt = max(abs(res[i]["Etot"] - r["Etot"]) for i, r in zip(sub, ref))
+    nbf = [r["nbf"] for r in res]
+    line = {
+        "metric": METRIC + " (batched)", "value": world * args.steps * len(mols) / wall, "unit": "molecules/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"water_batch{len(mols)}_1to12_jitter0.05A_631gss_rhf_diis_schwarz1e-12_mp2",
+                   "molecules": len(mols), "nbf_min": min(nbf), "nbf_max": max(nbf), "nbf_mean": float(np.mean(nbf)),
+                   "mp2": "split_bf16", "batch_streams": args.streams,
+                   "timing": "host wall clock between device-wide synchronizes (molecules run on several streams)",
+                   "parallelism": f"replicas x{world}"},
+        "plain_fp64_one_at_a_time": {"molecules_per_s": len(sub) / wall_plain, "sample": f"every 8th molecule ({len(sub)})",
+                                     "max_dE2": dE2, "max_dEtot": dEt},
+        "failed": failed,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_grad(args):
+    """Analytic RHF gradients of seeded 2/4/8/12-water clusters: ms per
+    gradient call (SCF + gradient) and for the gradient kernels alone."""
+    import torch
+
+    import hfsolver_gb300 as hf
+    from hfsolver_gb300.clusters import water_cluster
+
+    torch.cuda.set_device(0)
+    opt = hf.RHFOptions(nscf=100, diis=True, schwarz=1e-12, tolE=1e-10, tolP=1e-10, mp2="none")
+    out = {}
+    for nw in (2, 4, 8, 12):
+        atno, xyz = water_cluster(nw, seed=0)
+        for _ in range(args.warmup):
+            hf.rhf_gradient(atno, xyz, opt)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rs = [hf.rhf_gradient(atno, xyz, opt)[0] for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) / args.steps
+        out[f"water{nw}"] = {"nbf": rs[-1]["nbf"], "ms_per_call": 1e3 * wall,
+                             "ms_gradient_kernels": float(np.mean([r["ms_grad"] for r in rs])),
+                             "ms_scf": float(np.mean([r["ms_scf"] for r in rs])),
+                             "shell_quartets": rs[-1]["n_quartets"]}
+    print(json.dumps({"metric": "RHF gradient calls/s", "value": 1e3 / out["water12"]["ms_per_call"],
+                      "unit": "calls/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": "water12_631gss_rhf_gradient", "schwarz": 1e-12,
+                                 "timing": "host wall clock between device synchronizes"},
+                      "sizes": out}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -340,9 +444,17 @@ def main():
                     help="cluster size (8: 200 functions, the headline workload; 16: 400 functions)")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the CPU-baseline sample (profiling runs)")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="batched mode: this many water clusters of 1-12 waters per step")
+    ap.add_argument("--streams", type=int, default=8, help="batched mode: molecules in flight at once")
+    ap.add_argument("--grad", action="store_true", help="time the analytic gradient (2-12 waters)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.grad:
+        return run_grad(args)
+    if args.batch > 0:
+        return run_batch(args)
     return run_gpu(args)
 
 

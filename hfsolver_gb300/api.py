@@ -202,6 +202,7 @@ class RHFOptions:
     mp2: str = "fp64"          # "none" | "fp64" | "split_bf16"
     mp2_nocc: int = 0          # <= 0: sum(Z)/2
     purify: bool = False       # SP2 density purification instead of an eigensolve per iteration
+    batch_streams: int = 0     # rhf_batch: molecules in flight at once (<= 0: 8)
 
     def to_c(self):
         o = _lib.Options()
@@ -213,6 +214,7 @@ class RHFOptions:
         o.mp2 = {"none": _lib.MP2_NONE, "fp64": _lib.MP2_FP64, "split_bf16": _lib.MP2_SPLIT_BF16}[self.mp2]
         o.mp2_nocc = self.mp2_nocc
         o.purify = 1 if self.purify else 0
+        o.batch_streams = self.batch_streams
         return o
 
 

@@ -4,6 +4,10 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <atomic>
+#include <thread>
+#include <algorithm>
+#include <string>
 #include <vector>
 
 #include "internal.h"
@@ -97,7 +101,8 @@ void ints_dropin(const Basis& b, double* Ints, double schwarz, EriStats* st)
 }  // namespace
 
 static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu_options* opt_in, hfgpu_result* res,
-                     double* C, double* lam, int& conv, int& nscf, double* grad = nullptr)
+                     double* C, double* lam, int& conv, int& nscf, double* grad = nullptr,
+                     Context* ctx_in = nullptr)
 {
         check_ptr(atno, "atno"); check_ptr(xyz, "xyz"); check_ptr(res, "res");
         hfgpu_options opt;
@@ -108,7 +113,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
                  "unknown MP2 precision");
         std::memset(res, 0, sizeof(*res));
         Basis b = build_basis(natoms, atno, xyz);  // validates the input before any device work
-        Context& ctx = context();
+        Context& ctx = ctx_in ? *ctx_in : context();
         cudaStream_t st = ctx.stream;
         ctx.stat_fock_ms = ctx.stat_tc_ms = ctx.stat_tc_flops = 0;
         Timer total(st);
@@ -486,16 +491,60 @@ int hfgpu_rhf_batch(int nmol, const int* natoms, const int* atno, const double* 
         set_last_error("hfgpu_rhf_batch: invalid arguments");
         return HFGPU_ERR_INVALID;
     }
-    int64_t a0 = 0;
-    int first = HFGPU_OK;
-    for (int m = 0; m < nmol; ++m) {
-        int rc = hfgpu_rhf(natoms[m], atno + a0, xyz + 3 * a0, opt, &res[m], nullptr, nullptr);
-        if (rc != HFGPU_OK) {
-            res[m].niter = -rc;
-            if (first == HFGPU_OK) first = rc;
-        }
-        a0 += natoms[m] > 0 ? natoms[m] : 0;
+    std::vector<int64_t> a0(nmol + 1, 0);
+    for (int m = 0; m < nmol; ++m) a0[m + 1] = a0[m] + (natoms[m] > 0 ? natoms[m] : 0);
+    std::vector<int> rc(nmol, HFGPU_OK);
+    std::vector<std::string> err(nmol);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        set_last_error("hfgpu_rhf_batch: no CUDA device");
+        return HFGPU_ERR_NO_DEVICE;
     }
+    // molecules in flight at once, each on its own context (streams, handles):
+    // while one waits on a host-side convergence check the others fill the GPU
+    int nw = opt && opt->batch_streams > 0 ? opt->batch_streams : 8;
+    nw = std::max(1, std::min(nw, std::min(nmol, 64)));
+    std::atomic<int> next{0};
+    auto work = [&]() {
+        Context* c = nullptr;
+        int r0 = guard([&] {
+            HF_CUDA(cudaSetDevice(dev));
+            c = context_acquire();
+        });
+        for (int m; (m = next.fetch_add(1)) < nmol;) {
+            if (r0 != HFGPU_OK) {
+                rc[m] = r0;
+                err[m] = hfgpu_last_error();
+                continue;
+            }
+            int conv = 1, nscf = 0;
+            int r = guard([&] { rhf_impl(natoms[m], atno + a0[m], xyz + 3 * a0[m], opt, &res[m], nullptr, nullptr, conv,
+                                         nscf, nullptr, c); });
+            if (r == HFGPU_OK && !conv) {
+                r = HFGPU_ERR_NOT_CONVERGED;
+                set_last_error("SCF did not converge in " + std::to_string(nscf) + " iterations.");
+            }
+            rc[m] = r;
+            if (r != HFGPU_OK) err[m] = hfgpu_last_error();
+        }
+        context_release(c);
+    };
+    if (nw == 1) {
+        work();
+    } else {
+        std::vector<std::thread> th;
+        for (int w = 0; w < nw; ++w) th.emplace_back(work);
+        for (auto& t : th) t.join();
+    }
+    int first = HFGPU_OK;
+    for (int m = 0; m < nmol; ++m)
+        if (rc[m] != HFGPU_OK) {
+            res[m].niter = -rc[m];
+            if (first == HFGPU_OK) {
+                first = rc[m];
+                set_last_error("molecule " + std::to_string(m) + ": " + err[m]);
+            }
+        }
     return first;
 }
 

@@ -17,6 +17,8 @@ void count_launch(int n) { g_launches += n; }
 static std::mutex g_ctx_mutex;
 static std::vector<Context*> g_ctx;
 
+static Context* make_context(int dev);
+
 Context& context()
 {
     int dev = 0;
@@ -26,7 +28,42 @@ Context& context()
     HF_CUDA(cudaGetDevice(&dev));
     std::lock_guard<std::mutex> lk(g_ctx_mutex);
     if ((int)g_ctx.size() < ndev) g_ctx.resize(ndev, nullptr);
-    if (g_ctx[dev]) return *g_ctx[dev];
+    if (!g_ctx[dev]) g_ctx[dev] = make_context(dev);
+    return *g_ctx[dev];
+}
+
+// Extra contexts for concurrent molecules (hfgpu_rhf_batch workers): each has
+// its own streams and library handles; released contexts are kept for reuse.
+static std::vector<std::vector<Context*>> g_pool;
+
+Context* context_acquire()
+{
+    int dev = 0, ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) throw Error(HFGPU_ERR_NO_DEVICE, "no CUDA device");
+    HF_CUDA(cudaGetDevice(&dev));
+    {
+        std::lock_guard<std::mutex> lk(g_ctx_mutex);
+        if ((int)g_pool.size() < ndev) g_pool.resize(ndev);
+        if (!g_pool[dev].empty()) {
+            Context* c = g_pool[dev].back();
+            g_pool[dev].pop_back();
+            return c;
+        }
+    }
+    return make_context(dev);
+}
+
+void context_release(Context* c)
+{
+    if (!c) return;
+    std::lock_guard<std::mutex> lk(g_ctx_mutex);
+    if ((int)g_pool.size() <= c->device) g_pool.resize(c->device + 1);
+    g_pool[c->device].push_back(c);
+}
+
+static Context* make_context(int dev)
+{
     auto* c = new Context();
     c->device = dev;
     HF_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
@@ -36,12 +73,30 @@ Context& context()
     HF_CUSOLVER(cusolverDnCreate(&c->solver));
     HF_CUSOLVER(cusolverDnSetStream(c->solver, c->stream));
     HF_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev));
+    for (int i = 0; i < Context::NAUX; ++i) {
+        HF_CUDA(cudaStreamCreateWithFlags(&c->aux[i], cudaStreamNonBlocking));
+        HF_CUDA(cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming));
+    }
+    HF_CUDA(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
     std::vector<double> tab((size_t)BOYS_NROW * BOYS_STRIDE);
     boys_make_table(tab.data());
     HF_CUDA(cudaMalloc((void**)&c->boys, tab.size() * sizeof(double)));
     HF_CUDA(cudaMemcpy(c->boys, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
-    g_ctx[dev] = c;
-    return *c;
+    return c;
+}
+
+void Context::fork()
+{
+    HF_CUDA(cudaEventRecord(fork_ev, stream));
+    for (int i = 0; i < NAUX; ++i) HF_CUDA(cudaStreamWaitEvent(aux[i], fork_ev, 0));
+}
+
+void Context::join()
+{
+    for (int i = 0; i < NAUX; ++i) {
+        HF_CUDA(cudaEventRecord(join_ev[i], aux[i]));
+        HF_CUDA(cudaStreamWaitEvent(stream, join_ev[i], 0));
+    }
 }
 
 }  // namespace hfgpu

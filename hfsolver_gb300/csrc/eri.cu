@@ -422,6 +422,17 @@ __global__ void sym_kernel(int n, const double* __restrict__ Gh, double* G)
     G[idx] = Gh[idx] + Gh[j + (int64_t)i * n];
 }
 
+// lanes per quartet in the Fock digest: spread a class with few quartets and
+// large blocks over more lanes (at most one (a, b) row each), up to about
+// 150k threads in flight
+static int digest_split(const ClassPlan& c)
+{
+    const int nab = ncart(ptype_la(c.tb)) * ncart(ptype_lb(c.tb));
+    int s = 1;
+    while (s * 2 <= 32 && s * 2 <= nab && c.nq * s < 150000) s *= 2;
+    return s;
+}
+
 void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG)
 {
     HF_CHECK(P->blocks.p != nullptr, HFGPU_ERR_INVALID, "eri_digest: integrals were not kept");
@@ -433,7 +444,12 @@ void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG)
     HF_CUDA(cudaEventCreate(&e0));
     HF_CUDA(cudaEventCreate(&e1));
     HF_CUDA(cudaEventRecord(e0, ctx.stream));
-    for (auto& c : P->classes) {
+    // the classes are independent until the symmetrisation: spread them over the
+    // side streams, largest blocks first
+    ctx.fork();
+    int slot = 0;
+    for (int ci = (int)P->classes.size() - 1; ci >= 0; --ci) {
+        auto& c = P->classes[ci];
         if (c.nq == 0) continue;
         DigestArgs a;
         a.sh = P->shdev();
@@ -448,10 +464,16 @@ void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG)
         a.P = dP;
         a.n = n;
         a.Gh = Gh.p;
-        digest_fn(c.tb, c.tk)<<<(unsigned)((c.nq + 127) / 128), 128, 0, ctx.stream>>>(a);
+        a.split = digest_split(c);
+        cudaStream_t s = ctx.aux[slot++ % Context::NAUX];
+        if (a.split == 1)
+            digest_fn(c.tb, c.tk)<<<(unsigned)((c.nq + 127) / 128), 128, 0, s>>>(a);
+        else
+            digest_wide_fn(c.tb, c.tk)<<<(unsigned)((c.nq * a.split + 127) / 128), 128, 0, s>>>(a);
         count_launch();
         HF_CUDA(cudaGetLastError());
     }
+    ctx.join();
     sym_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, ctx.stream>>>(n, Gh.p, dG);
     count_launch();
     HF_CUDA(cudaGetLastError());

@@ -115,10 +115,19 @@ struct Context {
     cusolverDnHandle_t solver = nullptr;
     double* boys = nullptr;  // device copy of the Boys grid
     int num_sms = 0;
+    // side streams for independent launches (quartet classes), joined back to
+    // `stream` by events
+    static constexpr int NAUX = 4;
+    cudaStream_t aux[NAUX] = {};
+    cudaEvent_t fork_ev = nullptr, join_ev[NAUX] = {};
+    void fork();  // aux streams wait for the work queued so far on `stream`
+    void join();  // `stream` waits for the work queued on the aux streams
     // kernel-time counters, reset by the pipeline entry points
     double stat_fock_ms = 0, stat_tc_ms = 0, stat_tc_flops = 0;
 };
 Context& context();  // for the current device
+Context* context_acquire();        // a separate context on the current device (pooled)
+void context_release(Context* c);  // back to the pool
 void count_launch(int n = 1);  // bookkeeping for hfgpu_kernel_launches
 
 // ---------------------------------------------------------------- basis

@@ -32,6 +32,7 @@ struct DigestArgs {
     const double* P;
     int n;
     double* Gh;
+    int split;  // lanes per quartet (digest_wide_kernel; a power of two <= 32)
 };
 
 template <int TB, int TK>
@@ -164,7 +165,117 @@ __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
         for (int id = 0; id < ND; ++id) add(fb[ib], fd[id], -0.5 * kbd[ib * ND + id]);
 }
 
+// The same Fock contribution with `split` lanes per quartet, for classes with
+// few quartets and large blocks ((dd|dd) has a few hundred quartets of 1296
+// elements each): the lanes of a quartet take its (a, b) rows in turn, send
+// each row's J_ab and K contributions straight to Gh, and sum their partial
+// J_cd with warp shuffles before one lane per (c, d) adds it.
+template <int TB, int TK>
+__global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
+{
+    using CI = ClassInfo<TB, TK>;
+    constexpr int NA = ncart(CI::LA), NB = ncart(CI::LB), NC = ncart(CI::LC), ND = ncart(CI::LD);
+    const int split = a.split;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int sub = (int)(tid & (split - 1));
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned mask = split == 32 ? 0xffffffffu : (((1u << split) - 1u) << (lane & ~(unsigned)(split - 1)));
+    const int64_t qg = tid / split;
+    if (qg >= a.nq) return;  // all lanes of a quartet leave together
+    int lo = 0, hi = a.nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.segs[mid].qoff <= qg) lo = mid; else hi = mid - 1;
+    }
+    const Seg sg = a.segs[lo];
+    const int64_t q = qg - sg.qoff;
+    int bra, ket;
+    {
+        const int64_t* pf = a.prefix + sg.pref0;
+        int l2 = 0, h2 = sg.nbra - 1;
+        while (l2 < h2) {
+            const int mid = (l2 + h2 + 1) >> 1;
+            if (pf[mid] <= q) l2 = mid; else h2 = mid - 1;
+        }
+        bra = a.gpairs[sg.bra0 + l2];
+        ket = a.gpairs[sg.ket0 + (int)(q - pf[l2])];
+    }
+    const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
+    int fc[NC], fd[ND];
+#pragma unroll
+    for (int i = 0; i < NC; ++i) fc[i] = a.sh.comp_fn[a.sh.cfn0[C] + i];
+#pragma unroll
+    for (int i = 0; i < ND; ++i) fd[i] = a.sh.comp_fn[a.sh.cfn0[D] + i];
+    const int* fa = a.sh.comp_fn + a.sh.cfn0[A];
+    const int* fb = a.sh.comp_fn + a.sh.cfn0[B];
+    const int n = a.n;
+    auto Pv = [&](int x, int y) { return (x < 0 || y < 0) ? 0.0 : __ldg(a.P + x + (int64_t)y * n); };
+    double* Gh = a.Gh;
+    auto add = [&](int x, int y, double v) {
+        if (x >= 0 && y >= 0 && v != 0.0) atomicAdd(Gh + x + (int64_t)y * n, v);
+    };
+    const double f = (A == B ? 0.5 : 1.0) * (C == D ? 0.5 : 1.0) * (bra == ket ? 0.5 : 1.0);
+    double jcd[NC * ND], Pcd[NC * ND];
+#pragma unroll
+    for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+        for (int id = 0; id < ND; ++id) {
+            jcd[ic * ND + id] = 0.0;
+            Pcd[ic * ND + id] = Pv(fc[ic], fd[id]);
+        }
+#pragma unroll 1
+    for (int ab = sub; ab < NA * NB; ab += split) {
+        const int ia = ab / NB, ib = ab - ia * NB;
+        const int xa = __ldg(fa + ia), xb = __ldg(fb + ib);
+        const double Pab = Pv(xa, xb);
+        double Pac[NC], Pbc[NC], Pad[ND], Pbd[ND];
+#pragma unroll
+        for (int ic = 0; ic < NC; ++ic) {
+            Pac[ic] = Pv(xa, fc[ic]);
+            Pbc[ic] = Pv(xb, fc[ic]);
+        }
+#pragma unroll
+        for (int id = 0; id < ND; ++id) {
+            Pad[id] = Pv(xa, fd[id]);
+            Pbd[id] = Pv(xb, fd[id]);
+        }
+        double s_ab = 0.0, s_ad[ND], s_bd[ND];
+#pragma unroll
+        for (int id = 0; id < ND; ++id) s_ad[id] = s_bd[id] = 0.0;
+        const double* blk = a.blocks + (int64_t)(ab * CI::NCDT) * a.nq + qg;
+#pragma unroll
+        for (int ic = 0; ic < NC; ++ic) {
+            double s_ac = 0.0, s_bc = 0.0;
+#pragma unroll
+            for (int id = 0; id < ND; ++id) {
+                const double v = __ldg(blk + (int64_t)(ic * ND + id) * a.nq) * f;
+                s_ab = fma(v, Pcd[ic * ND + id], s_ab);
+                jcd[ic * ND + id] = fma(v, Pab, jcd[ic * ND + id]);
+                s_ac = fma(v, Pbd[id], s_ac);
+                s_bc = fma(v, Pad[id], s_bc);
+                s_ad[id] = fma(v, Pbc[ic], s_ad[id]);
+                s_bd[id] = fma(v, Pac[ic], s_bd[id]);
+            }
+            add(xa, fc[ic], -0.5 * s_ac);
+            add(xb, fc[ic], -0.5 * s_bc);
+        }
+        add(xa, xb, 2.0 * s_ab);
+#pragma unroll
+        for (int id = 0; id < ND; ++id) {
+            add(xa, fd[id], -0.5 * s_ad[id]);
+            add(xb, fd[id], -0.5 * s_bd[id]);
+        }
+    }
+    for (int o = split >> 1; o > 0; o >>= 1)
+#pragma unroll
+        for (int i = 0; i < NC * ND; ++i) jcd[i] += __shfl_xor_sync(mask, jcd[i], o);
+#pragma unroll
+    for (int i = 0; i < NC * ND; ++i)
+        if ((i & (split - 1)) == sub) add(fc[i / ND], fd[i % ND], 2.0 * jcd[i]);
+}
+
 using DigestFn = void (*)(DigestArgs);
-DigestFn digest_fn(int tb, int tk);  // jk_blocks.cu
+DigestFn digest_fn(int tb, int tk);       // jk_blocks.cu
+DigestFn digest_wide_fn(int tb, int tk);  // jk_blocks.cu
 
 }  // namespace hfgpu

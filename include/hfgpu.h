@@ -174,7 +174,9 @@ typedef struct {
     int mp2_nocc;        /* occupied orbitals passed to MBPT2; <= 0: sum(Z)/2 */
     int purify;          /* 1: density by SP2 purification (GEMMs only) in each iteration and one
                             final dsygvd for the orbitals; 0: dsygvd every iteration (reference) */
-    int reserved[7];
+    int batch_streams;   /* hfgpu_rhf_batch: molecules in flight at once, each on its own
+                            streams; <= 0: 8 */
+    int reserved[6];
 } hfgpu_options;
 
 typedef struct {
@@ -219,8 +221,10 @@ int hfgpu_rhf_gradient(int natoms, const int *atno, const double *xyz, const hfg
 
 /* hfgpu_rhf for nmol molecules in one call: molecule m has natoms[m] atoms, its
  * charges and coordinates follow those of molecule m-1 in atno and xyz; res[m]
- * gets its results (res[m].niter = -status if it failed).  Returns the first
- * failure's status, or HFGPU_OK. */
+ * gets its results (res[m].niter = -status if it failed).  opt->batch_streams
+ * molecules run at once, each on its own CUDA streams and library handles, so
+ * small molecules share the GPU.  Returns the first failure's status (in
+ * molecule order), or HFGPU_OK. */
 int hfgpu_rhf_batch(int nmol, const int *natoms, const int *atno, const double *xyz,
                     const hfgpu_options *opt, hfgpu_result *res);
 

@@ -65,7 +65,7 @@ def test_sixteen_water_mixed_vs_fp64():
     oracle fixtures up to 200 functions)."""
     from hfsolver_gb300.clusters import water_cluster
 
-    atno, xyz = water_cluster(16, seed=0)
+    atno, xyz = water_cluster(16, box=11.0, seed=0)
     o = dict(diis=True, purify=True, schwarz=1e-12, tolP=1e-8, tolE=1e-10)
     emx = hf.rhf(atno, xyz, hf.RHFOptions(mp2="split_bf16", **o))
     e64 = hf.rhf(atno, xyz, hf.RHFOptions(mp2="fp64", **o))
