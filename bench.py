@@ -106,7 +106,7 @@ def options(mp2="split_bf16"):
     import hfsolver_gb300 as hf
 
     return hf.RHFOptions(nscf=60, diis=True, diis_size=8, schwarz=1e-12, tolE=1e-10, tolP=1e-8, mp2=mp2,
-                         purify=True)
+                         purify=True, incremental=True)
 
 
 # ---------------------------------------------------------------- CPU baseline

@@ -22,7 +22,8 @@ class Options(ctypes.Structure):
     _fields_ = [("nscf", ctypes.c_int), ("mix_alpha", ctypes.c_double), ("tolE", ctypes.c_double),
                 ("tolP", ctypes.c_double), ("scf_accel", ctypes.c_int), ("diis_size", ctypes.c_int),
                 ("schwarz", ctypes.c_double), ("mp2", ctypes.c_int), ("mp2_nocc", ctypes.c_int),
-                ("purify", ctypes.c_int), ("batch_streams", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+                ("purify", ctypes.c_int), ("batch_streams", ctypes.c_int), ("incremental", ctypes.c_int),
+                ("reserved", ctypes.c_int * 5)]
 
 
 class Result(ctypes.Structure):

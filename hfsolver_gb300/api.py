@@ -203,6 +203,7 @@ class RHFOptions:
     mp2_nocc: int = 0          # <= 0: sum(Z)/2
     purify: bool = False       # SP2 density purification instead of an eigensolve per iteration
     batch_streams: int = 0     # rhf_batch: molecules in flight at once (<= 0: 8)
+    incremental: bool = False  # Fock builds from screened density differences
 
     def to_c(self):
         o = _lib.Options()
@@ -215,6 +216,7 @@ class RHFOptions:
         o.mp2_nocc = self.mp2_nocc
         o.purify = 1 if self.purify else 0
         o.batch_streams = self.batch_streams
+        o.incremental = 1 if self.incremental else 0
         return o
 
 

@@ -154,9 +154,10 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         in.tolE = opt.tolE; in.tolP = opt.tolP; in.alpha = opt.mix_alpha;
         in.accel = opt.scf_accel; in.diis_size = opt.diis_size > 0 ? opt.diis_size : 8;
         in.purify = opt.purify != 0;
-        in.direct_jk = [](Context& c, void* user, const double* P, double* G) {
-            eri_digest(c, (EriPlan*)user, P, G);
+        in.direct_jk = [](Context& c, void* user, const double* P, double* G, double screen) {
+            eri_digest(c, (EriPlan*)user, P, G, screen);
         };
+        if (opt.incremental) in.inc_screen = opt.schwarz > 0 ? opt.schwarz : 1e-12;
         in.direct_ctx = plan.get();
         ScfOut so = run_scf(ctx, in, dC.p, dP.p, dL.p);
         res->ms_scf = ts.ms();

@@ -337,6 +337,7 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
             groups.push_back(std::move(gg));
         }
         P->gpairs = to_device(gp, st);
+        P->dQ = to_device(P->Q, st);
 
         // segments per class
         std::vector<int64_t> prefix;
@@ -433,7 +434,28 @@ static int digest_split(const ClassPlan& c)
     return s;
 }
 
-void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG)
+// largest |P| element of each shell pair
+__global__ void shell_dmax_kernel(int ns, const int* __restrict__ L, const int* __restrict__ cfn0,
+                                  const int* __restrict__ comp_fn, const double* __restrict__ P, int n,
+                                  double* __restrict__ Dm)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ns * ns) return;
+    const int s1 = idx / ns, s2 = idx - s1 * ns;
+    const int n1 = ncart(L[s1]), n2 = ncart(L[s2]);
+    double m = 0.0;
+    for (int i = 0; i < n1; ++i) {
+        const int f = comp_fn[cfn0[s1] + i];
+        if (f < 0) continue;
+        for (int j = 0; j < n2; ++j) {
+            const int g = comp_fn[cfn0[s2] + j];
+            if (g >= 0) m = fmax(m, fabs(P[f + (int64_t)g * n]));
+        }
+    }
+    Dm[idx] = m;
+}
+
+void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG, double screen)
 {
     HF_CHECK(P->blocks.p != nullptr, HFGPU_ERR_INVALID, "eri_digest: integrals were not kept");
     const int n = P->basis.nbf;
@@ -444,6 +466,15 @@ void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG)
     HF_CUDA(cudaEventCreate(&e0));
     HF_CUDA(cudaEventCreate(&e1));
     HF_CUDA(cudaEventRecord(e0, ctx.stream));
+    const int ns = (int)P->basis.shells.size();
+    DBuf<double> Dm;
+    if (screen > 0) {
+        Dm.alloc((size_t)ns * ns, ctx.stream);
+        shell_dmax_kernel<<<(ns * ns + 127) / 128, 128, 0, ctx.stream>>>(ns, P->sL.p, P->scf.p, P->cfn.p, dP, n,
+                                                                        Dm.p);
+        count_launch();
+        HF_CUDA(cudaGetLastError());
+    }
     // the classes are independent until the symmetrisation: spread them over the
     // side streams, largest blocks first
     ctx.fork();
@@ -465,6 +496,10 @@ void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG)
         a.n = n;
         a.Gh = Gh.p;
         a.split = digest_split(c);
+        a.screen = screen;
+        a.Q = P->dQ.p;
+        a.Dm = Dm.p;
+        a.ns = ns;
         cudaStream_t s = ctx.aux[slot++ % Context::NAUX];
         if (a.split == 1)
             digest_fn(c.tb, c.tk)<<<(unsigned)((c.nq + 127) / 128), 128, 0, s>>>(a);

@@ -32,6 +32,7 @@ struct EriPlan {
     DBuf<double> pdata;
     // screening
     std::vector<double> Q;
+    DBuf<double> dQ;
     DBuf<int> gpairs;
     DBuf<int64_t> prefix;
     std::vector<ClassPlan> classes;

@@ -178,8 +178,10 @@ void eri_compute_packed(Context& ctx, EriPlan* p, double* d_out, EriStats* st);
 // the same, d_out may be null; keep_blocks also keeps the screened quartet blocks
 // in HBM for eri_digest
 void eri_compute(Context& ctx, EriPlan* p, double* d_out, bool keep_blocks, EriStats* st);
-// G = J - K/2 of density dP from the kept quartet blocks (n x n)
-void eri_digest(Context& ctx, EriPlan* p, const double* dP, double* dG);
+// G = J - K/2 of density dP from the kept quartet blocks (n x n); screen > 0
+// leaves out quartets whose Schwarz bound times the largest |dP| element they
+// touch is below screen (for density differences)
+void eri_digest(Context& ctx, EriPlan* p, const double* dP, double* dG, double screen = 0.0);
 
 // one-electron integrals (onee.cu): S, T, V on the device (n x n, symmetric)
 void onee_compute(Context& ctx, const Basis& b, int natoms, const int* atno, const double* x,

@@ -33,7 +33,26 @@ struct DigestArgs {
     int n;
     double* Gh;
     int split;  // lanes per quartet (digest_wide_kernel; a power of two <= 32)
+    // density-difference screening (screen > 0): pair Schwarz bounds Q and the
+    // largest |P| element of each shell pair, Dm[S1 * ns + S2]
+    double screen;
+    const double* Q;
+    const double* Dm;
+    int ns;
 };
+
+// true if the quartet's whole contribution is below the screening threshold:
+// |(ab|cd)| <= Q_bra Q_ket, and the largest density factor it meets is
+// 2|P_ab|, 2|P_cd| (Coulomb) or |P_ac|/2 ... (exchange)
+__device__ __forceinline__ bool digest_skip(const DigestArgs& a, int bra, int ket, int A, int B, int C, int D)
+{
+    if (a.screen <= 0.0) return false;
+    const double* Dm = a.Dm;
+    const int ns = a.ns;
+    const double dj = fmax(Dm[A * ns + B], Dm[C * ns + D]);
+    const double dk = fmax(fmax(Dm[A * ns + C], Dm[B * ns + D]), fmax(Dm[A * ns + D], Dm[B * ns + C]));
+    return a.Q[bra] * a.Q[ket] * fmax(2.0 * dj, 0.5 * dk) < a.screen;
+}
 
 template <int TB, int TK>
 __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
@@ -65,6 +84,7 @@ __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
         ket = a.gpairs[sg.ket0 + (int)(q - pf[l2])];
     }
     const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
+    if (digest_skip(a, bra, ket, A, B, C, D)) return;
     int fa[NA], fb[NB], fc[NC], fd[ND];
 #pragma unroll
     for (int i = 0; i < NA; ++i) fa[i] = a.sh.comp_fn[a.sh.cfn0[A] + i];
@@ -201,6 +221,7 @@ __global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
         ket = a.gpairs[sg.ket0 + (int)(q - pf[l2])];
     }
     const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
+    if (digest_skip(a, bra, ket, A, B, C, D)) return;  // same answer for all lanes of the quartet
     int fc[NC], fd[ND];
 #pragma unroll
     for (int i = 0; i < NC; ++i) fc[i] = a.sh.comp_fn[a.sh.cfn0[C] + i];

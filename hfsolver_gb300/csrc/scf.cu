@@ -25,6 +25,12 @@ __global__ void add_kernel(int64_t nn, const double* __restrict__ A, const doubl
     if (i < nn) C[i] = A[i] + B[i];
 }
 
+__global__ void sub_kernel(int64_t nn, const double* __restrict__ A, const double* __restrict__ B, double* C)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nn) C[i] = A[i] - B[i];
+}
+
 __global__ void mix_kernel(int64_t nn, double alpha, const double* __restrict__ Pold, double* P)
 {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -316,12 +322,39 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
 
     std::vector<double> Escf;
     ScfOut out;
+    // incremental Fock builds: Gacc = G(Pacc); each iteration adds G(P - Pacc)
+    const bool inc = in.direct_jk && in.inc_screen > 0;
+    DBuf<double> Gacc, Pacc;
+    if (inc) {
+        Gacc.alloc(nn, st);
+        Pacc.alloc(nn, st);
+    }
+    int since_full = 0;
+    bool last_full = true, need_full = false;
     for (int it = 1; it <= in.nscf; ++it) {
-        if (in.direct_jk)
-            in.direct_jk(ctx, in.direct_ctx, dP, G.p);
-        else
+        const double* Gcur = G.p;
+        if (inc) {
+            last_full = it == 1 || need_full || since_full >= in.inc_rebuild;
+            if (last_full) {
+                in.direct_jk(ctx, in.direct_ctx, dP, Gacc.p, 0.0);
+                since_full = 0;
+            } else {
+                sub_kernel<<<nblk(nn), 256, 0, st>>>(nn, dP, Pacc.p, Pacc.p);  // Pacc <- P - Pacc
+                count_launch();
+                in.direct_jk(ctx, in.direct_ctx, Pacc.p, G.p, in.inc_screen);
+                add_kernel<<<nblk(nn), 256, 0, st>>>(nn, Gacc.p, G.p, Gacc.p);
+                count_launch();
+                ++since_full;
+            }
+            HF_CUDA(cudaMemcpyAsync(Pacc.p, dP, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+            need_full = false;
+            Gcur = Gacc.p;
+        } else if (in.direct_jk) {
+            in.direct_jk(ctx, in.direct_ctx, dP, G.p, 0.0);
+        } else {
             jk_from_packed(ctx, n, in.d_int2, dP, G.p);
-        add_kernel<<<nblk(nn), 256, 0, st>>>(nn, in.dH, G.p, F.p);
+        }
+        add_kernel<<<nblk(nn), 256, 0, st>>>(nn, in.dH, Gcur, F.p);
         count_launch();
         reduce(ctx, 0, nn, dP, in.dH, F.p, scal.p);  // E0
         const double* Fsolve = F.p;
@@ -398,7 +431,9 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
         if (it > 3) {
             double emax = *std::max_element(Escf.end() - 4, Escf.end());
             double emin = *std::min_element(Escf.end() - 4, Escf.end());
-            if (dPv < in.tolP && emax - emin < in.tolE) {
+            if (dPv < in.tolP && emax - emin < in.tolE && !last_full) {
+                need_full = true;  // accept convergence only on a fully built Fock matrix
+            } else if (dPv < in.tolP && emax - emin < in.tolE) {
                 if (in.purify) {
                     // orbitals and orbital energies of the last Fock matrix, as the reference returns them
                     HF_CUDA(cudaMemcpyAsync(Sw.p, in.dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));

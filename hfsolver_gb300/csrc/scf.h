@@ -4,7 +4,10 @@
 
 namespace hfgpu {
 
-using DirectJK = void (*)(Context& ctx, void* user, const double* dP, double* dG);
+// G = J - K/2 of the density dP into dG.  screen > 0: a density difference;
+// quartets whose Schwarz bound times the largest |dP| element they touch is
+// below screen may be left out.
+using DirectJK = void (*)(Context& ctx, void* user, const double* dP, double* dG, double screen);
 
 struct ScfIn {
     int n = 0, nocc = 0, nscf = 40;
@@ -17,6 +20,11 @@ struct ScfIn {
     int accel = HFGPU_SCF_MIXING;
     int diis_size = 8;
     bool purify = false;  // density by SP2 purification instead of dsygvd each iteration
+    // incremental Fock builds (direct_jk only): G(P_k) = G(P_j) + G(P_k - P_j)
+    // with the difference screened at inc_screen; a full build every
+    // inc_rebuild iterations and before convergence is accepted.  0: off.
+    double inc_screen = 0.0;
+    int inc_rebuild = 8;
 };
 
 struct ScfOut {

@@ -176,7 +176,10 @@ typedef struct {
                             final dsygvd for the orbitals; 0: dsygvd every iteration (reference) */
     int batch_streams;   /* hfgpu_rhf_batch: molecules in flight at once, each on its own
                             streams; <= 0: 8 */
-    int reserved[6];
+    int incremental;     /* 1: Fock builds from density differences, screened at the Schwarz
+                            threshold (1e-12 if none), a full build every 8 iterations and
+                            before convergence is accepted; 0: full builds (reference) */
+    int reserved[5];
 } hfgpu_options;
 
 typedef struct {

@@ -32,6 +32,18 @@ def test_cluster_energies(nw, mp2):
 
 
 @pytest.mark.parametrize("nw", sorted(FIX, key=int))
+def test_cluster_energies_bench_configuration(nw):
+    """The bench's SCF: DIIS, SP2 purification and Fock builds from screened
+    density differences (full rebuild every 8 iterations and at convergence)."""
+    f = FIX[nw]
+    atno, xyz = water_cluster(f["n_waters"], seed=f["seed"])
+    r = hf.rhf(atno, xyz, hf.RHFOptions(nscf=60, diis=True, schwarz=1e-12, tolP=1e-10, tolE=1e-12,
+                                        mp2="split_bf16", purify=True, incremental=True))
+    assert abs(r["Etot"] - f["Etot"]) <= 1e-10
+    assert abs(r["E2"] - f["E2"]) <= 1e-8
+
+
+@pytest.mark.parametrize("nw", sorted(FIX, key=int))
 def test_cluster_packed_integrals(oracle, nw):
     f = FIX[nw]
     atno, xyz = water_cluster(f["n_waters"], seed=f["seed"])

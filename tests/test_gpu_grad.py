@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 H = 1e-4
 TOL = 1e-6
-OPT = dict(mp2="none", diis=True, tolP=1e-11, tolE=1e-13, nscf=200)
+OPT = dict(mp2="none", diis=True, tolP=1e-11, tolE=1e-11, nscf=200)
 
 
 def _fd(energy, xyz, coords):
@@ -43,7 +43,7 @@ def test_water_gradient_vs_oracle_fd(oracle):
     _, g = hf.rhf_gradient(atno, xyz, hf.RHFOptions(**OPT))
 
     def e_oracle(x):
-        return oracle.rhf_gauss(atno, x, nscf=200, tolE=1e-13, tolP=1e-11, diis=8)["Etot"]
+        return oracle.rhf_gauss(atno, x, nscf=200, tolE=1e-11, tolP=1e-11, diis=8)["Etot"]
 
     coords = [(a, k) for a in range(3) for k in range(3)]
     fd = _fd(e_oracle, xyz, coords)
