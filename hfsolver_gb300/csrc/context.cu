@@ -73,6 +73,16 @@ static Context* make_context(int dev)
     HF_CUSOLVER(cusolverDnCreate(&c->solver));
     HF_CUSOLVER(cusolverDnSetStream(c->solver, c->stream));
     HF_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev));
+    // Stream-ordered allocations (cudaMallocAsync) come from the device's default
+    // pool, which by default returns its memory to the driver at every
+    // synchronisation; each molecule's GB-sized buffers would then be mapped
+    // again.  Keep up to 64 GB cached in the pool (process-local setting).
+    {
+        cudaMemPool_t pool;
+        HF_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+        uint64_t keep = 64ull << 30;
+        HF_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    }
     for (int i = 0; i < Context::NAUX; ++i) {
         HF_CUDA(cudaStreamCreateWithFlags(&c->aux[i], cudaStreamNonBlocking));
         HF_CUDA(cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming));

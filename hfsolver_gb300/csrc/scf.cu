@@ -155,6 +155,92 @@ __global__ void __launch_bounds__(SQ_T* SQ_T) sym_square_kernel(int n, const dou
     }
 }
 
+// The whole SP2 recursion in one cooperative launch: one block per upper-
+// triangle 16x16 tile of the iterate X, grid-wide barriers between the square
+// and the update, the square-or-not choice and the convergence test made by
+// every block from the same traces.  A block keeps its own tile of X^2 in
+// registers, so only X travels through memory (read past L1: other blocks
+// wrote it).  Every barrier wait is bounded; a timeout sets err and all blocks
+// leave.
+struct Sp2Sync {
+    unsigned count, gen;
+    int err, steps;
+};
+
+__device__ bool sp2_grid_barrier(Sp2Sync* s, unsigned nblocks)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = &s->gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        if (atomicAdd(&s->count, 1u) == nblocks - 1) {
+            atomicExch(&s->count, 0u);
+            __threadfence();
+            atomicAdd(&s->gen, 1u);
+        } else {
+            long spins = 0;
+            while (*vgen == g) {
+                if (++spins > (1L << 22)) {
+                    atomicExch(&s->err, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        ok = *(volatile int*)&s->err == 0;
+    }
+    __syncthreads();
+    return ok;
+}
+
+__global__ void __launch_bounds__(SQ_T* SQ_T) sp2_persistent_kernel(int n, int nocc, double* X, double* tr, int maxs,
+                                                                    Sp2Sync* sync)
+{
+    __shared__ double As[SQ_T][SQ_T + 1], Bs[SQ_T][SQ_T + 1];
+    const int nt = (n + SQ_T - 1) / SQ_T;
+    int b = blockIdx.x, ti = 0;
+    while (b >= nt - ti) {
+        b -= nt - ti;
+        ++ti;
+    }
+    const int tj = ti + b;
+    const int ty = threadIdx.x / SQ_T, tx = threadIdx.x % SQ_T;
+    const int i = ti * SQ_T + ty, j = tj * SQ_T + tx;
+    const bool own = i < n && j < n;
+    for (int it = 0; it < maxs; ++it) {
+        double acc = 0.0;
+        for (int k0 = 0; k0 < n; k0 += SQ_T) {
+            const int ka = k0 + tx, kb = k0 + ty;
+            As[ty][tx] = (i < n && ka < n) ? __ldcg(X + i + (int64_t)ka * n) : 0.0;
+            Bs[ty][tx] = (kb < n && j < n) ? __ldcg(X + kb + (int64_t)j * n) : 0.0;
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < SQ_T; ++k) acc = fma(As[ty][k], Bs[k][tx], acc);
+            __syncthreads();
+        }
+        if (own && i == j) atomicAdd(tr + 2 * it + 1, acc);
+        if (!sp2_grid_barrier(sync, gridDim.x)) return;
+        const double t0 = __ldcg(tr + 2 * it), t1 = __ldcg(tr + 2 * it + 1);
+        const bool square = fabs(t1 - nocc) <= fabs(2 * t0 - t1 - nocc);
+        const bool done = fabs(t0 - t1) < 1e-13 * n && fabs(t0 - nocc) < 1e-6;
+        if (own) {
+            const double x = square ? acc : 2 * __ldcg(X + i + (int64_t)j * n) - acc;
+            X[i + (int64_t)j * n] = x;
+            if (ti != tj) X[j + (int64_t)i * n] = x;
+            if (i == j) atomicAdd(tr + 2 * it + 2, x);
+        }
+        if (done) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) sync->steps = it + 1;
+            return;
+        }
+        if (!sp2_grid_barrier(sync, gridDim.x)) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) sync->steps = maxs;
+}
+
 // X = (emax I - F) / (emax - emin): spectrum mapped into [0, 1], occupied states
 // near 1; trX = tr X of this initial iterate
 __global__ void sp2_init2_kernel(int n, const double* __restrict__ F, const double* __restrict__ b, double* X,
@@ -182,9 +268,20 @@ __global__ void sp2_step_kernel(int n, int nocc, const double* __restrict__ t, c
     if (i == j) atomicAdd(tnext, x);
 }
 
+// can all `blocks` blocks of the persistent SP2 kernel be resident at once?
+static bool coop_ok(Context& ctx, unsigned blocks)
+{
+    int coop = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx.device) != cudaSuccess || !coop) return false;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sp2_persistent_kernel, SQ_T * SQ_T, 0) != cudaSuccess)
+        return false;
+    return (int64_t)per_sm * ctx.num_sms >= (int64_t)blocks;
+}
+
 struct Purifier {
     int n = 0, nocc = 0;
     DBuf<double> X, T1, T2, B, tr;  // orthogonaliser S^-1/2 and work
+    DBuf<Sp2Sync> sync;
     void setup(Context& ctx, int n_, int nocc_, const double* dS)
     {
         n = n_;
@@ -236,6 +333,29 @@ struct Purifier {
         const unsigned tiles = (unsigned)(nt * (nt + 1) / 2);
         double h[2] = {0, 1};
         bool done = false;
+        if (coop_ok(ctx, tiles)) {
+            // one cooperative launch for the whole recursion
+            if (!sync.p) sync.alloc(1, st);
+            HF_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(Sp2Sync), st));
+            int n_ = n, nocc_ = nocc, maxs = MAXS;
+            double* Xp = T1.p;
+            double* trp = tr.p;
+            Sp2Sync* sp = sync.p;
+            void* args[] = {&n_, &nocc_, &Xp, &trp, &maxs, &sp};
+            HF_CUDA(cudaLaunchCooperativeKernel((const void*)sp2_persistent_kernel, dim3(tiles), dim3(SQ_T * SQ_T),
+                                                args, 0, st));
+            count_launch();
+            Sp2Sync hs{};
+            std::vector<double> ht((size_t)2 * (MAXS + 1));
+            HF_CUDA(cudaMemcpyAsync(&hs, sync.p, sizeof(Sp2Sync), cudaMemcpyDeviceToHost, st));
+            HF_CUDA(cudaMemcpyAsync(ht.data(), tr.p, sizeof(double) * ht.size(), cudaMemcpyDeviceToHost, st));
+            HF_CUDA(cudaStreamSynchronize(st));
+            HF_CHECK(hs.err == 0, HFGPU_ERR_CUDA, "density purification: grid barrier timed out");
+            const int last = std::max(hs.steps, 1) - 1;
+            h[0] = ht[2 * last];
+            h[1] = ht[2 * last + 1];
+            done = true;
+        }
         for (int it = 0; it < MAXS && !done; ++it) {
             sym_square_kernel<<<tiles, SQ_T * SQ_T, 0, st>>>(n, T1.p, T2.p, tr.p + 2 * it + 1);
             count_launch();
@@ -329,12 +449,14 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
         Gacc.alloc(nn, st);
         Pacc.alloc(nn, st);
     }
+    // near convergence (dP < 100 tolP) every build is a full one, so the last
+    // iterations converge exactly like the full-build SCF
     int since_full = 0;
-    bool last_full = true, need_full = false;
+    bool last_full = true, endgame = false;
     for (int it = 1; it <= in.nscf; ++it) {
         const double* Gcur = G.p;
         if (inc) {
-            last_full = it == 1 || need_full || since_full >= in.inc_rebuild;
+            last_full = it == 1 || endgame || since_full >= in.inc_rebuild;
             if (last_full) {
                 in.direct_jk(ctx, in.direct_ctx, dP, Gacc.p, 0.0);
                 since_full = 0;
@@ -347,7 +469,6 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
                 ++since_full;
             }
             HF_CUDA(cudaMemcpyAsync(Pacc.p, dP, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
-            need_full = false;
             Gcur = Gacc.p;
         } else if (in.direct_jk) {
             in.direct_jk(ctx, in.direct_ctx, dP, G.p, 0.0);
@@ -424,6 +545,7 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
                  "eigh: dsygvd returned info = " + std::to_string(hinfo) +
                      (hinfo > n ? " (S is not positive definite)" : ""));
         const double E0 = h[0], dPv = h[1];
+        if (dPv < 100 * in.tolP) endgame = true;
         Escf.push_back(E0);
         out.E0 = E0;
         out.dP = dPv;
@@ -432,7 +554,7 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
             double emax = *std::max_element(Escf.end() - 4, Escf.end());
             double emin = *std::min_element(Escf.end() - 4, Escf.end());
             if (dPv < in.tolP && emax - emin < in.tolE && !last_full) {
-                need_full = true;  // accept convergence only on a fully built Fock matrix
+                endgame = true;  // accept convergence only on a fully built Fock matrix
             } else if (dPv < in.tolP && emax - emin < in.tolE) {
                 if (in.purify) {
                     // orbitals and orbital energies of the last Fock matrix, as the reference returns them
