@@ -349,6 +349,7 @@ def run_batch(args):
     mols = water_batch(args.batch, seed=rank)
     opt = options("split_bf16")
     opt.batch_streams = args.streams
+    opt.autotune = True  # quartet-tile shapes timed on the first molecules of each size, then reused
     for w in range(args.warmup):
         hf.rhf_batch(mols[w * 4:(w + 1) * 4], opt)
     clocks = ClockSampler(local)
@@ -388,6 +389,7 @@ def run_batch(args):
         "config": {"workload": f"water_batch{len(mols)}_1to12_jitter0.05A_631gss_rhf_diis_schwarz1e-12_mp2",
                    "molecules": len(mols), "nbf_min": min(nbf), "nbf_max": max(nbf), "nbf_mean": float(np.mean(nbf)),
                    "mp2": "split_bf16", "batch_streams": args.streams,
+                   "autotuned_shapes": len(hf.autotune_table()),
                    "timing": "host wall clock between device-wide synchronizes (molecules run on several streams)",
                    "parallelism": f"replicas x{world}"},
         "plain_fp64_one_at_a_time": {"molecules_per_s": len(sub) / wall_plain, "sample": f"every 8th molecule ({len(sub)})",

@@ -23,7 +23,7 @@ class Options(ctypes.Structure):
                 ("tolP", ctypes.c_double), ("scf_accel", ctypes.c_int), ("diis_size", ctypes.c_int),
                 ("schwarz", ctypes.c_double), ("mp2", ctypes.c_int), ("mp2_nocc", ctypes.c_int),
                 ("purify", ctypes.c_int), ("batch_streams", ctypes.c_int), ("incremental", ctypes.c_int),
-                ("reserved", ctypes.c_int * 5)]
+                ("autotune", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
 
 
 class Result(ctypes.Structure):
@@ -70,6 +70,8 @@ SIGNATURES = {
                                  _dp]),
     "hfgpu_rhf_gradient": (ctypes.c_int, [ctypes.c_int, _ip, _dp, ctypes.POINTER(Options), ctypes.POINTER(Result),
                                           _dp]),
+    "hfgpu_autotune_table": (ctypes.c_int64, [ctypes.c_char_p, ctypes.c_int64]),
+    "hfgpu_autotune_clear": (None, []),
 }
 
 _LIB = None

@@ -21,6 +21,7 @@ rhf_gauss / rhf        src/drivers.f90:12-51 (+ MBPT2)                 hfgpu_rhf
 Errors raise HFGPUError (the reference stops the process instead); an SCF
 that does not converge raises SCFNotConverged, like stop_error in doscf.
 """
+import ctypes
 from dataclasses import dataclass
 
 import numpy as np
@@ -204,6 +205,7 @@ class RHFOptions:
     purify: bool = False       # SP2 density purification instead of an eigensolve per iteration
     batch_streams: int = 0     # rhf_batch: molecules in flight at once (<= 0: 8)
     incremental: bool = False  # Fock builds from screened density differences
+    autotune: bool = False     # time candidate kernel shapes on first use, keep the fastest
 
     def to_c(self):
         o = _lib.Options()
@@ -217,6 +219,7 @@ class RHFOptions:
         o.purify = 1 if self.purify else 0
         o.batch_streams = self.batch_streams
         o.incremental = 1 if self.incremental else 0
+        o.autotune = 1 if self.autotune else 0
         return o
 
 
@@ -260,6 +263,24 @@ def rhf_gradient(atno, xyz, options=None):
     _check(code)
     out = {k: getattr(res, k) for k, _ in _lib.Result._fields_ if k != "reserved"}
     return out, g
+
+
+def autotune_table():
+    """The autotuner's choices: a list of (kernel, bra type, ket type, size
+    bucket, choice) tuples (see hfgpu_autotune_table)."""
+    L = _lib.lib()
+    n = L.hfgpu_autotune_table(None, 0)
+    buf = ctypes.create_string_buffer(int(n) + 1)
+    L.hfgpu_autotune_table(buf, n + 1)
+    out = []
+    for line in buf.value.decode().splitlines():
+        k, tb, tk, b, c = line.split()
+        out.append((k, int(tb), int(tk), int(b), int(c)))
+    return out
+
+
+def autotune_clear():
+    _lib.lib().hfgpu_autotune_clear()
 
 
 def rhf_batch(molecules, options=None):

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "autotune.h"
 #include "internal.h"
 #include "scf.h"
 #include "tcgemm.h"
@@ -116,6 +117,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         Context& ctx = ctx_in ? *ctx_in : context();
         cudaStream_t st = ctx.stream;
         ctx.stat_fock_ms = ctx.stat_tc_ms = ctx.stat_tc_flops = 0;
+        ctx.tune = opt.autotune != 0 || tune_env_enabled();
         Timer total(st);
         const int n = b.nbf;
         int nelec = 0;
@@ -451,6 +453,19 @@ void hfgpu_default_options(hfgpu_options* o)
     o->mp2 = HFGPU_MP2_FP64;
     o->mp2_nocc = 0;
 }
+
+int64_t hfgpu_autotune_table(char* buf, int64_t len)
+{
+    const std::string s = tune_dump();
+    if (buf && len > 0) {
+        const int64_t k = std::min<int64_t>(len - 1, (int64_t)s.size());
+        std::memcpy(buf, s.data(), (size_t)k);
+        buf[k] = 0;
+    }
+    return (int64_t)s.size();
+}
+
+void hfgpu_autotune_clear(void) { tune_clear(); }
 
 int hfgpu_basis_size(int natoms, const int* atno)
 {

@@ -32,6 +32,7 @@
 #include "boys.cuh"
 #include "eri_kernel.cuh"
 #include "internal.h"
+#include "autotune.h"
 #include "eri_plan.h"
 #include "jk_blocks.cuh"
 #include "md.cuh"
@@ -158,12 +159,22 @@ static KernelFn get_kernel(int tb, int tk, int mode)
     return f;
 }
 
+// event-timed duration of the work between a and b (waits for b)
+static float elapsed(cudaEvent_t a, cudaEvent_t b)
+{
+    HF_CUDA(cudaEventSynchronize(b));
+    float ms = 0;
+    HF_CUDA(cudaEventElapsedTime(&ms, a, b));
+    return ms;
+}
+
 // lanes per quartet for kb x kk primitive quartets: enough independent work per
-// lane (about 16 primitive quartets) without idling the rest of the warp
-static int pick_split(int64_t kprod)
+// lane (between target and 2 target primitive quartets) without idling the rest
+// of the warp
+static int pick_split(int64_t kprod, int target = 16)
 {
     int s = 1;
-    while (s < 32 && kprod >= 32 * s) s <<= 1;
+    while (s < 32 && kprod >= 2 * (int64_t)target * s) s <<= 1;
     return s;
 }
 
@@ -388,6 +399,7 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
                         s.warp0 = c.nwarps;
                         s.qoff = c.nq;
                         s.split = pick_split((int64_t)A_.k * B_.k);
+                        c.kprod.push_back((int64_t)A_.k * B_.k);
                         const int64_t qpw = 32 / s.split;
                         c.nq += acc;
                         c.nwarps += (acc + qpw - 1) / qpw * G_;
@@ -455,6 +467,50 @@ __global__ void shell_dmax_kernel(int ns, const int* __restrict__ L, const int* 
     Dm[idx] = m;
 }
 
+static void launch_digest(const ClassPlan& c, const DigestArgs& a, cudaStream_t s)
+{
+    if (a.split == 1)
+        digest_fn(c.tb, c.tk)<<<(unsigned)((c.nq + 127) / 128), 128, 0, s>>>(a);
+    else
+        digest_wide_fn(c.tb, c.tk)<<<(unsigned)((c.nq * a.split + 127) / 128), 128, 0, s>>>(a);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+}
+
+// Lanes per quartet of the class's Fock digest: the built-in rule, or with
+// tuning on the fastest of 1, 2, 4, ... lanes timed once per (class, size
+// bucket) into a scratch matrix.
+static int digest_split_tuned(Context& ctx, const ClassPlan& c, DigestArgs a, int64_t nn)
+{
+    int split = digest_split(c);
+    if (!ctx.tune || c.nq == 0) return split;
+    const int bucket = tune_bucket(c.nq);
+    if (tune_get(TUNE_DIGEST, c.tb, c.tk, bucket, &split)) return split;
+    const int nab = ncart(ptype_la(c.tb)) * ncart(ptype_lb(c.tb));
+    DBuf<double> scratch(nn, ctx.stream);
+    scratch.zero();
+    a.Gh = scratch.p;
+    cudaEvent_t e0, e1;
+    HF_CUDA(cudaEventCreate(&e0));
+    HF_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int cand = 1; cand <= 32 && (cand == 1 || cand / 2 < nab); cand <<= 1) {
+        a.split = cand;
+        HF_CUDA(cudaEventRecord(e0, ctx.stream));
+        launch_digest(c, a, ctx.stream);
+        HF_CUDA(cudaEventRecord(e1, ctx.stream));
+        const float ms = elapsed(e0, e1);
+        if (ms < best) {
+            best = ms;
+            split = cand;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    tune_set(TUNE_DIGEST, c.tb, c.tk, bucket, split);
+    return split;
+}
+
 void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG, double screen)
 {
     HF_CHECK(P->blocks.p != nullptr, HFGPU_ERR_INVALID, "eri_digest: integrals were not kept");
@@ -495,18 +551,13 @@ void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG, double s
         a.P = dP;
         a.n = n;
         a.Gh = Gh.p;
-        a.split = digest_split(c);
         a.screen = screen;
         a.Q = P->dQ.p;
         a.Dm = Dm.p;
         a.ns = ns;
+        a.split = digest_split_tuned(ctx, c, a, nn);
         cudaStream_t s = ctx.aux[slot++ % Context::NAUX];
-        if (a.split == 1)
-            digest_fn(c.tb, c.tk)<<<(unsigned)((c.nq + 127) / 128), 128, 0, s>>>(a);
-        else
-            digest_wide_fn(c.tb, c.tk)<<<(unsigned)((c.nq * a.split + 127) / 128), 128, 0, s>>>(a);
-        count_launch();
-        HF_CUDA(cudaGetLastError());
+        launch_digest(c, a, s);
     }
     ctx.join();
     sym_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, ctx.stream>>>(n, Gh.p, dG);
@@ -532,6 +583,56 @@ static int block_size(int tb, int tk)
     return ncart(ptype_la(tb)) * ncart(ptype_lb(tb)) * ncart(ptype_la(tk)) * ncart(ptype_lb(tk));
 }
 
+// lay the warps of a class out again for another lanes-per-quartet target
+static void layout_class(Context& ctx, ClassPlan& c, int target)
+{
+    const int G_ = class_G(c.tb, c.tk);
+    c.nwarps = 0;
+    for (size_t i = 0; i < c.segs.size(); ++i) {
+        Seg& s = c.segs[i];
+        s.split = pick_split(c.kprod[i], target);
+        s.warp0 = c.nwarps;
+        const int64_t qpw = 32 / s.split;
+        c.nwarps += (s.nq + qpw - 1) / qpw * G_;
+    }
+    c.dsegs.upload(c.segs.data(), c.segs.size());
+    c.lane_target = target;
+}
+
+// The ERI launch of a class with the tuned lanes-per-quartet target.  On the
+// first molecule of a (class, size bucket) with tuning on, every candidate
+// target is timed on the real launch (the class writes the same values each
+// time) and the fastest is recorded.
+static void eri_class_tuned(Context& ctx, EriPlan* P, ClassPlan& c, double* d_out, double* blocks)
+{
+    int target = 16;
+    if (ctx.tune && c.nq > 0) {
+        const int bucket = tune_bucket(c.nq);
+        if (!tune_get(TUNE_ERI, c.tb, c.tk, bucket, &target)) {
+            cudaEvent_t a, b;
+            HF_CUDA(cudaEventCreate(&a));
+            HF_CUDA(cudaEventCreate(&b));
+            float best = 1e30f;
+            for (int cand : {4, 8, 16, 32, 64}) {
+                layout_class(ctx, c, cand);
+                HF_CUDA(cudaEventRecord(a, ctx.stream));
+                launch_class(ctx, P, c, MODE_PACKED, d_out, nullptr, blocks);
+                HF_CUDA(cudaEventRecord(b, ctx.stream));
+                const float ms = elapsed(a, b);
+                if (ms < best) {
+                    best = ms;
+                    target = cand;
+                }
+            }
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+            tune_set(TUNE_ERI, c.tb, c.tk, bucket, target);
+        }
+    }
+    if (c.lane_target != target) layout_class(ctx, c, target);
+    launch_class(ctx, P, c, MODE_PACKED, d_out, nullptr, blocks);
+}
+
 void eri_compute(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks, EriStats* st)
 {
     if (keep_blocks) {
@@ -548,8 +649,7 @@ void eri_compute(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks, EriS
     HF_CUDA(cudaEventRecord(e0, ctx.stream));
     // heaviest classes first so the tail of the launch sequence is short
     for (int i = (int)P->classes.size() - 1; i >= 0; --i)
-        launch_class(ctx, P, P->classes[i], MODE_PACKED, d_out, nullptr,
-                     keep_blocks ? P->blocks.p + P->classes[i].boff : nullptr);
+        eri_class_tuned(ctx, P, P->classes[i], d_out, keep_blocks ? P->blocks.p + P->classes[i].boff : nullptr);
     HF_CUDA(cudaEventRecord(e1, ctx.stream));
     HF_CUDA(cudaEventSynchronize(e1));
     float ms = 0;

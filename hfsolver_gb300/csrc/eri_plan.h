@@ -12,6 +12,8 @@ namespace hfgpu {
 struct ClassPlan {
     int tb, tk;
     std::vector<Seg> segs;
+    std::vector<int64_t> kprod;  // primitive quartets per quartet, per segment
+    int lane_target = 16;        // primitive quartets per lane that the splits were laid out for
     int64_t nwarps = 0;
     int64_t nq = 0;     // quartets of the class
     int64_t boff = 0;   // offset of the class's blocks in EriPlan::blocks

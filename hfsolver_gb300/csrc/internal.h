@@ -124,6 +124,7 @@ struct Context {
     void join();  // `stream` waits for the work queued on the aux streams
     // kernel-time counters, reset by the pipeline entry points
     double stat_fock_ms = 0, stat_tc_ms = 0, stat_tc_flops = 0;
+    bool tune = false;  // time candidate kernel shapes on first use (autotune.cpp)
 };
 Context& context();  // for the current device
 Context* context_acquire();        // a separate context on the current device (pooled)

@@ -21,6 +21,23 @@ namespace hfgpu {
 
 static const int64_t SLICE_BUDGET_ROWS = 1 << 20;  // rows per sliced operand (x K_pad x 10 bytes)
 
+// out[c][r] = in[r][c] for a rows x cols row-major matrix (32 x 32 tiles through
+// shared memory, both sides coalesced)
+__global__ void transpose_kernel(const double* __restrict__ in, int64_t rows, int64_t cols, double* __restrict__ out)
+{
+    __shared__ double t[32][33];
+    const int64_t c0 = (int64_t)blockIdx.x * 32, r0 = (int64_t)blockIdx.y * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int64_t r = r0 + y, c = c0 + threadIdx.x;
+        if (r < rows && c < cols) t[y][threadIdx.x] = in[r * cols + c];
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int64_t c = c0 + y, r = r0 + threadIdx.x;
+        if (r < rows && c < cols) out[c * rows + r] = t[threadIdx.x][y];
+    }
+}
+
 void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, int n1, const double* C2, int n2,
                   double* T)
 {
@@ -46,13 +63,23 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
         slice_dense(ctx, Y.p, np * n1, n, n, A, SLICE_TILE_A);
         sliced_gemm(ctx, A, B2, Z.p + p0 * nq, OutMap{0, n2}, false);  // rows (p, j) -> Z[p][j][b]
     }
+    // Z^T: one contiguous row of pairs per q, so that the (q, mu) rows of step 3
+    // gather from one L2-resident row instead of one cache line per element
+    DBuf<double> Zt((size_t)npair * nq, st);
+    {
+        const dim3 grid((unsigned)((nq + 31) / 32), (unsigned)((npair + 31) / 32));
+        transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(Z.p, npair, nq, Zt.p);
+        count_launch();
+        HF_CUDA(cudaGetLastError());
+        Z.release();
+    }
     // steps 3-4 over blocks of q
     const int64_t qb = std::max<int64_t>(1, SLICE_BUDGET_ROWS / std::max(n, n1));
     DBuf<double> W((size_t)std::min(qb, nq) * n1 * n, st);
     for (int64_t q0 = 0; q0 < nq; q0 += qb) {
         const int64_t nqb = std::min(qb, nq - q0);
-        // rows (q, mu) over nu of Z[pair(mu, nu)][q0 + q]
-        slice_sympair(ctx, Z.p + q0, nq, nqb, n, A);
+        // rows (q, mu) over nu of Zt[q0 + q][pair(mu, nu)]
+        slice_sympair(ctx, Zt.p + q0 * npair, npair, nqb, n, A);
         sliced_gemm(ctx, A, B1, W.p, OutMap{n, n1}, false);  // rows (q, mu) -> W[q][i][mu]
         slice_dense(ctx, W.p, nqb * n1, n, n, A, SLICE_TILE_A);
         sliced_gemm(ctx, A, B2, T + q0 * n1 * n2, OutMap{0, n2}, false);  // rows (q, i) -> T[q][i][a]

@@ -284,7 +284,8 @@ __device__ __forceinline__ int row_exponent(double amax)
     return (int)((((uint64_t)__double_as_longlong(amax)) >> 52) & 0x7FF) - 1022;
 }
 
-// One warp per row.  Element (r, k) of the source is fetched by Src::get(r, k).
+// One warp per row.  Src::row(r) sets up the row once; element (r, k) is
+// Src::at(row, k).
 template <class Src>
 __global__ void slice_kernel(Src src, int64_t rows, int K, int64_t rows_pad, int K_pad, __nv_bfloat16* planes,
                              int* rexp)
@@ -293,12 +294,13 @@ __global__ void slice_kernel(Src src, int64_t rows, int K, int64_t rows_pad, int
     const int lane = threadIdx.x & 31;
     const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += nwarp) {
+        const typename Src::Row row = src.row(r);
         double x[KMAX];
         double amax = 0.0;
 #pragma unroll
         for (int q = 0; q < KMAX; ++q) {
             const int k = lane + 32 * q;
-            x[q] = (k < K) ? src.get(r, k) : 0.0;
+            x[q] = (k < K) ? src.at(row, k) : 0.0;
             amax = fmax(amax, fabs(x[q]));
         }
 #pragma unroll
@@ -321,7 +323,9 @@ __global__ void slice_kernel(Src src, int64_t rows, int K, int64_t rows_pad, int
 struct DenseRows {  // row-major rows with stride ld
     const double* p;
     int64_t ld;
-    __device__ double get(int64_t r, int k) const { return p[r * ld + k]; }
+    using Row = const double*;
+    __device__ Row row(int64_t r) const { return p + r * ld; }
+    __device__ double at(Row w, int k) const { return __ldg(w + k); }
 };
 
 struct PackedRows {  // rows (pair p, la), k = si of the packed (mu nu|la si), pairs mu >= nu from p0
@@ -329,26 +333,42 @@ struct PackedRows {  // rows (pair p, la), k = si of the packed (mu nu|la si), p
     const int2* pairs;
     int64_t p0;
     int n;
-    __device__ double get(int64_t r, int k) const
+    struct Row {
+        int64_t ij, ij_base;  // pair index of (mu, nu) and ij (ij + 1) / 2
+        int la;
+    };
+    __device__ Row row(int64_t r) const
     {
-        const int2 mn = pairs[p0 + r / n];
-        const int64_t la = r % n, si = k;
-        const int64_t a = mn.x, b = mn.y;
-        const int64_t c = la > si ? la : si, d = la > si ? si : la;
-        const int64_t ij = a * (a + 1) / 2 + b, kl = c * (c + 1) / 2 + d;
-        return ints[ij >= kl ? ij * (ij + 1) / 2 + kl : kl * (kl + 1) / 2 + ij];
+        const int64_t p = r / n;
+        const int2 mn = pairs[p0 + p];
+        const int64_t ij = (int64_t)mn.x * (mn.x + 1) / 2 + mn.y;
+        return Row{ij, ij * (ij + 1) / 2, (int)(r - p * n)};
+    }
+    __device__ double at(const Row& w, int si) const
+    {
+        const int c = w.la > si ? w.la : si, d = w.la > si ? si : w.la;
+        const int64_t kl = (int64_t)(c * (c + 1) / 2 + d);
+        return __ldg(ints + (w.ij >= kl ? w.ij_base + kl : kl * (kl + 1) / 2 + w.ij));
     }
 };
 
-struct SymPairRows {  // rows (q, mu), k = nu of Z[pair(mu, nu) * ldz + q]
-    const double* Z;
+struct SymPairRows {  // rows (q, mu), k = nu of Zt[q * ldz + pair(mu, nu)] (Z transposed: one row per q)
+    const double* Zt;
     int64_t ldz;
     int n;
-    __device__ double get(int64_t r, int k) const
+    struct Row {
+        const double* z;
+        int mu;
+    };
+    __device__ Row row(int64_t r) const
     {
-        const int64_t q = r / n, mu = r % n, nu = k;
-        const int64_t a = mu > nu ? mu : nu, b = mu > nu ? nu : mu;
-        return Z[(a * (a + 1) / 2 + b) * ldz + q];
+        const int64_t q = r / n;
+        return Row{Zt + q * ldz, (int)(r - q * n)};
+    }
+    __device__ double at(const Row& w, int nu) const
+    {
+        const int a = w.mu > nu ? w.mu : nu, b = w.mu > nu ? nu : w.mu;
+        return __ldg(w.z + (a * (a + 1) / 2 + b));
     }
 };
 
@@ -424,10 +444,10 @@ void slice_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p
     launch_slice(ctx, PackedRows{ints, pairs, p0, n}, s);
 }
 
-void slice_sympair(Context& ctx, const double* Z, int64_t ldz, int64_t nq, int n, Sliced& s)
+void slice_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, Sliced& s)
 {
     s.alloc(ctx, nq * n, n, BM);
-    launch_slice(ctx, SymPairRows{Z, ldz, n}, s);
+    launch_slice(ctx, SymPairRows{Zt, ldz, n}, s);
 }
 
 void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, OutMap om, bool accumulate)

@@ -29,8 +29,8 @@ constexpr int SLICE_TILE_A = 128, SLICE_TILE_B = 64;
 void slice_dense(Context& ctx, const double* A, int64_t rows, int K, int64_t ld, Sliced& s, int row_tile);
 // rows (pair p, la) over si of the packed (mu nu|la si), pairs[p0 .. p0+npairs)
 void slice_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n, Sliced& s);
-// rows (q, mu), q < nq, over nu of Z[pair(mu, nu) * ldz + q]
-void slice_sympair(Context& ctx, const double* Z, int64_t ldz, int64_t nq, int n, Sliced& s);
+// rows (q, mu), q < nq, over nu of Zt[q * ldz + pair(mu, nu)]
+void slice_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, Sliced& s);
 // out (+)= A B^T for slices A (M x K) and B (N x K)
 void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, OutMap om, bool accumulate);
 

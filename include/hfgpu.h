@@ -178,8 +178,12 @@ typedef struct {
                             streams; <= 0: 8 */
     int incremental;     /* 1: Fock builds from density differences, screened at the Schwarz
                             threshold (1e-12 if none), a full build every 8 iterations and
-                            before convergence is accepted; 0: full builds (reference) */
-    int reserved[5];
+                            near convergence; 0: full builds (reference) */
+    int autotune;        /* 1: time the candidate quartet-tile shapes of the ERI and Fock
+                            kernels the first time a (class, size) is met and keep the
+                            fastest (process-wide table); 0: built-in rules, unless the
+                            environment sets HFGPU_AUTOTUNE=1 */
+    int reserved[4];
 } hfgpu_options;
 
 typedef struct {
@@ -230,6 +234,15 @@ int hfgpu_rhf_gradient(int natoms, const int *atno, const double *xyz, const hfg
  * molecule order), or HFGPU_OK. */
 int hfgpu_rhf_batch(int nmol, const int *natoms, const int *atno, const double *xyz,
                     const hfgpu_options *opt, hfgpu_result *res);
+
+/* The autotuner's table as text, one line per tuned (kernel, quartet class,
+ * size bucket): "<eri|digest> <bra pair type> <ket pair type> <log2 quartets>
+ * <choice>" (choice: primitive quartets per lane for eri, lanes per quartet for
+ * digest).  Writes at most len bytes including the terminating NUL and returns
+ * the length of the whole text. */
+int64_t hfgpu_autotune_table(char *buf, int64_t len);
+/* forget every tuned shape */
+void hfgpu_autotune_clear(void);
 
 /* number of basis functions hfgpu_rhf will use for these atoms (0 on error) */
 int hfgpu_basis_size(int natoms, const int *atno);

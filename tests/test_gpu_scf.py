@@ -164,3 +164,25 @@ def test_rhf_batch_matches_single_calls():
         assert r["niter"] == single["niter"]
         assert abs(r["Etot"] - single["Etot"]) < 1e-11
         assert abs(r["E2"] - single["E2"]) < 1e-11
+
+
+def test_autotune_keeps_energies():
+    """Tuned kernel shapes (timed on first use, then reused) give the same SCF
+    and MBPT2 energies as the built-in rules."""
+    from hfsolver_gb300.clusters import water_cluster
+
+    atno, xyz = water_cluster(4, seed=2)
+    o = dict(diis=True, schwarz=1e-12, tolP=1e-10, tolE=1e-12, mp2="split_bf16")
+    hf.autotune_clear()
+    a = hf.rhf(atno, xyz, hf.RHFOptions(**o))
+    b = hf.rhf(atno, xyz, hf.RHFOptions(autotune=True, **o))
+    table = hf.autotune_table()
+    c = hf.rhf(atno, xyz, hf.RHFOptions(autotune=True, **o))
+    assert hf.autotune_table() == table  # second molecule reuses the table
+    kinds = {k for k, *_ in table}
+    assert kinds == {"eri", "digest"}
+    for r in (b, c):
+        assert abs(r["Etot"] - a["Etot"]) < 1e-10
+        assert abs(r["E2"] - a["E2"]) < 1e-9
+    hf.autotune_clear()
+    assert hf.autotune_table() == []
