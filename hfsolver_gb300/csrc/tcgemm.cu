@@ -17,11 +17,14 @@
 //     applies the row and column scales with one FP64 multiply.
 // The result matches an FP64 GEMM to about 2^-42 K max|A_r.| max|B_.c| per element.
 //
-// Kernel: one CTA (128 threads) per 128 x 64 output tile; per K step of 64 one
-// thread issues the TMA loads of the 6 A and 6 B slice tiles (128B swizzle)
-// and then the 21 x 4 tcgen05.mma (M=128, N=64, K=16, BF16 in, FP32 out);
-// every wait on an mbarrier is bounded and reports a timeout through an error
-// flag instead of spinning forever.
+// Kernel: persistent CTAs (128 threads, one per SM) walk the 128 x 64 output
+// tiles.  A K step of 32 is one pipeline stage: the 6 A and 6 B slice tiles
+// (TMA, 64-byte swizzle, 72 KiB); three stages are in flight.  One thread
+// issues the loads and the 21 x 2 tcgen05.mma (M=128, N=64, K=16, BF16 in,
+// FP32 out) per step, queueing step k's products before it waits for step
+// k-1's to free that stage for step k-1+3.  The next tile's first loads are
+// issued before the epilogue reads TMEM.  Every wait on an mbarrier is bounded
+// and reports a timeout through an error flag instead of spinning forever.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -34,10 +37,12 @@
 namespace hfgpu {
 
 constexpr int NSL = 6, SL_BITS = 7;
-constexpr int BM = 128, BN = 64, BK = 64;
-constexpr int A_TILE = BM * BK * 2;  // 16 KiB
-constexpr int B_TILE = BN * BK * 2;  // 8 KiB
-constexpr int SMEM_BYTES = NSL * (A_TILE + B_TILE) + 1024 + 64;
+constexpr int BM = 128, BN = 64, BK = 32;
+constexpr int STAGES = 3;
+constexpr int A_TILE = BM * BK * 2;  // 8 KiB
+constexpr int B_TILE = BN * BK * 2;  // 4 KiB
+constexpr int STAGE_BYTES = NSL * (A_TILE + B_TILE);  // 72 KiB: the 12 slice tiles of one K step
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 128;
 constexpr uint32_t TMEM_COLS = 512;  // 6 accumulators x 64 columns, rounded to a power of two
 constexpr int WAIT_SPINS = 1 << 22;
 
@@ -87,14 +92,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// K-major operand tile written by TMA with 128-byte swizzle: 8-row groups 1024 B apart
+// K-major operand tile written by TMA with 64-byte swizzle (rows of BK = 32
+// bf16): 8-row groups 512 B apart
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
 {
     uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
     d |= (uint64_t)1 << 16;              // leading byte offset (not used by swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
+    d |= (uint64_t)(512 >> 4) << 32;     // stride byte offset
     d |= (uint64_t)1 << 46;              // descriptor version
-    d |= (uint64_t)2 << 61;              // 128-byte swizzle
+    d |= (uint64_t)4 << 61;              // 64-byte swizzle
     return d;
 }
 
@@ -146,22 +152,23 @@ __global__ void __launch_bounds__(128, 1)
     sliced_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                        int64_t a_rows_pad, int b_rows_pad, int ksteps, const int* __restrict__ ea,
                        const int* __restrict__ eb, int64_t M, int N, double* out, OutMap om, int accumulate,
-                       int* err)
+                       int* err, int64_t ntiles, int ntn)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    unsigned char* sA = smem;                       // NSL tiles of BM x BK bf16
-    unsigned char* sB = smem + NSL * A_TILE;        // NSL tiles of BN x BK bf16
-    uint64_t* bars = (uint64_t*)(sB + NSL * B_TILE);  // [0] TMA, [1] MMA
-    uint32_t* tslot = (uint32_t*)(bars + 2);
+    uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);  // TMA landed, one per stage
+    uint64_t* empty = full + STAGES;                            // products of the stage done
+    uint32_t* tslot = (uint32_t*)(empty + STAGES);
+    __shared__ int s_ok;
+    auto sA = [&](int s, int t) { return smem + s * STAGE_BYTES + t * A_TILE; };
+    auto sB = [&](int s, int t) { return smem + s * STAGE_BYTES + NSL * A_TILE + t * B_TILE; };
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t m0 = (int64_t)blockIdx.x * BM;
-    const int n0 = blockIdx.y * BN;
-
     if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -174,78 +181,124 @@ __global__ void __launch_bounds__(128, 1)
     fence_after();
     const uint32_t tmem = *tslot;
 
-    bool ok = true;
-    int stuck = -1;  // barrier whose wait timed out
-    uint32_t phase = 0;
-    for (int ks = 0; ks < ksteps && ok; ++ks) {
-        if (threadIdx.x == 0) {
-            mbar_expect_tx(&bars[0], NSL * (A_TILE + B_TILE));
+    // thread 0's bookkeeping: the K step whose load is in flight on each stage
+    // (-1: none), and the last K step whose products were committed
+    int64_t pend[STAGES];
+    for (int s = 0; s < STAGES; ++s) pend[s] = -1;
+    int64_t last_commit = -1;
+    auto load = [&](int64_t g, int64_t m0, int n0, int ks) {
+        const int s = (int)(g % STAGES);
+        mbar_expect_tx(&full[s], STAGE_BYTES);
 #pragma unroll
-            for (int t = 0; t < NSL; ++t) {
-                tma_load_2d(sA + t * A_TILE, &tmA, ks * BK, (int)(t * a_rows_pad + m0), &bars[0]);
-                tma_load_2d(sB + t * B_TILE, &tmB, ks * BK, t * b_rows_pad + n0, &bars[0]);
-            }
+        for (int t = 0; t < NSL; ++t) {
+            tma_load_2d(sA(s, t), &tmA, ks * BK, (int)(t * a_rows_pad + m0), &full[s]);
+            tma_load_2d(sB(s, t), &tmB, ks * BK, t * b_rows_pad + n0, &full[s]);
         }
-        ok = mbar_wait(&bars[0], phase);
-        if (!ok) stuck = 0;
-        if (ok && threadIdx.x == 0) {
+        pend[s] = g;
+    };
+    const int pro = ksteps < STAGES ? ksteps : STAGES;
+
+    bool ok = true;
+    int64_t g0 = 0;  // K steps run by this CTA before the current tile
+    int64_t tile = blockIdx.x;
+    if (tile < ntiles && threadIdx.x == 0)
+        for (int ks = 0; ks < pro; ++ks) load(ks, (tile / ntn) * BM, (int)(tile % ntn) * BN, ks);
+    for (; tile < ntiles && ok; tile += gridDim.x) {
+        const int64_t m0 = (tile / ntn) * BM;
+        const int n0 = (int)(tile % ntn) * BN;
+        if (threadIdx.x == 0) {
+            // products of step ks are queued before waiting for those of step ks-1,
+            // whose stage is then refilled STAGES steps ahead
+            for (int ks = 0; ks < ksteps && ok; ++ks) {
+                const int64_t g = g0 + ks;
+                const int s = (int)(g % STAGES);
+                if (!mbar_wait(&full[s], (uint32_t)((g / STAGES) & 1))) {
+                    ok = false;
+                    break;
+                }
+                pend[s] = -1;
+                fence_after();
+#pragma unroll
+                for (int i = 0; i < NSL; ++i)
+#pragma unroll
+                    for (int j = 0; j < NSL - i; ++j) {
+                        const uint32_t dt = tmem + (uint32_t)((i + j) * BN);
+#pragma unroll
+                        for (int kk = 0; kk < BK / 16; ++kk) {
+                            const uint64_t ad = sdesc(su32(sA(s, i)) + kk * 32);
+                            const uint64_t bd = sdesc(su32(sB(s, j)) + kk * 32);
+                            // group t = i + j is first written by (i = 0, j = t) at ks = 0, kk = 0
+                            umma(dt, ad, bd, (ks == 0 && i == 0 && kk == 0) ? 0u : 1u);
+                        }
+                    }
+                umma_commit(&empty[s]);
+                last_commit = g;
+                if (ks >= 1 && ks - 1 + STAGES < ksteps) {
+                    const int64_t gp = g - 1;
+                    if (!mbar_wait(&empty[gp % STAGES], (uint32_t)((gp / STAGES) & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    load(gp + STAGES, m0, n0, ks - 1 + STAGES);
+                }
+            }
+            s_ok = ok;
+        }
+        __syncthreads();
+        ok = s_ok;
+        const int64_t glast = g0 + ksteps - 1;
+        if (ok) ok = mbar_wait(&empty[glast % STAGES], (uint32_t)((glast / STAGES) & 1));
+        ok = __syncthreads_and(ok);
+        // every stage is free again: start the next tile's loads before the epilogue
+        const int64_t next = tile + gridDim.x;
+        if (ok && threadIdx.x == 0 && next < ntiles)
+            for (int ks = 0; ks < pro; ++ks) load(glast + 1 + ks, (next / ntn) * BM, (int)(next % ntn) * BN, ks);
+        if (ok) {
             fence_after();
+            // epilogue: warp w owns TMEM lanes (rows) 32w .. 32w+31
+            // Every group sum is an integer-valued FP32 (sums of digit products), so the
+            // groups recombine exactly in int64: S = sum_t acc_t 2^{7(NSL-1-t)} < 2^59,
+            // and the value is S 2^{-7(NSL+1)} times the row and column scales.
+            const int64_t r = m0 + warp * 32 + lane;
+            const int er = (r < M) ? ea[r] : 0;
+            for (int c0 = 0; c0 < BN && n0 + c0 < N; c0 += 16) {
+                long long S[16];
 #pragma unroll
-            for (int i = 0; i < NSL; ++i)
+                for (int i = 0; i < 16; ++i) S[i] = 0;
 #pragma unroll
-                for (int j = 0; j < NSL - i; ++j) {
-                    const uint32_t dt = tmem + (uint32_t)((i + j) * BN);
+                for (int t = 0; t < NSL; ++t) {
+                    float f[16];
+                    tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(t * BN + c0), f);
 #pragma unroll
-                    for (int kk = 0; kk < BK / 16; ++kk) {
-                        const uint64_t ad = sdesc(su32(sA + i * A_TILE) + kk * 32);
-                        const uint64_t bd = sdesc(su32(sB + j * B_TILE) + kk * 32);
-                        // group t = i + j is first written by (i = 0, j = t) at ks = 0, kk = 0
-                        umma(dt, ad, bd, (ks == 0 && i == 0 && kk == 0) ? 0u : 1u);
+                    for (int i = 0; i < 16; ++i)  // |group sum| < 6 K 2^14 < 2^31 for K <= 512
+                        S[i] += (long long)__float2int_rn(f[i]) << (SL_BITS * (NSL - 1 - t));
+                }
+                if (r < M) {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int c = n0 + c0 + i;
+                        if (c < N) {
+                            const double x = (double)S[i] * pow2(er + eb[c] - SL_BITS * (NSL + 1));
+                            const int64_t o = out_index(om, r, c);
+                            out[o] = accumulate ? out[o] + x : x;
+                        }
                     }
                 }
-            umma_commit(&bars[1]);
+            }
         }
-        if (ok) {
-            ok = mbar_wait(&bars[1], phase);
-            if (!ok) stuck = 1;
-        }
-        if (ok) phase ^= 1;
+        // the epilogue's TMEM reads finish before the next tile's products overwrite it
+        fence_before();
         __syncthreads();
+        fence_after();
+        g0 += ksteps;
     }
     if (!ok) {
         if (lane == 0) atomicExch(err, 1);
-        // let the copies or products still in flight land before TMEM is freed (bounded)
-        mbar_wait(&bars[stuck], phase);
-    } else {
-        fence_after();
-        // epilogue: warp w owns TMEM lanes (rows) 32w .. 32w+31
-        // Every group sum is an integer-valued FP32 (sums of digit products), so the
-        // groups recombine exactly in int64: S = sum_t acc_t 2^{7(NSL-1-t)} < 2^59,
-        // and the value is S 2^{-7(NSL+1)} times the row and column scales.
-        const int64_t r = m0 + warp * 32 + lane;
-        const int er = (r < M) ? ea[r] : 0;
-        for (int c0 = 0; c0 < BN && n0 + c0 < N; c0 += 16) {
-            long long S[16];
-#pragma unroll
-            for (int i = 0; i < 16; ++i) S[i] = 0;
-#pragma unroll
-            for (int t = 0; t < NSL; ++t) {
-                float f[16];
-                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(t * BN + c0), f);
-#pragma unroll
-                for (int i = 0; i < 16; ++i) S[i] += __float2ll_rn(f[i]) << (SL_BITS * (NSL - 1 - t));
-            }
-            if (r < M) {
-#pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const int c = n0 + c0 + i;
-                    if (c < N) {
-                        const double x = (double)S[i] * pow2(er + eb[c] - SL_BITS * (NSL + 1));
-                        const int64_t o = out_index(om, r, c);
-                        out[o] = accumulate ? out[o] + x : x;
-                    }
-                }
-            }
+        if (threadIdx.x == 0) {
+            // let copies and products still in flight land before TMEM and shared memory go (bounded)
+            for (int s = 0; s < STAGES; ++s)
+                if (pend[s] >= 0) mbar_wait(&full[s], (uint32_t)((pend[s] / STAGES) & 1));
+            if (last_commit >= 0) mbar_wait(&empty[last_commit % STAGES], (uint32_t)((last_commit / STAGES) & 1));
         }
     }
     fence_before();
@@ -268,20 +321,23 @@ __device__ __forceinline__ void digits5(double x, int e, float (&d)[NSL])
         else if (sh > -63)
             Y = (m + (1ull << (-sh - 1))) >> (-sh);
     }
-    const float sgn = (bits >> 63) ? -1.0f : 1.0f;
+    // digits are < 2^7: convert from 32-bit integers (64-bit conversions run on
+    // the FP64 pipe) and set the sign bit directly
+    const uint32_t sgn = (uint32_t)(bits >> 63) << 31;
 #pragma unroll
     for (int t = 0; t < NSL; ++t) {
         const int shift = SL_BITS * (NSL - 1 - t);
-        const uint64_t dig = (t == 0) ? (Y >> shift) : ((Y >> shift) & ((1u << SL_BITS) - 1));
-        d[t] = sgn * (float)dig;
+        const uint32_t dig = (uint32_t)(Y >> shift) & (t == 0 ? 0xFFFFFFFFu : ((1u << SL_BITS) - 1));
+        d[t] = __uint_as_float(__float_as_uint((float)dig) | sgn);
     }
 }
 
-// row exponent: |x| < 2^e for every x in the row (0 for an all-zero row)
-__device__ __forceinline__ int row_exponent(double amax)
+// row exponent from the bits of the largest |x| of the row: |x| < 2^e for every
+// x in the row (0 for an all-zero row)
+__device__ __forceinline__ int row_exponent(uint64_t amax_bits)
 {
-    if (!(amax > 0)) return 0;
-    return (int)((((uint64_t)__double_as_longlong(amax)) >> 52) & 0x7FF) - 1022;
+    if (amax_bits == 0) return 0;
+    return (int)((amax_bits >> 52) & 0x7FF) - 1022;
 }
 
 // One warp per row.  Src::row(r) sets up the row once; element (r, k) is
@@ -296,15 +352,21 @@ __global__ void slice_kernel(Src src, int64_t rows, int K, int64_t rows_pad, int
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += nwarp) {
         const typename Src::Row row = src.row(r);
         double x[KMAX];
-        double amax = 0.0;
+        // the largest |x| as an integer compare of the magnitude bits (finite
+        // doubles order like their bit patterns), off the FP64 pipe
+        unsigned long long amax = 0;
 #pragma unroll
         for (int q = 0; q < KMAX; ++q) {
             const int k = lane + 32 * q;
             x[q] = (k < K) ? src.at(row, k) : 0.0;
-            amax = fmax(amax, fabs(x[q]));
+            const unsigned long long m = (unsigned long long)__double_as_longlong(x[q]) & 0x7FFFFFFFFFFFFFFFull;
+            amax = m > amax ? m : amax;
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long v = __shfl_xor_sync(0xffffffffu, amax, o);
+            amax = v > amax ? v : amax;
+        }
         const int e = row_exponent(amax);
         if (lane == 0) rexp[r] = e;
 #pragma unroll
@@ -401,7 +463,7 @@ static CUtensorMap make_map(const Sliced& s, int box_rows)
     cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
     cuuint32_t es[2] = {1, 1};
     CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)s.planes.p, dims, strides, box, es,
-                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     HF_CHECK(r == CUDA_SUCCESS, HFGPU_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
     return m;
@@ -466,11 +528,14 @@ void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, Ou
     HF_CUDA(cudaEventCreate(&e0));
     HF_CUDA(cudaEventCreate(&e1));
     HF_CUDA(cudaEventRecord(e0, ctx.stream));
-    dim3 grid((unsigned)(A.rows_pad / BM), (unsigned)(B.rows_pad / BN));
-    HF_CHECK(grid.x > 0 && grid.y > 0 && A.rows_pad / BM < 2147483647LL, HFGPU_ERR_INVALID, "sliced GEMM: grid");
+    // persistent CTAs, one per SM, walking the output tiles (column tile fastest)
+    const int ntn = (int)(B.rows_pad / BN);
+    const int64_t ntiles = (A.rows_pad / BM) * ntn;
+    HF_CHECK(ntiles > 0, HFGPU_ERR_INVALID, "sliced GEMM: empty");
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, ctx.num_sms);
     sliced_gemm_kernel<<<grid, 128, SMEM_BYTES, ctx.stream>>>(ta, tb, A.rows_pad, (int)B.rows_pad, A.K_pad / BK,
                                                                A.rexp.p, B.rexp.p, A.rows, (int)B.rows, out, om,
-                                                               accumulate ? 1 : 0, err.p);
+                                                               accumulate ? 1 : 0, err.p, ntiles, ntn);
     count_launch();
     HF_CUDA(cudaGetLastError());
     HF_CUDA(cudaEventRecord(e1, ctx.stream));
