@@ -196,10 +196,13 @@ __device__ bool sp2_grid_barrier(Sp2Sync* s, unsigned nblocks)
     return ok;
 }
 
-__global__ void __launch_bounds__(SQ_T* SQ_T) sp2_persistent_kernel(int n, int nocc, double* X, double* tr, int maxs,
-                                                                    Sp2Sync* sync)
+// T = double for the final steps; T = float for the coarse steps of early SCF
+// iterations (stop once tr(X - X^2) < tol_idem and |tr X - nocc| < tol_n).
+template <typename T>
+__global__ void __launch_bounds__(SQ_T* SQ_T) sp2_persistent_kernel(int n, int nocc, T* X, double* tr, int maxs,
+                                                                    double tol_idem, double tol_n, Sp2Sync* sync)
 {
-    __shared__ double As[SQ_T][SQ_T + 1], Bs[SQ_T][SQ_T + 1];
+    __shared__ T As[SQ_T][SQ_T + 1], Bs[SQ_T][SQ_T + 1];
     const int nt = (n + SQ_T - 1) / SQ_T;
     int b = blockIdx.x, ti = 0;
     while (b >= nt - ti) {
@@ -211,26 +214,26 @@ __global__ void __launch_bounds__(SQ_T* SQ_T) sp2_persistent_kernel(int n, int n
     const int i = ti * SQ_T + ty, j = tj * SQ_T + tx;
     const bool own = i < n && j < n;
     for (int it = 0; it < maxs; ++it) {
-        double acc = 0.0;
+        T acc = 0;
         for (int k0 = 0; k0 < n; k0 += SQ_T) {
             const int ka = k0 + tx, kb = k0 + ty;
-            As[ty][tx] = (i < n && ka < n) ? __ldcg(X + i + (int64_t)ka * n) : 0.0;
-            Bs[ty][tx] = (kb < n && j < n) ? __ldcg(X + kb + (int64_t)j * n) : 0.0;
+            As[ty][tx] = (i < n && ka < n) ? __ldcg(X + i + (int64_t)ka * n) : T(0);
+            Bs[ty][tx] = (kb < n && j < n) ? __ldcg(X + kb + (int64_t)j * n) : T(0);
             __syncthreads();
 #pragma unroll
             for (int k = 0; k < SQ_T; ++k) acc = fma(As[ty][k], Bs[k][tx], acc);
             __syncthreads();
         }
-        if (own && i == j) atomicAdd(tr + 2 * it + 1, acc);
+        if (own && i == j) atomicAdd(tr + 2 * it + 1, (double)acc);
         if (!sp2_grid_barrier(sync, gridDim.x)) return;
         const double t0 = __ldcg(tr + 2 * it), t1 = __ldcg(tr + 2 * it + 1);
         const bool square = fabs(t1 - nocc) <= fabs(2 * t0 - t1 - nocc);
-        const bool done = fabs(t0 - t1) < 1e-13 * n && fabs(t0 - nocc) < 1e-6;
+        const bool done = fabs(t0 - t1) < tol_idem && fabs(t0 - nocc) < tol_n;
         if (own) {
-            const double x = square ? acc : 2 * __ldcg(X + i + (int64_t)j * n) - acc;
+            const T x = square ? acc : T(2) * __ldcg(X + i + (int64_t)j * n) - acc;
             X[i + (int64_t)j * n] = x;
             if (ti != tj) X[j + (int64_t)i * n] = x;
-            if (i == j) atomicAdd(tr + 2 * it + 2, x);
+            if (i == j) atomicAdd(tr + 2 * it + 2, (double)x);
         }
         if (done) {
             if (blockIdx.x == 0 && threadIdx.x == 0) sync->steps = it + 1;
@@ -239,6 +242,17 @@ __global__ void __launch_bounds__(SQ_T* SQ_T) sp2_persistent_kernel(int n, int n
         if (!sp2_grid_barrier(sync, gridDim.x)) return;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) sync->steps = maxs;
+}
+
+// dst = src in another precision; tr0 += its trace
+template <typename S, typename D>
+__global__ void convert_trace_kernel(int n, const S* __restrict__ src, D* __restrict__ dst, double* tr0)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * n) return;
+    const D v = (D)src[idx];
+    dst[idx] = v;
+    if (idx % n == idx / n) atomicAdd(tr0, (double)v);
 }
 
 // X = (emax I - F) / (emax - emin): spectrum mapped into [0, 1], occupied states
@@ -273,7 +287,8 @@ static bool coop_ok(Context& ctx, unsigned blocks)
 {
     int coop = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx.device) != cudaSuccess || !coop) return false;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sp2_persistent_kernel, SQ_T * SQ_T, 0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sp2_persistent_kernel<double>, SQ_T * SQ_T, 0) !=
+        cudaSuccess)
         return false;
     return (int64_t)per_sm * ctx.num_sms >= (int64_t)blocks;
 }
@@ -281,6 +296,7 @@ static bool coop_ok(Context& ctx, unsigned blocks)
 struct Purifier {
     int n = 0, nocc = 0;
     DBuf<double> X, T1, T2, B, tr;  // orthogonaliser S^-1/2 and work
+    DBuf<float> Xf;                 // FP32 iterate of the coarse steps
     DBuf<Sp2Sync> sync;
     void setup(Context& ctx, int n_, int nocc_, const double* dS)
     {
@@ -313,8 +329,37 @@ struct Purifier {
         const double one = 1.0, zero = 0.0;
         HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, n, &one, T1.p, n, U.p, n, &zero, X.p, n));
     }
-    // P = 2 X proj(X F X) X: the closed-shell density of F without diagonalising it
-    void density(Context& ctx, const double* dF, double* dP)
+    // One cooperative launch of the whole recursion on the iterate Xs; h gets
+    // (tr X, tr X^2) of the last step.
+    template <typename T>
+    void run_persistent(Context& ctx, T* Xs, double* trs, int maxs, double tol_idem, double tol_n, unsigned tiles,
+                        double* h)
+    {
+        cudaStream_t st = ctx.stream;
+        if (!sync.p) sync.alloc(1, st);
+        HF_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(Sp2Sync), st));
+        int n_ = n, nocc_ = nocc;
+        Sp2Sync* sp = sync.p;
+        void* args[] = {&n_, &nocc_, &Xs, &trs, &maxs, &tol_idem, &tol_n, &sp};
+        HF_CUDA(cudaLaunchCooperativeKernel((const void*)sp2_persistent_kernel<T>, dim3(tiles), dim3(SQ_T * SQ_T),
+                                            args, 0, st));
+        count_launch();
+        Sp2Sync hs{};
+        std::vector<double> ht((size_t)2 * (maxs + 1));
+        HF_CUDA(cudaMemcpyAsync(&hs, sync.p, sizeof(Sp2Sync), cudaMemcpyDeviceToHost, st));
+        HF_CUDA(cudaMemcpyAsync(ht.data(), trs, sizeof(double) * ht.size(), cudaMemcpyDeviceToHost, st));
+        HF_CUDA(cudaStreamSynchronize(st));
+        HF_CHECK(hs.err == 0, HFGPU_ERR_CUDA, "density purification: grid barrier timed out");
+        const int last = std::max(hs.steps, 1) - 1;
+        h[0] = ht[2 * last];
+        h[1] = ht[2 * last + 1];
+    }
+    // P = 2 X proj(X F X) X: the closed-shell density of F without diagonalising it.
+    // coarse: run the recursion in FP32 until tr(X - X^2) < 1e-3, then finish in
+    // FP64 (a few steps); the result is idempotent to FP64 precision but its
+    // occupied subspace carries FP32 rounding (~1e-7), which is fine while the
+    // SCF is far from convergence.
+    void density(Context& ctx, const double* dF, double* dP, bool coarse = false)
     {
         const int64_t nn = (int64_t)n * n;
         cudaStream_t st = ctx.stream;
@@ -325,8 +370,8 @@ struct Purifier {
         count_launch();
         // per-step trace slots [step][tr X, tr X^2], zeroed once
         const int MAXS = 160, CHECK = 8;
-        if (tr.n < (size_t)2 * (MAXS + 1)) tr.alloc(2 * (MAXS + 1), st);
-        HF_CUDA(cudaMemsetAsync(tr.p, 0, sizeof(double) * 2 * (MAXS + 1), st));
+        if (tr.n < (size_t)4 * (MAXS + 1)) tr.alloc(4 * (MAXS + 1), st);
+        HF_CUDA(cudaMemsetAsync(tr.p, 0, sizeof(double) * 4 * (MAXS + 1), st));
         sp2_init2_kernel<<<nblk(nn), 256, 0, st>>>(n, T2.p, B.p, T1.p, tr.p);  // T1 = iterate
         count_launch();
         const int nt = (n + SQ_T - 1) / SQ_T;
@@ -334,26 +379,18 @@ struct Purifier {
         double h[2] = {0, 1};
         bool done = false;
         if (coop_ok(ctx, tiles)) {
-            // one cooperative launch for the whole recursion
-            if (!sync.p) sync.alloc(1, st);
-            HF_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(Sp2Sync), st));
-            int n_ = n, nocc_ = nocc, maxs = MAXS;
-            double* Xp = T1.p;
-            double* trp = tr.p;
-            Sp2Sync* sp = sync.p;
-            void* args[] = {&n_, &nocc_, &Xp, &trp, &maxs, &sp};
-            HF_CUDA(cudaLaunchCooperativeKernel((const void*)sp2_persistent_kernel, dim3(tiles), dim3(SQ_T * SQ_T),
-                                                args, 0, st));
-            count_launch();
-            Sp2Sync hs{};
-            std::vector<double> ht((size_t)2 * (MAXS + 1));
-            HF_CUDA(cudaMemcpyAsync(&hs, sync.p, sizeof(Sp2Sync), cudaMemcpyDeviceToHost, st));
-            HF_CUDA(cudaMemcpyAsync(ht.data(), tr.p, sizeof(double) * ht.size(), cudaMemcpyDeviceToHost, st));
-            HF_CUDA(cudaStreamSynchronize(st));
-            HF_CHECK(hs.err == 0, HFGPU_ERR_CUDA, "density purification: grid barrier timed out");
-            const int last = std::max(hs.steps, 1) - 1;
-            h[0] = ht[2 * last];
-            h[1] = ht[2 * last + 1];
+            double* tr64 = tr.p;
+            if (coarse) {
+                if (Xf.n < (size_t)nn) Xf.alloc(nn, st);
+                double* trf = tr.p + 2 * (MAXS + 1);
+                convert_trace_kernel<double, float><<<nblk(nn), 256, 0, st>>>(n, T1.p, Xf.p, trf);
+                count_launch();
+                run_persistent<float>(ctx, Xf.p, trf, MAXS, 1e-3, 1e-3, tiles, h);
+                HF_CUDA(cudaMemsetAsync(tr64, 0, sizeof(double) * 2 * (MAXS + 1), st));
+                convert_trace_kernel<float, double><<<nblk(nn), 256, 0, st>>>(n, Xf.p, T1.p, tr64);
+                count_launch();
+            }
+            run_persistent<double>(ctx, T1.p, tr64, MAXS, 1e-13 * n, 1e-6, tiles, h);
             done = true;
         }
         for (int it = 0; it < MAXS && !done; ++it) {
@@ -453,6 +490,7 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
     // iterations converge exactly like the full-build SCF
     int since_full = 0;
     bool last_full = true, endgame = false;
+    double last_dP = 1.0;
     for (int it = 1; it <= in.nscf; ++it) {
         const double* Gcur = G.p;
         if (inc) {
@@ -526,7 +564,8 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
         HF_CUDA(cudaMemcpyAsync(Pold.p, dP, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
         if (in.purify) {
             HF_CUDA(cudaMemcpyAsync(Fw.p, Fsolve, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
-            pur.density(ctx, Fw.p, dP);
+            // FP32 steps while the density is still far from converged
+            pur.density(ctx, Fw.p, dP, it > 1 && !endgame && last_dP > 1e-4);
             HF_CUDA(cudaMemsetAsync(info.p, 0, sizeof(int), st));
         } else {
             HF_CUDA(cudaMemcpyAsync(Fw.p, Fsolve, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
@@ -545,6 +584,7 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
                  "eigh: dsygvd returned info = " + std::to_string(hinfo) +
                      (hinfo > n ? " (S is not positive definite)" : ""));
         const double E0 = h[0], dPv = h[1];
+        last_dP = dPv;
         if (dPv < 100 * in.tolP) endgame = true;
         Escf.push_back(E0);
         out.E0 = E0;

@@ -307,8 +307,19 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // ------------------------------------------------------------------ slicing
-// digits of |x| * 2^(35 - e) (rounded), with the sign of x applied
-__device__ __forceinline__ void digits5(double x, int e, float (&d)[NSL])
+// bf16 bit pattern of sign * v for an integer 0 <= v <= 128 (exact: bf16 holds
+// 8 significant bits), built with integer operations only
+__device__ __forceinline__ uint16_t small_int_bf16(uint32_t v, uint32_t sign)
+{
+    if (v == 0) return (uint16_t)(sign << 15);
+    const int e = 31 - __clz(v);  // 2^e <= v < 2^(e+1), e <= 7
+    return (uint16_t)((sign << 15) | ((uint32_t)(127 + e) << 7) | ((v << (7 - e)) & 0x7Fu));
+}
+
+// digits of |x| * 2^(42 - e) (rounded), with the sign of x applied, as bf16
+// bit patterns: no floating-point instruction at all (GB300 runs 64-bit
+// conversions on its narrow FP64 pipe)
+__device__ __forceinline__ void digits_bf16(double x, int e, uint16_t (&d)[NSL])
 {
     const uint64_t bits = (uint64_t)__double_as_longlong(x);
     const int ex = (int)((bits >> 52) & 0x7FF);
@@ -321,14 +332,12 @@ __device__ __forceinline__ void digits5(double x, int e, float (&d)[NSL])
         else if (sh > -63)
             Y = (m + (1ull << (-sh - 1))) >> (-sh);
     }
-    // digits are < 2^7: convert from 32-bit integers (64-bit conversions run on
-    // the FP64 pipe) and set the sign bit directly
-    const uint32_t sgn = (uint32_t)(bits >> 63) << 31;
+    const uint32_t sgn = (uint32_t)(bits >> 63);
 #pragma unroll
     for (int t = 0; t < NSL; ++t) {
         const int shift = SL_BITS * (NSL - 1 - t);
         const uint32_t dig = (uint32_t)(Y >> shift) & (t == 0 ? 0xFFFFFFFFu : ((1u << SL_BITS) - 1));
-        d[t] = __uint_as_float(__float_as_uint((float)dig) | sgn);
+        d[t] = small_int_bf16(dig, sgn);
     }
 }
 
@@ -373,10 +382,11 @@ __global__ void slice_kernel(Src src, int64_t rows, int K, int64_t rows_pad, int
         for (int q = 0; q < KMAX; ++q) {
             const int k = lane + 32 * q;
             if (k < K) {
-                float d[NSL];
-                digits5(x[q], e, d);
+                uint16_t d[NSL];
+                digits_bf16(x[q], e, d);
+                uint16_t* pl = reinterpret_cast<uint16_t*>(planes);
 #pragma unroll
-                for (int t = 0; t < NSL; ++t) planes[((int64_t)t * rows_pad + r) * K_pad + k] = __float2bfloat16_rn(d[t]);
+                for (int t = 0; t < NSL; ++t) pl[((int64_t)t * rows_pad + r) * K_pad + k] = d[t];
             }
         }
     }
