@@ -116,6 +116,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         Basis b = build_basis(natoms, atno, xyz);  // validates the input before any device work
         Context& ctx = ctx_in ? *ctx_in : context();
         cudaStream_t st = ctx.stream;
+        ctx.settle_timers();  // drop timers a failed earlier call may have left
         ctx.stat_fock_ms = ctx.stat_tc_ms = ctx.stat_tc_flops = 0;
         ctx.tune = opt.autotune != 0 || tune_env_enabled();
         Timer total(st);
@@ -198,6 +199,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         if (lam) dL.download(lam, n);
         HF_CUDA(cudaStreamSynchronize(st));
         res->ms_total = total.ms();
+        ctx.settle_timers();
         res->ms_fock = ctx.stat_fock_ms;
         res->ms_tcgemm = ctx.stat_tc_ms;
         res->tc_flops = ctx.stat_tc_flops;

@@ -101,6 +101,19 @@ void Context::fork()
     for (int i = 0; i < NAUX; ++i) HF_CUDA(cudaStreamWaitEvent(aux[i], fork_ev, 0));
 }
 
+void Context::settle_timers()
+{
+    for (auto& e : fock_events) {
+        HF_CUDA(cudaEventSynchronize(e.second));
+        float ms = 0;
+        HF_CUDA(cudaEventElapsedTime(&ms, e.first, e.second));
+        stat_fock_ms += ms;
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+    }
+    fock_events.clear();
+}
+
 void Context::join()
 {
     for (int i = 0; i < NAUX; ++i) {

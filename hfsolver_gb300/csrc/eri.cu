@@ -564,12 +564,7 @@ void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG, double s
     count_launch();
     HF_CUDA(cudaGetLastError());
     HF_CUDA(cudaEventRecord(e1, ctx.stream));
-    HF_CUDA(cudaEventSynchronize(e1));
-    float ms = 0;
-    HF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    ctx.stat_fock_ms += ms;
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    ctx.fock_events.emplace_back(e0, e1);  // timed later, without a host wait here
 }
 EriStats eri_plan_stats(const EriPlan* p) { return p->stats; }
 

@@ -122,6 +122,10 @@ struct Context {
     cudaEvent_t fork_ev = nullptr, join_ev[NAUX] = {};
     void fork();  // aux streams wait for the work queued so far on `stream`
     void join();  // `stream` waits for the work queued on the aux streams
+    // event pairs around Fock builds, summed into stat_fock_ms by settle_timers()
+    // once the stream is synchronised anyway (no host wait per build)
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> fock_events;
+    void settle_timers();
     // kernel-time counters, reset by the pipeline entry points
     double stat_fock_ms = 0, stat_tc_ms = 0, stat_tc_flops = 0;
     bool tune = false;  // time candidate kernel shapes on first use (autotune.cpp)

@@ -331,28 +331,42 @@ struct Purifier {
     }
     // One cooperative launch of the whole recursion on the iterate Xs; h gets
     // (tr X, tr X^2) of the last step.
+    // One cooperative launch of the whole recursion on the iterate Xs, with
+    // barrier state slot `which` (0: FP32 steps, 1: FP64 steps).
     template <typename T>
     void run_persistent(Context& ctx, T* Xs, double* trs, int maxs, double tol_idem, double tol_n, unsigned tiles,
-                        double* h)
+                        int which)
     {
         cudaStream_t st = ctx.stream;
-        if (!sync.p) sync.alloc(1, st);
-        HF_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(Sp2Sync), st));
+        HF_CUDA(cudaMemsetAsync(sync.p + which, 0, sizeof(Sp2Sync), st));
         int n_ = n, nocc_ = nocc;
-        Sp2Sync* sp = sync.p;
+        Sp2Sync* sp = sync.p + which;
         void* args[] = {&n_, &nocc_, &Xs, &trs, &maxs, &tol_idem, &tol_n, &sp};
         HF_CUDA(cudaLaunchCooperativeKernel((const void*)sp2_persistent_kernel<T>, dim3(tiles), dim3(SQ_T * SQ_T),
                                             args, 0, st));
         count_launch();
-        Sp2Sync hs{};
-        std::vector<double> ht((size_t)2 * (maxs + 1));
-        HF_CUDA(cudaMemcpyAsync(&hs, sync.p, sizeof(Sp2Sync), cudaMemcpyDeviceToHost, st));
-        HF_CUDA(cudaMemcpyAsync(ht.data(), trs, sizeof(double) * ht.size(), cudaMemcpyDeviceToHost, st));
-        HF_CUDA(cudaStreamSynchronize(st));
-        HF_CHECK(hs.err == 0, HFGPU_ERR_CUDA, "density purification: grid barrier timed out");
-        const int last = std::max(hs.steps, 1) - 1;
-        h[0] = ht[2 * last];
-        h[1] = ht[2 * last + 1];
+    }
+    // The outcome of the last cooperative purification (barrier timeouts, final
+    // trace) is copied to pinned host memory without waiting; check() reads it
+    // after the caller's next synchronisation.
+    Sp2Sync* hsync = nullptr;
+    double* htr = nullptr;
+    bool pending = false;
+    static constexpr int MAXS = 160;
+    void check()
+    {
+        if (!pending) return;
+        pending = false;
+        HF_CHECK(hsync[0].err == 0 && hsync[1].err == 0, HFGPU_ERR_CUDA,
+                 "density purification: grid barrier timed out");
+        const int last = std::max(hsync[1].steps, 1) - 1;
+        HF_CHECK(fabs(htr[2 * last] - nocc) < 1e-6, HFGPU_ERR_LINALG,
+                 "density purification did not converge (no gap?)");
+    }
+    ~Purifier()
+    {
+        if (hsync) cudaFreeHost(hsync);
+        if (htr) cudaFreeHost(htr);
     }
     // P = 2 X proj(X F X) X: the closed-shell density of F without diagonalising it.
     // coarse: run the recursion in FP32 until tr(X - X^2) < 1e-3, then finish in
@@ -369,7 +383,7 @@ struct Purifier {
         gersh_kernel<<<1, 256, 0, st>>>(n, T2.p, B.p);
         count_launch();
         // per-step trace slots [step][tr X, tr X^2], zeroed once
-        const int MAXS = 160, CHECK = 8;
+        const int CHECK = 8;
         if (tr.n < (size_t)4 * (MAXS + 1)) tr.alloc(4 * (MAXS + 1), st);
         HF_CUDA(cudaMemsetAsync(tr.p, 0, sizeof(double) * 4 * (MAXS + 1), st));
         sp2_init2_kernel<<<nblk(nn), 256, 0, st>>>(n, T2.p, B.p, T1.p, tr.p);  // T1 = iterate
@@ -379,19 +393,31 @@ struct Purifier {
         double h[2] = {0, 1};
         bool done = false;
         if (coop_ok(ctx, tiles)) {
+            if (!sync.p) {
+                sync.alloc(2, st);
+                HF_CUDA(cudaMemsetAsync(sync.p, 0, 2 * sizeof(Sp2Sync), st));
+                HF_CUDA(cudaMallocHost((void**)&hsync, 2 * sizeof(Sp2Sync)));
+                HF_CUDA(cudaMallocHost((void**)&htr, 2 * (MAXS + 1) * sizeof(double)));
+            }
             double* tr64 = tr.p;
             if (coarse) {
                 if (Xf.n < (size_t)nn) Xf.alloc(nn, st);
                 double* trf = tr.p + 2 * (MAXS + 1);
                 convert_trace_kernel<double, float><<<nblk(nn), 256, 0, st>>>(n, T1.p, Xf.p, trf);
                 count_launch();
-                run_persistent<float>(ctx, Xf.p, trf, MAXS, 1e-3, 1e-3, tiles, h);
+                run_persistent<float>(ctx, Xf.p, trf, MAXS, 1e-3, 1e-3, tiles, 0);
                 HF_CUDA(cudaMemsetAsync(tr64, 0, sizeof(double) * 2 * (MAXS + 1), st));
                 convert_trace_kernel<float, double><<<nblk(nn), 256, 0, st>>>(n, Xf.p, T1.p, tr64);
                 count_launch();
+            } else {
+                HF_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(Sp2Sync), st));  // no FP32 phase this time
             }
-            run_persistent<double>(ctx, T1.p, tr64, MAXS, 1e-13 * n, 1e-6, tiles, h);
+            run_persistent<double>(ctx, T1.p, tr64, MAXS, 1e-13 * n, 1e-6, tiles, 1);
+            HF_CUDA(cudaMemcpyAsync(hsync, sync.p, 2 * sizeof(Sp2Sync), cudaMemcpyDeviceToHost, st));
+            HF_CUDA(cudaMemcpyAsync(htr, tr64, 2 * (MAXS + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+            pending = true;
             done = true;
+            h[0] = nocc;  // checked later by check()
         }
         for (int it = 0; it < MAXS && !done; ++it) {
             sym_square_kernel<<<tiles, SQ_T * SQ_T, 0, st>>>(n, T1.p, T2.p, tr.p + 2 * it + 1);
@@ -580,6 +606,7 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
         scal.download(h, 2);
         info.download(&hinfo, 1);
         HF_CUDA(cudaStreamSynchronize(st));
+        if (in.purify) pur.check();
         HF_CHECK(hinfo == 0, HFGPU_ERR_LINALG,
                  "eigh: dsygvd returned info = " + std::to_string(hinfo) +
                      (hinfo > n ? " (S is not positive definite)" : ""));
