@@ -117,7 +117,7 @@ struct Context {
     int num_sms = 0;
     // side streams for independent launches (quartet classes), joined back to
     // `stream` by events
-    static constexpr int NAUX = 4;
+    static constexpr int NAUX = 8;
     cudaStream_t aux[NAUX] = {};
     cudaEvent_t fork_ev = nullptr, join_ev[NAUX] = {};
     void fork();  // aux streams wait for the work queued so far on `stream`

@@ -6,7 +6,9 @@
 //   T_ab from overlaps with the ket power raised/lowered by 2 (the same
 //        kinetic formula as cints.c:186-210)
 //   V_ab = -sum_C Z_C sum c_a c_b K_ab (2 pi/p) sum_tuv E^{ab}_{tuv} R_tuv(p, P-C)
-// One thread per matrix element (i, j); n x n column-major like the reference.
+// One thread per matrix element (i, j) and chunk of nuclei; n x n column-major like
+// the reference.
+#include <algorithm>
 #include <vector>
 
 #include "boys.cuh"
@@ -78,6 +80,10 @@ __device__ static void r_aux(int L, double (&R)[OE_L + 1][nherm(OE_L)], const do
                 }
 }
 
+// blockIdx.y = a chunk of ONEE_ATOMS nuclei: chunk 0 also writes S and T; every
+// chunk adds its nuclei's attraction to V (zeroed by the caller) atomically.
+constexpr int ONEE_ATOMS = 4;
+
 __global__ void onee_kernel(FnDev f, int n, int nat, const int* __restrict__ Z, const double* __restrict__ C,
                             const double* __restrict__ boys, double* S, double* T, double* V)
 {
@@ -119,9 +125,10 @@ __global__ void onee_kernel(FnDev f, int n, int nat, const int* __restrict__ Z, 
             if (n2 >= 2) t2 += n2 * (n2 - 1) * sx * sy * Ez[n1][n2 - 2][0];
             s_acc += pre * s0;
             t_acc += pre * (t0 + t1 - 0.5 * t2);
-            // nuclear attraction
+            // nuclear attraction of this block's nuclei
             double vsum = 0;
-            for (int c = 0; c < nat; ++c) {
+            const int c0 = blockIdx.y * ONEE_ATOMS, c1 = min(nat, c0 + ONEE_ATOMS);
+            for (int c = c0; c < c1; ++c) {
                 double X = px - C[3 * c], Y = py - C[3 * c + 1], Zc = pz - C[3 * c + 2];
                 double F[OE_L + 1];
                 const double Tc = p * (X * X + Y * Y + Zc * Zc);
@@ -145,9 +152,14 @@ __global__ void onee_kernel(FnDev f, int n, int nat, const int* __restrict__ Z, 
             v_acc += cc * K * 2 * PI * ip * vsum;
         }
     const int64_t o1 = i + (int64_t)j * n, o2 = j + (int64_t)i * n;
-    if (S) S[o1] = S[o2] = s_acc;
-    if (T) T[o1] = T[o2] = t_acc;
-    if (V) V[o1] = V[o2] = v_acc;
+    if (blockIdx.y == 0) {
+        if (S) S[o1] = S[o2] = s_acc;
+        if (T) T[o1] = T[o2] = t_acc;
+    }
+    if (V && v_acc != 0.0) {
+        atomicAdd(V + o1, v_acc);
+        if (o2 != o1) atomicAdd(V + o2, v_acc);
+    }
 }
 
 void onee_compute(Context& ctx, const Basis& b, int nat, const int* atno, const double* x, const double* y,
@@ -185,8 +197,9 @@ void onee_compute(Context& ctx, const Basis& b, int nat, const int* atno, const 
     auto dC = to_device(C, st);
     FnDev f{dl.p, dn.p, da.p, dc.p, dx.p, dal.p, dco.p};
     const int64_t npair = (int64_t)n * (n + 1) / 2;
-    const int blocks = (int)((npair + 127) / 128);
-    onee_kernel<<<blocks, 128, 0, st>>>(f, n, nat, dZ.p, dC.p, ctx.boys, dS, dT, dV);
+    if (dV) HF_CUDA(cudaMemsetAsync(dV, 0, sizeof(double) * n * n, st));
+    const dim3 grid((unsigned)((npair + 127) / 128), (unsigned)std::max(1, (nat + ONEE_ATOMS - 1) / ONEE_ATOMS));
+    onee_kernel<<<grid, 128, 0, st>>>(f, n, nat, dZ.p, dC.p, ctx.boys, dS, dT, dV);
     count_launch();
     HF_CUDA(cudaGetLastError());
     HF_CUDA(cudaStreamSynchronize(st));

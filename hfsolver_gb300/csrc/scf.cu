@@ -85,40 +85,44 @@ static void reduce(Context& ctx, int mode, int64_t nn, const double* A, const do
 static unsigned nblk(int64_t n) { return (unsigned)((n + 255) / 256); }
 
 // ---- density by purification (SP2, Niklasson, Phys. Rev. B 66, 155115 (2002)) ----
-// Gershgorin bounds of a symmetric matrix: b[0] <= lowest, b[1] >= highest eigenvalue
+// Gershgorin bounds of a symmetric matrix: b[0] <= lowest, b[1] >= highest eigenvalue.
+// One warp per column (the matrix is symmetric, so column sums are row sums):
+// coalesced reads, shuffle sums.
 __global__ void gersh_kernel(int n, const double* __restrict__ A, double* b)
 {
-    __shared__ double lo[256], hi[256];
+    __shared__ double lo[32], hi[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     double l = 1e300, h = -1e300;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = warp; i < n; i += nw) {
+        const double* col = A + (int64_t)i * n;
         double r = 0;
-        for (int j = 0; j < n; ++j)
-            if (j != i) r += fabs(A[i + (int64_t)j * n]);
-        const double d = A[i + (int64_t)i * n];
+        for (int j = lane; j < n; j += 32)
+            if (j != i) r += fabs(col[j]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+        const double d = col[i];
         l = fmin(l, d - r);
         h = fmax(h, d + r);
     }
-    lo[threadIdx.x] = l;
-    hi[threadIdx.x] = h;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) {
-            lo[threadIdx.x] = fmin(lo[threadIdx.x], lo[threadIdx.x + o]);
-            hi[threadIdx.x] = fmax(hi[threadIdx.x], hi[threadIdx.x + o]);
-        }
-        __syncthreads();
+    if (lane == 0) {
+        lo[warp] = l;
+        hi[warp] = h;
     }
+    __syncthreads();
     if (threadIdx.x == 0) {
-        b[0] = lo[0];
-        b[1] = hi[0];
+        for (int w = 1; w < nw; ++w) {
+            l = fmin(l, lo[w]);
+            h = fmax(h, hi[w]);
+        }
+        b[0] = l;
+        b[1] = h;
     }
 }
 
-__global__ void scale_cols_kernel(int n, const double* __restrict__ U, const double* __restrict__ w, double* V)
+__global__ void identity_kernel(int n, double* X)
 {
-    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)n * n) return;
-    V[idx] = U[idx] / sqrt(w[idx / n]);
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < (int64_t)n * n) X[idx] = (idx % n == idx / n) ? 1.0 : 0.0;
 }
 
 // X2 = X X for symmetric X (n <= 1024), upper-triangle 16x16 tiles mirrored;
@@ -309,28 +313,26 @@ struct Purifier {
         T2.alloc(nn, st);
         B.alloc(4, st);
         tr.alloc(4, st);
-        DBuf<double> U(nn, st), w(n, st);
+        // orthogonaliser X = L^-T from the Cholesky factor S = L L^T (X^T S X = I):
+        // a factorisation and a triangular solve instead of an eigensolve
+        DBuf<double> L(nn, st);
         DBuf<int> info(1, st);
-        HF_CUDA(cudaMemcpyAsync(U.p, dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+        HF_CUDA(cudaMemcpyAsync(L.p, dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
         int lwork = 0;
-        HF_CUSOLVER(cusolverDnDsyevd_bufferSize(ctx.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, U.p,
-                                                n, w.p, &lwork));
+        HF_CUSOLVER(cusolverDnDpotrf_bufferSize(ctx.solver, CUBLAS_FILL_MODE_LOWER, n, L.p, n, &lwork));
         DBuf<double> work(std::max(lwork, 1), st);
-        HF_CUSOLVER(cusolverDnDsyevd(ctx.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, U.p, n, w.p,
-                                     work.p, lwork, info.p));
-        std::vector<double> hw(n);
+        HF_CUSOLVER(cusolverDnDpotrf(ctx.solver, CUBLAS_FILL_MODE_LOWER, n, L.p, n, work.p, lwork, info.p));
         int hinfo = 0;
-        w.download(hw.data(), n);
         info.download(&hinfo, 1);
         HF_CUDA(cudaStreamSynchronize(st));
-        HF_CHECK(hinfo == 0 && hw[0] > 0, HFGPU_ERR_LINALG, "S is not positive definite");
-        scale_cols_kernel<<<nblk(nn), 256, 0, st>>>(n, U.p, w.p, T1.p);  // U w^-1/2
+        HF_CHECK(hinfo == 0, HFGPU_ERR_LINALG, "S is not positive definite");
+        identity_kernel<<<nblk(nn), 256, 0, st>>>(n, X.p);
         count_launch();
-        const double one = 1.0, zero = 0.0;
-        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, n, &one, T1.p, n, U.p, n, &zero, X.p, n));
+        const double one = 1.0;
+        // L^T X = I
+        HF_CUBLAS(cublasDtrsm(ctx.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n,
+                              n, &one, L.p, n, X.p, n));
     }
-    // One cooperative launch of the whole recursion on the iterate Xs; h gets
-    // (tr X, tr X^2) of the last step.
     // One cooperative launch of the whole recursion on the iterate Xs, with
     // barrier state slot `which` (0: FP32 steps, 1: FP64 steps).
     template <typename T>
@@ -368,7 +370,7 @@ struct Purifier {
         if (hsync) cudaFreeHost(hsync);
         if (htr) cudaFreeHost(htr);
     }
-    // P = 2 X proj(X F X) X: the closed-shell density of F without diagonalising it.
+    // P = 2 X proj(X^T F X) X^T: the closed-shell density of F without diagonalising it.
     // coarse: run the recursion in FP32 until tr(X - X^2) < 1e-3, then finish in
     // FP64 (a few steps); the result is idempotent to FP64 precision but its
     // occupied subspace carries FP32 rounding (~1e-7), which is fine while the
@@ -378,9 +380,9 @@ struct Purifier {
         const int64_t nn = (int64_t)n * n;
         cudaStream_t st = ctx.stream;
         const double one = 1.0, zero = 0.0, two = 2.0;
-        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, X.p, n, dF, n, &zero, T1.p, n));
+        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, X.p, n, dF, n, &zero, T1.p, n));
         HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, T1.p, n, X.p, n, &zero, T2.p, n));
-        gersh_kernel<<<1, 256, 0, st>>>(n, T2.p, B.p);
+        gersh_kernel<<<1, 1024, 0, st>>>(n, T2.p, B.p);
         count_launch();
         // per-step trace slots [step][tr X, tr X^2], zeroed once
         const int CHECK = 8;
@@ -433,7 +435,7 @@ struct Purifier {
         }
         HF_CHECK(fabs(h[0] - nocc) < 1e-6, HFGPU_ERR_LINALG, "density purification did not converge (no gap?)");
         HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, X.p, n, T1.p, n, &zero, T2.p, n));
-        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &two, T2.p, n, X.p, n, &zero, dP, n));
+        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, n, &two, T2.p, n, X.p, n, &zero, dP, n));
     }
 };
 
