@@ -58,8 +58,8 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
     DBuf<double> Y((size_t)std::min(pb, npair) * n1 * n, st);
     for (int64_t p0 = 0; p0 < npair; p0 += pb) {
         const int64_t np = std::min(pb, npair - p0);
-        slice_packed(ctx, d_int2, pairs.p, p0, np, n, A);
-        sliced_gemm(ctx, A, B1, Y.p, OutMap{n, n1}, false);  // rows (p, la) -> Y[p][j][la]
+        // rows (p, la) -> Y[p][j][la], the ERIs sliced inside the GEMM
+        sliced_gemm_packed(ctx, d_int2, pairs.p, p0, np, n, B1, Y.p, OutMap{n, n1});
         slice_dense(ctx, Y.p, np * n1, n, n, A, SLICE_TILE_A);
         sliced_gemm(ctx, A, B2, Z.p + p0 * nq, OutMap{0, n2}, false);  // rows (p, j) -> Z[p][j][b]
     }
@@ -78,9 +78,8 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
     DBuf<double> W((size_t)std::min(qb, nq) * n1 * n, st);
     for (int64_t q0 = 0; q0 < nq; q0 += qb) {
         const int64_t nqb = std::min(qb, nq - q0);
-        // rows (q, mu) over nu of Zt[q0 + q][pair(mu, nu)]
-        slice_sympair(ctx, Zt.p + q0 * npair, npair, nqb, n, A);
-        sliced_gemm(ctx, A, B1, W.p, OutMap{n, n1}, false);  // rows (q, mu) -> W[q][i][mu]
+        // rows (q, mu) over nu of Zt[q0 + q][pair(mu, nu)] -> W[q][i][mu], sliced inside the GEMM
+        sliced_gemm_sympair(ctx, Zt.p + q0 * npair, npair, nqb, n, B1, W.p, OutMap{n, n1});
         slice_dense(ctx, W.p, nqb * n1, n, n, A, SLICE_TILE_A);
         sliced_gemm(ctx, A, B2, T + q0 * n1 * n2, OutMap{0, n2}, false);  // rows (q, i) -> T[q][i][a]
     }

@@ -444,6 +444,199 @@ struct SymPairRows {  // rows (q, mu), k = nu of Zt[q * ldz + pair(mu, nu)] (Z t
     }
 };
 
+// ------------------------------------------------------------------ gather-fed GEMM
+// The same product with the A operand sliced on the fly: instead of writing six
+// bf16 planes of A to HBM and reading them back through TMA, the CTA's threads
+// gather A's FP64 elements (Src::row / Src::at), cut them into digits and store
+// them straight into the stage's shared-memory tiles in the 64-byte-swizzled
+// K-major layout the MMA reads (16-byte chunk c of row r at chunk c ^ ((r >> 1) & 3)).
+// B still arrives by TMA.  The row exponents come from row_exp_kernel.
+// 256 threads: thread t produces row t % 128, K half t / 128 of every stage;
+// thread 0 also issues the B loads and the products; all 8 warps share the
+// epilogue (warp w: TMEM lanes 32 (w % 4), columns half w / 4).
+constexpr int GATHER_THREADS = 256;
+
+template <class Src>
+__global__ void row_exp_kernel(Src src, int64_t rows, int K, int* __restrict__ rexp)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += nwarp) {
+        const typename Src::Row row = src.row(r);
+        unsigned long long amax = 0;
+        for (int k = lane; k < K; k += 32) {
+            const unsigned long long m = (unsigned long long)__double_as_longlong(src.at(row, k)) & 0x7FFFFFFFFFFFFFFFull;
+            amax = m > amax ? m : amax;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long v = __shfl_xor_sync(0xffffffffu, amax, o);
+            amax = v > amax ? v : amax;
+        }
+        if (lane == 0) rexp[r] = row_exponent(amax);
+    }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
+}
+
+template <class Src>
+__global__ void __launch_bounds__(GATHER_THREADS, 1)
+    sliced_gemm_gather_kernel(Src src, const int* __restrict__ ea, const __grid_constant__ CUtensorMap tmB,
+                              int b_rows_pad, int K, int ksteps, const int* __restrict__ eb, int64_t M, int N,
+                              double* out, OutMap om, int* err, int64_t ntiles, int ntn)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+    uint64_t* empty = full + STAGES;
+    uint32_t* tslot = (uint32_t*)(empty + STAGES);
+    __shared__ int s_ok;
+    auto sA = [&](int s, int t) { return smem + s * STAGE_BYTES + t * A_TILE; };
+    auto sB = [&](int s, int t) { return smem + s * STAGE_BYTES + NSL * A_TILE + t * B_TILE; };
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int prow = tid & (BM - 1), half = tid / BM;
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], GATHER_THREADS + 1);  // every producer + the B expect_tx
+            mbar_init(&empty[s], 1);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_ok = 1;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tslot)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+
+    bool ok = true;
+    int64_t g0 = 0;
+    int64_t last_commit = -1;  // thread 0
+    int64_t pend_b = -1;       // thread 0: last step whose B load was issued
+    for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int64_t m0 = (tile / ntn) * BM;
+        const int n0 = (int)(tile % ntn) * BN;
+        const int64_t R = m0 + prow;
+        const bool live = R < M;
+        const typename Src::Row row = src.row(live ? R : 0);
+        const int e = live ? ea[R] : 0;
+        for (int ks = 0; ks < ksteps && ok; ++ks) {
+            const int64_t g = g0 + ks;
+            const int s = (int)(g % STAGES);
+            if (g >= STAGES && !mbar_wait(&empty[s], (uint32_t)(((g - STAGES) / STAGES) & 1))) {
+                ok = false;
+                break;
+            }
+            if (tid == 0) {
+                mbar_expect_tx(&full[s], NSL * B_TILE);
+#pragma unroll
+                for (int t = 0; t < NSL; ++t) tma_load_2d(sB(s, t), &tmB, ks * BK, t * b_rows_pad + n0, &full[s]);
+                pend_b = g;
+            }
+            // 16 elements of this thread's row -> 2 swizzled 16-byte chunks per plane
+            uint32_t w[NSL][8];
+#pragma unroll
+            for (int j = 0; j < 16; j += 2) {
+                const int k = ks * BK + half * 16 + j;
+                const double x0 = (live && k < K) ? src.at(row, k) : 0.0;
+                const double x1 = (live && k + 1 < K) ? src.at(row, k + 1) : 0.0;
+                uint16_t d0[NSL], d1[NSL];
+                digits_bf16(x0, e, d0);
+                digits_bf16(x1, e, d1);
+#pragma unroll
+                for (int t = 0; t < NSL; ++t) w[t][j / 2] = (uint32_t)d0[t] | ((uint32_t)d1[t] << 16);
+            }
+            const int sw = (prow >> 1) & 3;
+#pragma unroll
+            for (int t = 0; t < NSL; ++t)
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int c = (half * 2 + q) ^ sw;
+                    uint4 v = make_uint4(w[t][4 * q], w[t][4 * q + 1], w[t][4 * q + 2], w[t][4 * q + 3]);
+                    *reinterpret_cast<uint4*>(sA(s, t) + prow * 64 + c * 16) = v;
+                }
+            // the tensor core reads shared memory through the async proxy
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(&full[s]);
+            if (tid == 0) {
+                if (!mbar_wait(&full[s], (uint32_t)((g / STAGES) & 1))) {
+                    ok = false;
+                    break;
+                }
+                fence_after();
+#pragma unroll
+                for (int i = 0; i < NSL; ++i)
+#pragma unroll
+                    for (int jj = 0; jj < NSL - i; ++jj) {
+                        const uint32_t dt = tmem + (uint32_t)((i + jj) * BN);
+#pragma unroll
+                        for (int kk = 0; kk < BK / 16; ++kk) {
+                            const uint64_t ad = sdesc(su32(sA(s, i)) + kk * 32);
+                            const uint64_t bd = sdesc(su32(sB(s, jj)) + kk * 32);
+                            umma(dt, ad, bd, (ks == 0 && i == 0 && kk == 0) ? 0u : 1u);
+                        }
+                    }
+                umma_commit(&empty[s]);
+                last_commit = g;
+            }
+        }
+        if (!ok) atomicExch(&s_ok, 0);
+        __syncthreads();
+        ok = s_ok != 0;
+        const int64_t glast = g0 + ksteps - 1;
+        if (ok) ok = mbar_wait(&empty[glast % STAGES], (uint32_t)((glast / STAGES) & 1));
+        ok = __syncthreads_and(ok);
+        if (ok) {
+            fence_after();
+            const int64_t r = m0 + (warp & 3) * 32 + lane;
+            const int er = (r < M) ? ea[r] : 0;
+            const int cbeg = (warp >> 2) * (BN / 2);
+            for (int c0 = cbeg; c0 < cbeg + BN / 2 && n0 + c0 < N; c0 += 16) {
+                long long S[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) S[i] = 0;
+#pragma unroll
+                for (int t = 0; t < NSL; ++t) {
+                    float f[16];
+                    tmem_ld16(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(t * BN + c0), f);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) S[i] += (long long)__float2int_rn(f[i]) << (SL_BITS * (NSL - 1 - t));
+                }
+                if (r < M) {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int c = n0 + c0 + i;
+                        if (c < N) out[out_index(om, r, c)] = (double)S[i] * pow2(er + eb[c] - SL_BITS * (NSL + 1));
+                    }
+                }
+            }
+        }
+        fence_before();
+        __syncthreads();
+        fence_after();
+        g0 += ksteps;
+    }
+    if (!ok) {
+        if (lane == 0) atomicExch(err, 1);
+        if (tid == 0) {
+            // B copies and products still in flight land before shared memory and TMEM go (bounded)
+            if (pend_b >= 0) mbar_wait(&full[pend_b % STAGES], (uint32_t)((pend_b / STAGES) & 1));
+            if (last_commit >= 0) mbar_wait(&empty[last_commit % STAGES], (uint32_t)((last_commit / STAGES) & 1));
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+}
+
 // ------------------------------------------------------------------ host side
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -559,6 +752,69 @@ void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, Ou
     ctx.stat_tc_ms += ms;
     ctx.stat_tc_flops += 2.0 * (NSL * (NSL + 1) / 2) * (double)A.rows * (double)B.rows * (double)A.K;
     HF_CHECK(h == 0, HFGPU_ERR_CUDA, "sliced GEMM: an mbarrier wait timed out");
+}
+
+}  // namespace hfgpu
+
+namespace hfgpu {
+
+template <class Src>
+static void gather_gemm(Context& ctx, const Src& src, int64_t M, int K, const Sliced& B, double* out, OutMap om)
+{
+    HF_CHECK(K == B.K, HFGPU_ERR_INVALID, "gather GEMM: K mismatch");
+    HF_CHECK(B.rows_pad % BN == 0, HFGPU_ERR_INVALID, "gather GEMM: padding");
+    static bool attr = false;
+    if (!attr) {
+        HF_CUDA(cudaFuncSetAttribute(sliced_gemm_gather_kernel<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     SMEM_BYTES));
+        attr = true;
+    }
+    DBuf<int> rexp((size_t)std::max<int64_t>(M, 1), ctx.stream);
+    {
+        const int64_t warps = std::min<int64_t>(M, (int64_t)ctx.num_sms * 64);
+        row_exp_kernel<Src><<<(unsigned)std::max<int64_t>(1, (warps * 32 + 255) / 256), 256, 0, ctx.stream>>>(
+            src, M, K, rexp.p);
+        count_launch();
+        HF_CUDA(cudaGetLastError());
+    }
+    const CUtensorMap tb = make_map(B, BN);
+    DBuf<int> err(1, ctx.stream);
+    err.zero();
+    cudaEvent_t e0, e1;
+    HF_CUDA(cudaEventCreate(&e0));
+    HF_CUDA(cudaEventCreate(&e1));
+    HF_CUDA(cudaEventRecord(e0, ctx.stream));
+    const int ntn = (int)(B.rows_pad / BN);
+    const int64_t ntiles = (M + BM - 1) / BM * ntn;
+    HF_CHECK(ntiles > 0, HFGPU_ERR_INVALID, "gather GEMM: empty");
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, ctx.num_sms);
+    sliced_gemm_gather_kernel<Src><<<grid, GATHER_THREADS, SMEM_BYTES, ctx.stream>>>(
+        src, rexp.p, tb, (int)B.rows_pad, K, B.K_pad / BK, B.rexp.p, M, (int)B.rows, out, om, err.p, ntiles, ntn);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+    HF_CUDA(cudaEventRecord(e1, ctx.stream));
+    int h = 0;
+    err.download(&h, 1);
+    HF_CUDA(cudaStreamSynchronize(ctx.stream));
+    float ms = 0;
+    HF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx.stat_tc_ms += ms;
+    ctx.stat_tc_flops += 2.0 * (NSL * (NSL + 1) / 2) * (double)M * (double)B.rows * (double)K;
+    HF_CHECK(h == 0, HFGPU_ERR_CUDA, "gather GEMM: an mbarrier wait timed out");
+}
+
+void sliced_gemm_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n,
+                        const Sliced& B, double* out, OutMap om)
+{
+    gather_gemm(ctx, PackedRows{ints, pairs, p0, n}, npairs * n, n, B, out, om);
+}
+
+void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, const Sliced& B,
+                         double* out, OutMap om)
+{
+    gather_gemm(ctx, SymPairRows{Zt, ldz, n}, nq * n, n, B, out, om);
 }
 
 }  // namespace hfgpu

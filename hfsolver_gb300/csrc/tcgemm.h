@@ -33,5 +33,12 @@ void slice_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p
 void slice_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, Sliced& s);
 // out (+)= A B^T for slices A (M x K) and B (N x K)
 void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, OutMap om, bool accumulate);
+// out = A B^T with A's rows gathered and sliced inside the GEMM (no A planes in
+// HBM): rows (pair p, la) over si of the packed (mu nu|la si) ...
+void sliced_gemm_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n,
+                        const Sliced& B, double* out, OutMap om);
+// ... or rows (q, mu), q < nq, over nu of Zt[q * ldz + pair(mu, nu)]
+void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, const Sliced& B,
+                         double* out, OutMap om);
 
 }  // namespace hfgpu
