@@ -200,13 +200,38 @@ __device__ bool sp2_grid_barrier(Sp2Sync* s, unsigned nblocks)
     return ok;
 }
 
-// T = double for the final steps; T = float for the coarse steps of early SCF
-// iterations (stop once tr(X - X^2) < tol_idem and |tr X - nocc| < tol_n).
+// Sum of v over the block into *dst (one atomic per block).
+__device__ __forceinline__ void block_add(double v, double* dst)
+{
+    __shared__ double part[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) part[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += part[w];
+        if (s != 0.0) atomicAdd(dst, s);
+    }
+    __syncthreads();
+}
+
+// The whole SP2 recursion as one cooperative launch, one grid barrier per step.
+// tr[2k] = tr X_k and tr[2k+1] = ||X_k||_F^2 = tr X_k^2 (X_k symmetric) are
+// reduced while X_k is written, so every block can choose X^2 or 2X - X^2 for
+// step k before it squares.  The iterate alternates between X0 and X1; a block
+// squares its 16 x 16 upper-triangle tile from its 16 rows and 16 columns of X_k,
+// staged whole in shared memory (stride n + 1: no bank conflicts).  The result
+// ends in X0.  T = float for the coarse steps of early SCF iterations.
 template <typename T>
-__global__ void __launch_bounds__(SQ_T* SQ_T) sp2_persistent_kernel(int n, int nocc, T* X, double* tr, int maxs,
+__global__ void __launch_bounds__(SQ_T* SQ_T) sp2_persistent_kernel(int n, int nocc, T* X0, T* X1, double* tr, int maxs,
                                                                     double tol_idem, double tol_n, Sp2Sync* sync)
 {
-    __shared__ T As[SQ_T][SQ_T + 1], Bs[SQ_T][SQ_T + 1];
+    extern __shared__ __align__(16) unsigned char sp2_smem[];
+    const int ld = n + 1;
+    T* Ar = (T*)sp2_smem;  // rows i0 .. i0+15 of X_k, all k
+    T* Bc = Ar + SQ_T * ld;  // columns j0 .. j0+15 (rows by symmetry)
     const int nt = (n + SQ_T - 1) / SQ_T;
     int b = blockIdx.x, ti = 0;
     while (b >= nt - ti) {
@@ -214,62 +239,80 @@ __global__ void __launch_bounds__(SQ_T* SQ_T) sp2_persistent_kernel(int n, int n
         ++ti;
     }
     const int tj = ti + b;
+    const int i0 = ti * SQ_T, j0 = tj * SQ_T;
     const int ty = threadIdx.x / SQ_T, tx = threadIdx.x % SQ_T;
-    const int i = ti * SQ_T + ty, j = tj * SQ_T + tx;
+    const int i = i0 + ty, j = j0 + tx;
     const bool own = i < n && j < n;
     for (int it = 0; it < maxs; ++it) {
-        T acc = 0;
-        for (int k0 = 0; k0 < n; k0 += SQ_T) {
-            const int ka = k0 + tx, kb = k0 + ty;
-            As[ty][tx] = (i < n && ka < n) ? __ldcg(X + i + (int64_t)ka * n) : T(0);
-            Bs[ty][tx] = (kb < n && j < n) ? __ldcg(X + kb + (int64_t)j * n) : T(0);
-            __syncthreads();
-#pragma unroll
-            for (int k = 0; k < SQ_T; ++k) acc = fma(As[ty][k], Bs[k][tx], acc);
-            __syncthreads();
-        }
-        if (own && i == j) atomicAdd(tr + 2 * it + 1, (double)acc);
-        if (!sp2_grid_barrier(sync, gridDim.x)) return;
+        T* Xc = (it & 1) ? X1 : X0;
+        T* Xn = (it & 1) ? X0 : X1;
         const double t0 = __ldcg(tr + 2 * it), t1 = __ldcg(tr + 2 * it + 1);
-        const bool square = fabs(t1 - nocc) <= fabs(2 * t0 - t1 - nocc);
-        const bool done = fabs(t0 - t1) < tol_idem && fabs(t0 - nocc) < tol_n;
-        if (own) {
-            const T x = square ? acc : T(2) * __ldcg(X + i + (int64_t)j * n) - acc;
-            X[i + (int64_t)j * n] = x;
-            if (ti != tj) X[j + (int64_t)i * n] = x;
-            if (i == j) atomicAdd(tr + 2 * it + 2, (double)x);
-        }
-        if (done) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) sync->steps = it + 1;
+        if (fabs(t0 - t1) < tol_idem && fabs(t0 - nocc) < tol_n) {
+            if ((it & 1) && own) {  // X_k is in X1: move this block's tile to X0
+                X0[i + (int64_t)j * n] = __ldcg(X1 + i + (int64_t)j * n);
+                if (ti != tj) X0[j + (int64_t)i * n] = __ldcg(X1 + j + (int64_t)i * n);
+            }
+            if (blockIdx.x == 0 && threadIdx.x == 0) sync->steps = it;
             return;
         }
+        const bool square = fabs(t1 - nocc) <= fabs(2 * t0 - t1 - nocc);
+        for (int e = threadIdx.x; e < SQ_T * n; e += SQ_T * SQ_T) {
+            const int r = e % SQ_T, k = e / SQ_T;  // r fastest: 16 consecutive doubles of a column
+            Ar[r * ld + k] = (i0 + r < n) ? __ldcg(Xc + i0 + r + (int64_t)k * n) : T(0);
+            Bc[r * ld + k] = (j0 + r < n) ? __ldcg(Xc + j0 + r + (int64_t)k * n) : T(0);
+        }
+        __syncthreads();
+        T acc = 0;
+        const T* ar = Ar + ty * ld;
+        const T* bc = Bc + tx * ld;
+        for (int k = 0; k < n; ++k) acc = fma(ar[k], bc[k], acc);
+        double pt = 0.0, pn = 0.0;
+        if (own) {
+            const T x = square ? acc : T(2) * __ldcg(Xc + i + (int64_t)j * n) - acc;
+            Xn[i + (int64_t)j * n] = x;
+            if (ti != tj) Xn[j + (int64_t)i * n] = x;
+            if (i == j) pt = (double)x;
+            pn = (double)x * (double)x * (ti != tj ? 2.0 : 1.0);
+        }
+        block_add(pt, tr + 2 * (it + 1));  // (its __syncthreads also guard Ar/Bc reuse)
+        block_add(pn, tr + 2 * (it + 1) + 1);
         if (!sp2_grid_barrier(sync, gridDim.x)) return;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) sync->steps = maxs;
 }
 
-// dst = src in another precision; tr0 += its trace
+// dst = src in another precision; trn[0] += its trace, trn[1] += its squared norm
 template <typename S, typename D>
-__global__ void convert_trace_kernel(int n, const S* __restrict__ src, D* __restrict__ dst, double* tr0)
+__global__ void convert_trace_kernel(int n, const S* __restrict__ src, D* __restrict__ dst, double* trn)
 {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)n * n) return;
-    const D v = (D)src[idx];
-    dst[idx] = v;
-    if (idx % n == idx / n) atomicAdd(tr0, (double)v);
+    double t = 0.0, q = 0.0;
+    if (idx < (int64_t)n * n) {
+        const D v = (D)src[idx];
+        dst[idx] = v;
+        if (idx % n == idx / n) t = (double)v;
+        q = (double)v * (double)v;
+    }
+    block_add(t, trn);
+    block_add(q, trn + 1);
 }
 
 // X = (emax I - F) / (emax - emin): spectrum mapped into [0, 1], occupied states
-// near 1; trX = tr X of this initial iterate
+// near 1; trX[0] = tr X and trX[1] = ||X||_F^2 of this initial iterate
 __global__ void sp2_init2_kernel(int n, const double* __restrict__ F, const double* __restrict__ b, double* X,
                                  double* trX)
 {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)n * n) return;
-    const int i = idx % n, j = idx / n;
-    const double x = ((i == j ? b[1] : 0.0) - F[idx]) / (b[1] - b[0]);
-    X[idx] = x;
-    if (i == j) atomicAdd(trX, x);
+    double t = 0.0, q = 0.0;
+    if (idx < (int64_t)n * n) {
+        const int i = idx % n, j = idx / n;
+        const double x = ((i == j ? b[1] : 0.0) - F[idx]) / (b[1] - b[0]);
+        X[idx] = x;
+        if (i == j) t = x;
+        q = x * x;
+    }
+    block_add(t, trX);
+    block_add(q, trX + 1);
 }
 
 // one SP2 step from the traces of this step (t[0] = tr X, t[1] = tr X^2);
@@ -287,11 +330,17 @@ __global__ void sp2_step_kernel(int n, int nocc, const double* __restrict__ t, c
 }
 
 // can all `blocks` blocks of the persistent SP2 kernel be resident at once?
-static bool coop_ok(Context& ctx, unsigned blocks)
+static bool coop_ok(Context& ctx, int n, unsigned blocks)
 {
     int coop = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx.device) != cudaSuccess || !coop) return false;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sp2_persistent_kernel<double>, SQ_T * SQ_T, 0) !=
+    const size_t smem = 2 * SQ_T * (size_t)(n + 1) * sizeof(double);
+    if (cudaFuncSetAttribute(sp2_persistent_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(sp2_persistent_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+        return false;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sp2_persistent_kernel<double>, SQ_T * SQ_T, smem) !=
         cudaSuccess)
         return false;
     return (int64_t)per_sm * ctx.num_sms >= (int64_t)blocks;
@@ -336,16 +385,17 @@ struct Purifier {
     // One cooperative launch of the whole recursion on the iterate Xs, with
     // barrier state slot `which` (0: FP32 steps, 1: FP64 steps).
     template <typename T>
-    void run_persistent(Context& ctx, T* Xs, double* trs, int maxs, double tol_idem, double tol_n, unsigned tiles,
-                        int which)
+    void run_persistent(Context& ctx, T* Xs, T* Xw, double* trs, int maxs, double tol_idem, double tol_n,
+                        unsigned tiles, int which)
     {
         cudaStream_t st = ctx.stream;
         HF_CUDA(cudaMemsetAsync(sync.p + which, 0, sizeof(Sp2Sync), st));
         int n_ = n, nocc_ = nocc;
         Sp2Sync* sp = sync.p + which;
-        void* args[] = {&n_, &nocc_, &Xs, &trs, &maxs, &tol_idem, &tol_n, &sp};
+        void* args[] = {&n_, &nocc_, &Xs, &Xw, &trs, &maxs, &tol_idem, &tol_n, &sp};
+        const size_t smem = 2 * SQ_T * (size_t)(n + 1) * sizeof(T);
         HF_CUDA(cudaLaunchCooperativeKernel((const void*)sp2_persistent_kernel<T>, dim3(tiles), dim3(SQ_T * SQ_T),
-                                            args, 0, st));
+                                            args, smem, st));
         count_launch();
     }
     // The outcome of the last cooperative purification (barrier timeouts, final
@@ -361,7 +411,7 @@ struct Purifier {
         pending = false;
         HF_CHECK(hsync[0].err == 0 && hsync[1].err == 0, HFGPU_ERR_CUDA,
                  "density purification: grid barrier timed out");
-        const int last = std::max(hsync[1].steps, 1) - 1;
+        const int last = std::min(std::max(hsync[1].steps, 0), MAXS);
         HF_CHECK(fabs(htr[2 * last] - nocc) < 1e-6, HFGPU_ERR_LINALG,
                  "density purification did not converge (no gap?)");
     }
@@ -394,7 +444,7 @@ struct Purifier {
         const unsigned tiles = (unsigned)(nt * (nt + 1) / 2);
         double h[2] = {0, 1};
         bool done = false;
-        if (coop_ok(ctx, tiles)) {
+        if (coop_ok(ctx, n, tiles)) {
             if (!sync.p) {
                 sync.alloc(2, st);
                 HF_CUDA(cudaMemsetAsync(sync.p, 0, 2 * sizeof(Sp2Sync), st));
@@ -403,24 +453,27 @@ struct Purifier {
             }
             double* tr64 = tr.p;
             if (coarse) {
-                if (Xf.n < (size_t)nn) Xf.alloc(nn, st);
+                if (Xf.n < (size_t)(2 * nn)) Xf.alloc(2 * nn, st);
                 double* trf = tr.p + 2 * (MAXS + 1);
                 convert_trace_kernel<double, float><<<nblk(nn), 256, 0, st>>>(n, T1.p, Xf.p, trf);
                 count_launch();
-                run_persistent<float>(ctx, Xf.p, trf, MAXS, 1e-3, 1e-3, tiles, 0);
+                run_persistent<float>(ctx, Xf.p, Xf.p + nn, trf, MAXS, 1e-3, 1e-3, tiles, 0);
                 HF_CUDA(cudaMemsetAsync(tr64, 0, sizeof(double) * 2 * (MAXS + 1), st));
                 convert_trace_kernel<float, double><<<nblk(nn), 256, 0, st>>>(n, Xf.p, T1.p, tr64);
                 count_launch();
             } else {
                 HF_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(Sp2Sync), st));  // no FP32 phase this time
             }
-            run_persistent<double>(ctx, T1.p, tr64, MAXS, 1e-13 * n, 1e-6, tiles, 1);
+            // T2 (X^T F X) is free once the first iterate is built: the second buffer
+            run_persistent<double>(ctx, T1.p, T2.p, tr64, MAXS, 1e-13 * n, 1e-6, tiles, 1);
             HF_CUDA(cudaMemcpyAsync(hsync, sync.p, 2 * sizeof(Sp2Sync), cudaMemcpyDeviceToHost, st));
             HF_CUDA(cudaMemcpyAsync(htr, tr64, 2 * (MAXS + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
             pending = true;
             done = true;
             h[0] = nocc;  // checked later by check()
         }
+        // launch-per-step fallback: tr[2k+1] is accumulated by the square kernel
+        if (!done) HF_CUDA(cudaMemsetAsync(tr.p + 1, 0, sizeof(double), st));
         for (int it = 0; it < MAXS && !done; ++it) {
             sym_square_kernel<<<tiles, SQ_T * SQ_T, 0, st>>>(n, T1.p, T2.p, tr.p + 2 * it + 1);
             count_launch();

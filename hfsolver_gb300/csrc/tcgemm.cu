@@ -451,10 +451,12 @@ struct SymPairRows {  // rows (q, mu), k = nu of Zt[q * ldz + pair(mu, nu)] (Z t
 // them straight into the stage's shared-memory tiles in the 64-byte-swizzled
 // K-major layout the MMA reads (16-byte chunk c of row r at chunk c ^ ((r >> 1) & 3)).
 // B still arrives by TMA.  The row exponents come from row_exp_kernel.
-// 256 threads: thread t produces row t % 128, K half t / 128 of every stage;
-// thread 0 also issues the B loads and the products; all 8 warps share the
-// epilogue (warp w: TMEM lanes 32 (w % 4), columns half w / 4).
-constexpr int GATHER_THREADS = 256;
+// 512 threads: thread t produces row t % 128, K quarter t / 128 (8 elements, one
+// 16-byte chunk per plane) of every stage, fetching the next stage's elements
+// before it stores this one; thread 0 also issues the B loads and the products;
+// the 16 warps share the epilogue (warp w: TMEM lanes 32 (w % 4), columns
+// 16 (w / 4) .. +15).
+constexpr int GATHER_THREADS = 512;
 
 template <class Src>
 __global__ void row_exp_kernel(Src src, int64_t rows, int K, int* __restrict__ rexp)
@@ -498,7 +500,10 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
     auto sB = [&](int s, int t) { return smem + s * STAGE_BYTES + NSL * A_TILE + t * B_TILE; };
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int prow = tid & (BM - 1), half = tid / BM;
+    constexpr int PARTS = GATHER_THREADS / BM;  // K parts of a stage per row
+    constexpr int PK = BK / PARTS;              // elements per thread and stage (8: one 16-byte chunk)
+    static_assert(PK == 8, "one 16-byte chunk per thread and plane");
+    const int prow = tid & (BM - 1), part = tid / BM;
     if (tid == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(&full[s], GATHER_THREADS + 1);  // every producer + the B expect_tx
@@ -528,6 +533,13 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
         const bool live = R < M;
         const typename Src::Row row = src.row(live ? R : 0);
         const int e = live ? ea[R] : 0;
+        // this thread's 8 elements of step 0, fetched ahead
+        double x[PK];
+#pragma unroll
+        for (int j = 0; j < PK; ++j) {
+            const int k = part * PK + j;
+            x[j] = (live && k < K) ? src.at(row, k) : 0.0;
+        }
         for (int ks = 0; ks < ksteps && ok; ++ks) {
             const int64_t g = g0 + ks;
             const int s = (int)(g % STAGES);
@@ -541,28 +553,27 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
                 for (int t = 0; t < NSL; ++t) tma_load_2d(sB(s, t), &tmB, ks * BK, t * b_rows_pad + n0, &full[s]);
                 pend_b = g;
             }
-            // 16 elements of this thread's row -> 2 swizzled 16-byte chunks per plane
-            uint32_t w[NSL][8];
+            uint32_t w[NSL][PK / 2];
 #pragma unroll
-            for (int j = 0; j < 16; j += 2) {
-                const int k = ks * BK + half * 16 + j;
-                const double x0 = (live && k < K) ? src.at(row, k) : 0.0;
-                const double x1 = (live && k + 1 < K) ? src.at(row, k + 1) : 0.0;
+            for (int j = 0; j < PK; j += 2) {
                 uint16_t d0[NSL], d1[NSL];
-                digits_bf16(x0, e, d0);
-                digits_bf16(x1, e, d1);
+                digits_bf16(x[j], e, d0);
+                digits_bf16(x[j + 1], e, d1);
 #pragma unroll
                 for (int t = 0; t < NSL; ++t) w[t][j / 2] = (uint32_t)d0[t] | ((uint32_t)d1[t] << 16);
             }
-            const int sw = (prow >> 1) & 3;
+            // the next step's elements are in flight while this one is stored and multiplied
+            if (ks + 1 < ksteps) {
+#pragma unroll
+                for (int j = 0; j < PK; ++j) {
+                    const int k = (ks + 1) * BK + part * PK + j;
+                    x[j] = (live && k < K) ? src.at(row, k) : 0.0;
+                }
+            }
+            const int c = part ^ ((prow >> 1) & 3);  // 64-byte swizzle: chunk c of row r at c ^ ((r >> 1) & 3)
 #pragma unroll
             for (int t = 0; t < NSL; ++t)
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    const int c = (half * 2 + q) ^ sw;
-                    uint4 v = make_uint4(w[t][4 * q], w[t][4 * q + 1], w[t][4 * q + 2], w[t][4 * q + 3]);
-                    *reinterpret_cast<uint4*>(sA(s, t) + prow * 64 + c * 16) = v;
-                }
+                *reinterpret_cast<uint4*>(sA(s, t) + prow * 64 + c * 16) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
             // the tensor core reads shared memory through the async proxy
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(&full[s]);
@@ -596,10 +607,11 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
         ok = __syncthreads_and(ok);
         if (ok) {
             fence_after();
+            // warp w: TMEM lanes 32 (w % 4), 16 columns starting at 16 (w / 4)
             const int64_t r = m0 + (warp & 3) * 32 + lane;
             const int er = (r < M) ? ea[r] : 0;
-            const int cbeg = (warp >> 2) * (BN / 2);
-            for (int c0 = cbeg; c0 < cbeg + BN / 2 && n0 + c0 < N; c0 += 16) {
+            const int c0 = (warp >> 2) * 16;
+            if (c0 < BN && n0 + c0 < N) {
                 long long S[16];
 #pragma unroll
                 for (int i = 0; i < 16; ++i) S[i] = 0;
