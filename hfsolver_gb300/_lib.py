@@ -35,7 +35,8 @@ class Result(ctypes.Structure):
                 ("eri_flops", ctypes.c_double), ("ms_eri", ctypes.c_double), ("ms_scf", ctypes.c_double),
                 ("ms_mp2", ctypes.c_double), ("ms_total", ctypes.c_double), ("ms_setup", ctypes.c_double),
                 ("ms_fock", ctypes.c_double), ("ms_tcgemm", ctypes.c_double), ("tc_flops", ctypes.c_double),
-                ("ms_grad", ctypes.c_double), ("reserved", ctypes.c_double * 3)]
+                ("ms_grad", ctypes.c_double), ("ms_fock_full", ctypes.c_double), ("n_fock_full", ctypes.c_double),
+                ("block_elems", ctypes.c_double)]
 
 
 # name -> (restype, argtypes); the list every test of the ABI checks against

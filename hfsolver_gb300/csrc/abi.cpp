@@ -118,6 +118,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         cudaStream_t st = ctx.stream;
         ctx.settle_timers();  // drop timers a failed earlier call may have left
         ctx.stat_fock_ms = ctx.stat_tc_ms = ctx.stat_tc_flops = 0;
+        ctx.stat_fock_full_ms = ctx.stat_fock_full_n = 0;
         ctx.tune = opt.autotune != 0 || tune_env_enabled();
         Timer total(st);
         const int n = b.nbf;
@@ -201,6 +202,9 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         res->ms_total = total.ms();
         ctx.settle_timers();
         res->ms_fock = ctx.stat_fock_ms;
+        res->ms_fock_full = ctx.stat_fock_full_ms;
+        res->n_fock_full = ctx.stat_fock_full_n;
+        res->block_elems = (double)es.n_block_elems;
         res->ms_tcgemm = ctx.stat_tc_ms;
         res->tc_flops = ctx.stat_tc_flops;
 }

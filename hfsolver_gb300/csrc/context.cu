@@ -104,12 +104,16 @@ void Context::fork()
 void Context::settle_timers()
 {
     for (auto& e : fock_events) {
-        HF_CUDA(cudaEventSynchronize(e.second));
+        HF_CUDA(cudaEventSynchronize(e.b));
         float ms = 0;
-        HF_CUDA(cudaEventElapsedTime(&ms, e.first, e.second));
+        HF_CUDA(cudaEventElapsedTime(&ms, e.a, e.b));
         stat_fock_ms += ms;
-        cudaEventDestroy(e.first);
-        cudaEventDestroy(e.second);
+        if (e.full) {
+            stat_fock_full_ms += ms;
+            stat_fock_full_n += 1;
+        }
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
     }
     fock_events.clear();
 }

@@ -564,7 +564,7 @@ void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG, double s
     count_launch();
     HF_CUDA(cudaGetLastError());
     HF_CUDA(cudaEventRecord(e1, ctx.stream));
-    ctx.fock_events.emplace_back(e0, e1);  // timed later, without a host wait here
+    ctx.fock_events.push_back({e0, e1, screen <= 0});  // timed later, without a host wait here
 }
 EriStats eri_plan_stats(const EriPlan* p) { return p->stats; }
 
@@ -630,6 +630,8 @@ static void eri_class_tuned(Context& ctx, EriPlan* P, ClassPlan& c, double* d_ou
 
 void eri_compute(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks, EriStats* st)
 {
+    P->stats.n_block_elems = 0;
+    for (auto& c : P->classes) P->stats.n_block_elems += c.nq * block_size(c.tb, c.tk);
     if (keep_blocks) {
         int64_t total = 0;
         for (auto& c : P->classes) {

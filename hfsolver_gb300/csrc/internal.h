@@ -124,8 +124,13 @@ struct Context {
     void join();  // `stream` waits for the work queued on the aux streams
     // event pairs around Fock builds, summed into stat_fock_ms by settle_timers()
     // once the stream is synchronised anyway (no host wait per build)
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> fock_events;
+    struct FockTimer {
+        cudaEvent_t a, b;
+        bool full;  // a full build (not a screened density difference)
+    };
+    std::vector<FockTimer> fock_events;
     void settle_timers();
+    double stat_fock_full_ms = 0, stat_fock_full_n = 0;
     // kernel-time counters, reset by the pipeline entry points
     double stat_fock_ms = 0, stat_tc_ms = 0, stat_tc_flops = 0;
     bool tune = false;  // time candidate kernel shapes on first use (autotune.cpp)
@@ -167,6 +172,7 @@ int basis_size(int natoms, const int* atno);
 // ---------------------------------------------------------------- integrals
 struct EriStats {
     int64_t n_quartets = 0, n_bf_quartets = 0, n_prim_quartets = 0;
+    int64_t n_block_elems = 0;  // component quartets of the surviving shell quartets (Fock digest work)
     double flops = 0;
     double ms = 0;
 };

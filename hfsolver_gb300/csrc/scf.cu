@@ -12,6 +12,7 @@
 // back two scalars (E0, dP) for the convergence test.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "internal.h"
@@ -186,7 +187,7 @@ __device__ bool sp2_grid_barrier(Sp2Sync* s, unsigned nblocks)
         } else {
             long spins = 0;
             while (*vgen == g) {
-                if (++spins > (1L << 22)) {
+                if (++spins > (1L << 24)) {  // ~1 s: other streams may hold SMs for a while
                     atomicExch(&s->err, 1);
                     break;
                 }
@@ -334,12 +335,19 @@ static bool coop_ok(Context& ctx, int n, unsigned blocks)
 {
     int coop = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx.device) != cudaSuccess || !coop) return false;
+    // the attribute is per process: set it once, for the largest n (512), so that
+    // concurrent molecules of other sizes never lower it under each other
+    static std::once_flag once;
+    static bool attr_ok = false;
+    std::call_once(once, [] {
+        const int most = (int)(2 * SQ_T * (size_t)(512 + 1) * sizeof(double));
+        attr_ok = cudaFuncSetAttribute(sp2_persistent_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       most) == cudaSuccess &&
+                  cudaFuncSetAttribute(sp2_persistent_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       most) == cudaSuccess;
+    });
     const size_t smem = 2 * SQ_T * (size_t)(n + 1) * sizeof(double);
-    if (cudaFuncSetAttribute(sp2_persistent_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(sp2_persistent_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
-        return false;
+    if (!attr_ok || n > 512) return false;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sp2_persistent_kernel<double>, SQ_T * SQ_T, smem) !=
         cudaSuccess)
         return false;

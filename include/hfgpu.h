@@ -202,7 +202,9 @@ typedef struct {
     double ms_tcgemm;        /* tensor-core sliced GEMM kernels (mixed MBPT2) */
     double tc_flops;         /* bf16 tensor flops those kernels performed (2 M N K per product) */
     double ms_grad;          /* analytic gradient (hfgpu_rhf_gradient) */
-    double reserved[3];
+    double ms_fock_full;     /* the part of ms_fock spent in full (not incremental) Fock builds */
+    double n_fock_full;      /* number of those full builds */
+    double block_elems;      /* component quartets a full Fock build digests (12 flops each) */
 } hfgpu_result;
 
 void hfgpu_default_options(hfgpu_options *opt);
