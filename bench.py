@@ -107,7 +107,7 @@ def options(mp2="split_bf16"):
     import hfsolver_gb300 as hf
 
     return hf.RHFOptions(nscf=60, diis=True, diis_size=8, schwarz=1e-12, tolE=1e-10, tolP=1e-8, mp2=mp2,
-                         purify=True, incremental=True, autotune=True)
+                         purify=True, incremental=True, autotune=True, guess="sad")
 
 
 # ---------------------------------------------------------------- CPU baseline
@@ -307,7 +307,7 @@ def run_gpu(args):
                    "molecule": f"{args.waters} H2O, seed=rank, "
                                f"{11.0 if args.waters == 16 else 8.0 * (args.waters / 8) ** (1 / 3):.2f} A cube",
                    "nbf": n, "nocc": r["nocc"],
-                   "global_batch": world, "scf": "DIIS + SP2 purification, incremental Fock builds",
+                   "global_batch": world, "scf": "DIIS + SP2 purification, incremental Fock builds, atomic-density start",
                    "autotune": True, "schwarz": 1e-12, "mp2": main_mp2,
                    "l2": f"no flush: each step rebuilds the {8 * (n * (n + 1) // 2) * (n * (n + 1) // 2 + 1) // 2 / 1e9:.1f} GB "
                          "packed ERI array (> 129 MB L2)",

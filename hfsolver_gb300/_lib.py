@@ -23,7 +23,7 @@ class Options(ctypes.Structure):
                 ("tolP", ctypes.c_double), ("scf_accel", ctypes.c_int), ("diis_size", ctypes.c_int),
                 ("schwarz", ctypes.c_double), ("mp2", ctypes.c_int), ("mp2_nocc", ctypes.c_int),
                 ("purify", ctypes.c_int), ("batch_streams", ctypes.c_int), ("incremental", ctypes.c_int),
-                ("autotune", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
+                ("autotune", ctypes.c_int), ("guess", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 class Result(ctypes.Structure):

@@ -206,6 +206,7 @@ class RHFOptions:
     batch_streams: int = 0     # rhf_batch: molecules in flight at once (<= 0: 8)
     incremental: bool = False  # Fock builds from screened density differences
     autotune: bool = False     # time candidate kernel shapes on first use, keep the fastest
+    guess: str = "core"        # starting density: "core" (P = 0, the reference) | "sad" (atomic densities)
 
     def to_c(self):
         o = _lib.Options()
@@ -220,6 +221,7 @@ class RHFOptions:
         o.batch_streams = self.batch_streams
         o.incremental = 1 if self.incremental else 0
         o.autotune = 1 if self.autotune else 0
+        o.guess = {"core": 0, "sad": 1}[self.guess]
         return o
 
 

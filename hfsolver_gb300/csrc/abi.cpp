@@ -163,6 +163,12 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         };
         if (opt.incremental) in.inc_screen = opt.schwarz > 0 ? opt.schwarz : 1e-12;
         in.direct_ctx = plan.get();
+        DBuf<double> dP0;
+        if (opt.guess == 1) {  // superposition of atomic densities instead of P = 0
+            dP0.alloc(nn, st);
+            sad_guess(ctx, natoms, atno, n, dP0.p);
+            in.dP0 = dP0.p;
+        }
         ScfOut so = run_scf(ctx, in, dC.p, dP.p, dL.p);
         res->ms_scf = ts.ms();
         conv = so.converged;

@@ -205,6 +205,10 @@ void jk_separate_from_packed(Context& ctx, int n, const double* d_int2, const do
 
 int64_t packed_size(int64_t n);
 
+// superposition of atomic densities for a basis built by build_basis (guess.cpp):
+// dP0 (device, nbf x nbf) gets the block-diagonal sum of cached free-atom densities
+void sad_guess(Context& ctx, int natoms, const int* atno, int nbf, double* dP0);
+
 // analytic RHF nuclear gradient (grad.cu) at converged orbitals dC, energies dL
 // (device, n x n and n); grad gets 3 values per atom (Ha/bohr), host memory
 void rhf_gradient(Context& ctx, EriPlan* plan, int natoms, const int* atno, const double* xyz, const double* dC,

@@ -545,7 +545,10 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
     HF_CHECK(in.nocc >= 0 && in.nocc <= n, HFGPU_ERR_INVALID, "nocc out of range");
     DBuf<double> G(nn, st), F(nn, st), Fw(nn, st), Sw(nn, st), Pold(nn, st), scal(4, st);
     DBuf<int> info(1, st);
-    HF_CUDA(cudaMemsetAsync(dP, 0, sizeof(double) * nn, st));
+    if (in.dP0)
+        HF_CUDA(cudaMemcpyAsync(dP, in.dP0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+    else
+        HF_CUDA(cudaMemsetAsync(dP, 0, sizeof(double) * nn, st));
     int lwork = 0;
     HF_CUSOLVER(cusolverDnDsygvd_bufferSize(ctx.solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
                                             CUBLAS_FILL_MODE_LOWER, n, Fw.p, n, Sw.p, n, dLam, &lwork));
@@ -606,9 +609,9 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
         count_launch();
         reduce(ctx, 0, nn, dP, in.dH, F.p, scal.p);  // E0
         const double* Fsolve = F.p;
-        // the first iteration has P = 0, whose commutator vanishes trivially: keep
-        // it out of the DIIS history
-        if (diis && it >= 2) {
+        // the first iteration of a P = 0 start has a commutator that vanishes
+        // trivially: keep it out of the DIIS history
+        if (diis && (it >= 2 || in.dP0)) {
             const double one = 1.0, zero = 0.0;
             // error = F P S - S P F = Y - Y^T with Y = F P S
             HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, F.p, n, dP, n, &zero, G.p, n));

@@ -25,6 +25,8 @@ struct ScfIn {
     // inc_rebuild iterations and before convergence is accepted.  0: off.
     double inc_screen = 0.0;
     int inc_rebuild = 8;
+    // starting density (device, n x n); null: P = 0 as in the reference's doscf
+    const double* dP0 = nullptr;
 };
 
 struct ScfOut {

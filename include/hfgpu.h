@@ -183,7 +183,9 @@ typedef struct {
                             kernels the first time a (class, size) is met and keep the
                             fastest (process-wide table); 0: built-in rules, unless the
                             environment sets HFGPU_AUTOTUNE=1 */
-    int reserved[4];
+    int guess;           /* starting density: 0 = P = 0 (the reference's doscf), 1 = superposition
+                            of free-atom densities (closer start, fewer iterations) */
+    int reserved[3];
 } hfgpu_options;
 
 typedef struct {

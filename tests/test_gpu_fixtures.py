@@ -44,6 +44,20 @@ def test_cluster_energies_bench_configuration(nw):
 
 
 @pytest.mark.parametrize("nw", sorted(FIX, key=int))
+def test_cluster_energies_atomic_guess(nw):
+    """Starting from the superposition of atomic densities reaches the same SCF
+    solution as the reference's P = 0 start, in fewer iterations."""
+    f = FIX[nw]
+    atno, xyz = water_cluster(f["n_waters"], seed=f["seed"])
+    o = dict(nscf=60, diis=True, schwarz=1e-12, tolP=1e-10, tolE=1e-12, mp2="fp64")
+    core = hf.rhf(atno, xyz, hf.RHFOptions(**o))
+    sad = hf.rhf(atno, xyz, hf.RHFOptions(guess="sad", **o))
+    assert abs(sad["Etot"] - f["Etot"]) <= 1e-10
+    assert abs(sad["E2"] - f["E2"]) <= 1e-8
+    assert sad["niter"] < core["niter"]
+
+
+@pytest.mark.parametrize("nw", sorted(FIX, key=int))
 def test_cluster_packed_integrals(oracle, nw):
     f = FIX[nw]
     atno, xyz = water_cluster(f["n_waters"], seed=f["seed"])
