@@ -450,34 +450,14 @@ struct SymPairRows {  // rows (q, mu), k = nu of Zt[q * ldz + pair(mu, nu)] (Z t
 // gather A's FP64 elements (Src::row / Src::at), cut them into digits and store
 // them straight into the stage's shared-memory tiles in the 64-byte-swizzled
 // K-major layout the MMA reads (16-byte chunk c of row r at chunk c ^ ((r >> 1) & 3)).
-// B still arrives by TMA.  The row exponents come from row_exp_kernel.
+// B still arrives by TMA.  Each tile first takes its rows' exponents (the
+// largest magnitude of each row, from the same gathers).
 // 512 threads: thread t produces row t % 128, K quarter t / 128 (8 elements, one
 // 16-byte chunk per plane) of every stage, fetching the next stage's elements
 // before it stores this one; thread 0 also issues the B loads and the products;
 // the 16 warps share the epilogue (warp w: TMEM lanes 32 (w % 4), columns
 // 16 (w / 4) .. +15).
 constexpr int GATHER_THREADS = 512;
-
-template <class Src>
-__global__ void row_exp_kernel(Src src, int64_t rows, int K, int* __restrict__ rexp)
-{
-    const int lane = threadIdx.x & 31;
-    const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += nwarp) {
-        const typename Src::Row row = src.row(r);
-        unsigned long long amax = 0;
-        for (int k = lane; k < K; k += 32) {
-            const unsigned long long m = (unsigned long long)__double_as_longlong(src.at(row, k)) & 0x7FFFFFFFFFFFFFFFull;
-            amax = m > amax ? m : amax;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long v = __shfl_xor_sync(0xffffffffu, amax, o);
-            amax = v > amax ? v : amax;
-        }
-        if (lane == 0) rexp[r] = row_exponent(amax);
-    }
-}
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 {
@@ -486,7 +466,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 
 template <class Src>
 __global__ void __launch_bounds__(GATHER_THREADS, 1)
-    sliced_gemm_gather_kernel(Src src, const int* __restrict__ ea, const __grid_constant__ CUtensorMap tmB,
+    sliced_gemm_gather_kernel(Src src, const __grid_constant__ CUtensorMap tmB,
                               int b_rows_pad, int K, int ksteps, const int* __restrict__ eb, int64_t M, int N,
                               double* out, OutMap om, int* err, int64_t ntiles, int ntn)
 {
@@ -496,11 +476,13 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
     uint64_t* empty = full + STAGES;
     uint32_t* tslot = (uint32_t*)(empty + STAGES);
     __shared__ int s_ok;
+    constexpr int PARTS = GATHER_THREADS / BM;  // K parts of a stage per row
+    __shared__ unsigned long long s_amax[PARTS][BM];
+    __shared__ int s_exp[BM];  // row exponents of the current tile (for the epilogue)
     auto sA = [&](int s, int t) { return smem + s * STAGE_BYTES + t * A_TILE; };
     auto sB = [&](int s, int t) { return smem + s * STAGE_BYTES + NSL * A_TILE + t * B_TILE; };
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    constexpr int PARTS = GATHER_THREADS / BM;  // K parts of a stage per row
     constexpr int PK = BK / PARTS;              // elements per thread and stage (8: one 16-byte chunk)
     static_assert(PK == 8, "one 16-byte chunk per thread and plane");
     const int prow = tid & (BM - 1), part = tid / BM;
@@ -532,7 +514,24 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
         const int64_t R = m0 + prow;
         const bool live = R < M;
         const typename Src::Row row = src.row(live ? R : 0);
-        const int e = live ? ea[R] : 0;
+        // the row's exponent: the PARTS threads of a row take every PARTS-th element
+        // (these reads also bring the row into L2 for the steps below)
+        {
+            unsigned long long amax = 0;
+            if (live)
+                for (int k = part; k < K; k += PARTS) {
+                    const unsigned long long m =
+                        (unsigned long long)__double_as_longlong(src.at(row, k)) & 0x7FFFFFFFFFFFFFFFull;
+                    amax = m > amax ? m : amax;
+                }
+            s_amax[part][prow] = amax;
+        }
+        __syncthreads();
+        unsigned long long amax = s_amax[0][prow];
+#pragma unroll
+        for (int q = 1; q < PARTS; ++q) amax = s_amax[q][prow] > amax ? s_amax[q][prow] : amax;
+        const int e = row_exponent(amax);
+        if (part == 0) s_exp[prow] = e;
         // this thread's 8 elements of step 0, fetched ahead
         double x[PK];
 #pragma unroll
@@ -609,7 +608,7 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
             fence_after();
             // warp w: TMEM lanes 32 (w % 4), 16 columns starting at 16 (w / 4)
             const int64_t r = m0 + (warp & 3) * 32 + lane;
-            const int er = (r < M) ? ea[r] : 0;
+            const int er = s_exp[(warp & 3) * 32 + lane];
             const int c0 = (warp >> 2) * 16;
             if (c0 < BN && n0 + c0 < N) {
                 long long S[16];
@@ -781,14 +780,6 @@ static void gather_gemm(Context& ctx, const Src& src, int64_t M, int K, const Sl
                                      SMEM_BYTES));
         attr = true;
     }
-    DBuf<int> rexp((size_t)std::max<int64_t>(M, 1), ctx.stream);
-    {
-        const int64_t warps = std::min<int64_t>(M, (int64_t)ctx.num_sms * 64);
-        row_exp_kernel<Src><<<(unsigned)std::max<int64_t>(1, (warps * 32 + 255) / 256), 256, 0, ctx.stream>>>(
-            src, M, K, rexp.p);
-        count_launch();
-        HF_CUDA(cudaGetLastError());
-    }
     const CUtensorMap tb = make_map(B, BN);
     DBuf<int> err(1, ctx.stream);
     err.zero();
@@ -801,7 +792,7 @@ static void gather_gemm(Context& ctx, const Src& src, int64_t M, int K, const Sl
     HF_CHECK(ntiles > 0, HFGPU_ERR_INVALID, "gather GEMM: empty");
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, ctx.num_sms);
     sliced_gemm_gather_kernel<Src><<<grid, GATHER_THREADS, SMEM_BYTES, ctx.stream>>>(
-        src, rexp.p, tb, (int)B.rows_pad, K, B.K_pad / BK, B.rexp.p, M, (int)B.rows, out, om, err.p, ntiles, ntn);
+        src, tb, (int)B.rows_pad, K, B.K_pad / BK, B.rexp.p, M, (int)B.rows, out, om, err.p, ntiles, ntn);
     count_launch();
     HF_CUDA(cudaGetLastError());
     HF_CUDA(cudaEventRecord(e1, ctx.stream));
