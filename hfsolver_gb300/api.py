@@ -15,7 +15,9 @@ mp2_energy             transform_int2 + mbpt2 (E2 only)                hfgpu_mp2
 rhf_batch              rhf_gauss over many molecules                   hfgpu_rhf_batch
 transform_int2         src/mbpt.f90:11-79                              hfgpu_transform_int2
 mbpt2                  src/mbpt.f90:154-159, src/mbpt2.f90:8-31        hfgpu_mbpt2
+mbpt3                  src/mbpt.f90:161-169, src/mbpt3.f90:8-128       hfgpu_mbpt3
 rhf_gauss / rhf        src/drivers.f90:12-51 (+ MBPT2)                 hfgpu_rhf
+rhf_gradient           dE/dR for src/md.f90:13-20 (no reference)       hfgpu_rhf_gradient
 =====================  ==============================================  =======================
 
 Errors raise HFGPUError (the reference stops the process instead); an SCF
@@ -189,6 +191,14 @@ def mbpt2(moint2, lam, Noccupied):
     E2 = np.zeros(1)
     _check(_lib.lib().hfgpu_mbpt2(len(lam), _d(moint2), _d(lam), int(Noccupied), _d(E2)))
     return float(E2[0])
+
+
+def mbpt3(moint2, lam, Noccupied):
+    """mbpt.f90 mbpt3: the third-order energy from the packed MO integrals."""
+    moint2, lam = _f64(moint2), _f64(lam)
+    E3 = np.zeros(1)
+    _check(_lib.lib().hfgpu_mbpt3(len(lam), _d(moint2), _d(lam), int(Noccupied), _d(E3)))
+    return float(E3[0])
 
 
 @dataclass

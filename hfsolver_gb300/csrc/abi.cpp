@@ -415,6 +415,20 @@ int hfgpu_mbpt2(int n, const double* moint2, const double* lam, int nocc, double
     });
 }
 
+int hfgpu_mbpt3(int n, const double* moint2, const double* lam, int nocc, double* E3)
+{
+    return guard([&] {
+        HF_CHECK(n >= 1 && nocc >= 0 && nocc <= n, HFGPU_ERR_INVALID, "invalid sizes");
+        check_ptr(moint2, "moint2"); check_ptr(lam, "lam"); check_ptr(E3, "E3");
+        Context& ctx = context();
+        const int64_t np = packed_size(n);
+        DBuf<double> dM(np, ctx.stream), dL(n, ctx.stream);
+        dM.upload(moint2, np);
+        dL.upload(lam, n);
+        *E3 = mbpt3_packed(ctx, n, dM.p, dL.p, nocc);
+    });
+}
+
 int hfgpu_dgemm_sliced(int64_t M, int N, int K, const double* A, const double* Bt, double* C)
 {
     return guard([&] {

@@ -55,4 +55,6 @@ void transform_packed(Context& ctx, int n, const double* d_int2, const double* d
 double mp2_energy_mixed(Context& ctx, int n, const double* d_int2, const double* dC, int nocc, const double* d_eps);
 // term1 of src/mbpt2.f90 on packed MO integrals (mbpt2 drop-in)
 double mbpt2_packed(Context& ctx, int n, const double* d_mo, const double* d_lam, int nocc);
+// E3 of src/mbpt3.f90 on packed MO integrals (mbpt3 drop-in, mbpt3.cu)
+double mbpt3_packed(Context& ctx, int n, const double* d_mo, const double* d_lam, int nocc);
 }  // namespace hfgpu

@@ -142,6 +142,12 @@ int hfgpu_transform_int2(int n, const double *int2, const double *C, double *moi
  * from the packed MO integrals. */
 int hfgpu_mbpt2(int n, const double *moint2, const double *lam, int nocc, double *E2);
 
+/* replaces mbpt3, src/mbpt.f90:161-169 (term1 + term2 + term3 of
+ * src/mbpt3.f90:8-128): the third-order energy from the packed MO integrals,
+ * all electrons correlated.  FP64; the terms run as dense GEMMs over compound
+ * occupied-virtual indices instead of the reference's six nested loops. */
+int hfgpu_mbpt3(int n, const double *moint2, const double *lam, int nocc, double *E3);
+
 /* FP64-accurate C = A B on the tcgen05 tensor cores (the kernel behind the
  * mixed-precision transform): A row-major M x K, Bt = B^T row-major N x K
  * (B column-major), C row-major M x N; 1 <= K <= 512.  Rows of A and columns

@@ -412,6 +412,49 @@ def mbpt2(moint2, lam, nocc):
     return float(np.sum((2 * arbs * arbs - arbs * asbr) / den))
 
 
+def mbpt3(moint2, lam, nocc):
+    """E3 = term1 + term2 + term3 of mbpt3.f90 (the three functions of
+    mbpt3.f90:8-128, summed by mbpt.f90:161-169), each restated term for term
+    from its loops with numpy contractions over the dense MO integrals."""
+    n = len(lam)
+    I = unpack(moint2, n)
+    o, v = slice(0, nocc), slice(nocc, n)
+    e_o, e_v = lam[:nocc], lam[nocc:]
+    # D[a, b, r, s] = -lam(r) - lam(s) + lam(a) + lam(b)
+    D = e_o[:, None, None, None] + e_o[None, :, None, None] - e_v[None, None, :, None] - e_v[None, None, None, :]
+    ovov = I[o, v, o, v]            # (a r | b s) as [a, r, b, s]
+    arbs = ovov.transpose(0, 2, 1, 3)  # [a, b, r, s]
+    brs_a = ovov.transpose(2, 0, 1, 3)  # (b r | a s) as [a, b, r, s]
+    # term1 (mbpt3.f90:8-62): a, b, c occupied; r, s, t virtual; denominators
+    # D[a,b,r,s] * D[b,c,s,t]
+    ra_ct = I[v, o, o, v]           # (r a | c t) as [r, a, c, t]
+    sb_tc = I[v, o, v, o]           # (s b | t c) as [s, b, t, c]
+    tb_sc = I[v, o, v, o]           # (t b | s c) as [t, b, s, c]
+    ca_rt = I[o, o, v, v]           # (c a | r t) as [c, a, r, t]
+    A1 = np.einsum("ract->acrt", ra_ct)       # (ra|ct)[a, c, r, t]
+    A2 = np.einsum("cart->acrt", ca_rt)       # (ca|rt)[a, c, r, t]
+    B1 = np.einsum("sbtc->bcst", sb_tc)       # (sb|tc)[b, c, s, t]
+    B2 = np.einsum("tbsc->bcst", tb_sc)       # (tb|sc)[b, c, s, t]
+    t1 = 0.0
+    for coef, F, A, B in ((8, arbs, A1, B1), (-4, arbs, A1, B2), (-4, arbs, A2, B1), (2, arbs, A2, B2),
+                          (-4, brs_a, A1, B1), (2, brs_a, A1, B2), (2, brs_a, A2, B1), (-4, brs_a, A2, B2)):
+        # sum_{a b c r s t} F[a,b,r,s] A[a,c,r,t] B[b,c,s,t] / (D[a,b,r,s] D[b,c,s,t])
+        t1 += coef * np.einsum("abrs,acrt,bcst->", F / D, A, B / D, optimize=True)
+    # term2 (mbpt3.f90:64-94): a, b, c, d occupied; r, s virtual
+    ca_db = np.einsum("cadb->abcd", I[o, o, o, o])   # (ca|db)[a, b, c, d]
+    rc_sd = np.einsum("rcsd->cdrs", I[v, o, v, o])   # (rc|sd)[c, d, r, s]
+    sc_rd = np.einsum("scrd->cdrs", I[v, o, v, o])   # (sc|rd)[c, d, r, s]
+    t2 = (2 * np.einsum("abrs,abcd,cdrs->", arbs / D, ca_db, rc_sd / D, optimize=True)
+          - 1 * np.einsum("abrs,abcd,cdrs->", arbs / D, ca_db, sc_rd / D, optimize=True))
+    # term3 (mbpt3.f90:96-126): a, b occupied; r, s, t, u virtual
+    rt_su = np.einsum("rtsu->rstu", I[v, v, v, v])   # (rt|su)[r, s, t, u]
+    ta_ub = np.einsum("taub->abtu", I[v, o, v, o])   # (ta|ub)[a, b, t, u]
+    ua_tb = np.einsum("uatb->abtu", I[v, o, v, o])   # (ua|tb)[a, b, t, u]
+    t3 = (2 * np.einsum("abrs,rstu,abtu->", arbs / D, rt_su, ta_ub / D, optimize=True)
+          - 1 * np.einsum("abrs,rstu,abtu->", arbs / D, rt_su, ua_tb / D, optimize=True))
+    return float(t1 + t2 + t3)
+
+
 def mp2_semidirect(int2, C, lam, nocc, block=8):
     """The same E2 as mbpt2(transform_int2(...)), built from (ia|jb) only, in
     blocks of mu so that no n^4 tensor is formed (for n beyond 120)."""

@@ -12,7 +12,7 @@ CASES = {
     # test_gaussians_molecules.f90
     "H2": dict(atno=[1, 1], xyz=[[0, 0, 0], [0, 0, 1.4]], alpha=1.0, nocc_mp2=1,
                etot=(-1.13128434, 1e-7, ":42"), e2=(-0.0263, 6e-5, ":48"),
-               lam=[(0, -0.595, 6e-4, ":44")]),
+               e3=(-0.00551598, 1e-8, ":52"), lam=[(0, -0.595, 6e-4, ":44")]),
     "N2": dict(atno=[7, 7], xyz=[[0, 0, 0], [0, 0, 2.074]], alpha=1.0, nocc_mp2=None,
                etot=(-108.94268654, 1e-8, ":66"),
                lam=[(4, -0.630, 6e-4, ":68"), (5, -0.612, 6e-4, ":69"), (6, -0.612, 6e-4, ":70")]),
@@ -23,7 +23,7 @@ CASES = {
                   xyz=[[0, 0, 0], [2.05, 0, 0], [-0.683292, 1.932773, 0],
                        [-0.683292, -0.966387, -1.673831], [-0.683292, -0.966387, 1.673831]],
                   alpha=1.0, nocc_mp2=5, etot=(-40.20170036, 1e-8, ":106"),
-                  e2=(-0.16815509, 1e-7, ":114"),
+                  e2=(-0.16815509, 1e-7, ":114"), e3=(-0.01819243, 1e-7, ":116"),
                   lam=[(4, -0.545, 6e-4, ":109"), (4, -0.54451008, 1e-8, ":110")]),
     "CH4_2": dict(atno=[6, 1, 1, 1, 1],
                   xyz=[[0, 0, 0], [_a, -_a, _a], [-_a, _a, _a], [_a, _a, -_a], [-_a, -_a, -_a]],
@@ -36,7 +36,8 @@ CASES = {
                 lam=[(4, -0.41491598, 1e-8, ":158")]),
     "H2O": dict(atno=[8, 1, 1], xyz=[[0, 0, 0], [1.809, 0, 0], [-0.453549, 1.751221, 0]],
                 alpha=1.0, nocc_mp2=5, etot=(-76.02315869, 1e-8, ":183"),
-                e2=(-0.19925995, 1e-6, ":189"), lam=[(4, -0.497, 6e-4, ":186")]),
+                e2=(-0.19925995, 1e-6, ":189"), e3=(-0.00611895, 1e-6, ":191"),
+                lam=[(4, -0.497, 6e-4, ":186")]),
     "FH": dict(atno=[9, 1], xyz=[[0, 0, 0], [1.733, 0, 0]], alpha=1.0, nocc_mp2=None,
                etot=(-100.01134814, 1e-8, ":209"),
                lam=[(3, -0.627, 6e-4, ":211"), (4, -0.627, 6e-4, ":212")]),

@@ -186,3 +186,16 @@ def test_autotune_keeps_energies():
         assert abs(r["E2"] - a["E2"]) < 1e-9
     hf.autotune_clear()
     assert hf.autotune_table() == []
+
+
+@pytest.mark.parametrize("name", [k for k in CASES if "e3" in CASES[k]])
+def test_mbpt3_reference_known_answers(oracle, name):
+    """mbpt3 drop-in on the reference's own H2, CH4 and H2O cases: the asserted
+    E3 (test_gaussians_molecules.f90:52, :116, :191) and the oracle's terms."""
+    c = CASES[name]
+    ref = oracle.rhf_gauss(c["atno"], np.array(c["xyz"], float), nscf=40, alpha=c["alpha"], tolE=1e-10, tolP=1e-8)
+    mo = hf.transform_int2(ref["int2"], ref["C"])
+    e3 = hf.mbpt3(mo, ref["lam"], c["nocc_mp2"])
+    val, tol, _ = c["e3"]
+    assert abs(e3 - val) < tol
+    assert abs(e3 - oracle.mbpt3(mo, ref["lam"], c["nocc_mp2"])) < 1e-12

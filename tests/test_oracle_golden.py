@@ -1,4 +1,4 @@
-"""The oracle's RHF and MBPT2 against every energy that hfsolver's own tests
+"""The oracle's RHF, MBPT2 and MBPT3 against every energy that hfsolver's own tests
 assert for the GTO path (src/tests/test_gaussians_molecules.f90,
 src/tests/test_gaussians_atoms.f90), with the reference's tolerances.  The H2
 total energy is asserted at 1e-7 in the reference (eps, :16,42)."""
@@ -24,6 +24,12 @@ def test_reference_known_answers(oracle, name):
         assert abs(E2 - val) < tol
         # the (ia|jb)-only form used for large molecules gives the same E2
         assert abs(oracle.mp2_semidirect(r["int2"], r["C"], r["lam"], c["nocc_mp2"]) - E2) < 1e-12
+        if "e3" in c:
+            E3 = oracle.mbpt3(mo, r["lam"], c["nocc_mp2"])
+            val, tol, _ = c["e3"]
+            assert abs(E3 - val) < tol
+            if c["atno"] == [1, 1]:
+                assert abs(E2 + E3 - (-0.0319)) < 6e-5  # test_gaussians_molecules.f90:49
 
 
 def test_scf_nonconvergence_is_reported(oracle):
