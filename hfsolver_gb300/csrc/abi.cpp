@@ -74,6 +74,7 @@ void onee_dropin(int which, int nbf, const int* nprim, const int* istart, const 
     check_ptr(out, "output");
     Basis b = basis_from_functions(nbf, nprim, istart, xc, yc, zc, lp, mp, np, n2, coef, alpha);
     Context& ctx = context();
+    std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
     DBuf<double> d((size_t)nbf * nbf, ctx.stream);
     onee_compute(ctx, b, nat, atno, x, y, z, which == 0 ? d.p : nullptr, which == 1 ? d.p : nullptr,
                  which == 2 ? d.p : nullptr);
@@ -84,6 +85,7 @@ void onee_dropin(int which, int nbf, const int* nprim, const int* istart, const 
 void ints_dropin(const Basis& b, double* Ints, double schwarz, EriStats* st)
 {
     Context& ctx = context();
+    std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
     const int64_t np = packed_size(b.nbf);
     DBuf<double> d(np, ctx.stream);
     d.zero();
@@ -115,6 +117,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         std::memset(res, 0, sizeof(*res));
         Basis b = build_basis(natoms, atno, xyz);  // validates the input before any device work
         Context& ctx = ctx_in ? *ctx_in : context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
         cudaStream_t st = ctx.stream;
         ctx.settle_timers();  // drop timers a failed earlier call may have left
         ctx.stat_fock_ms = ctx.stat_tc_ms = ctx.stat_tc_flops = 0;
@@ -291,6 +294,7 @@ int hfgpu_doscf(int n, const double* H, const double* int2, const double* S, int
         check_ptr(H, "H"); check_ptr(int2, "int2"); check_ptr(S, "S");
         check_ptr(C, "C"); check_ptr(P, "P"); check_ptr(lam, "lam"); check_ptr(E0, "E0");
         Context& ctx = context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
         const size_t nn = (size_t)n * n;
         DBuf<double> dH(nn, ctx.stream), dS(nn, ctx.stream), dI(packed_size(n), ctx.stream);
         DBuf<double> dC(nn, ctx.stream), dP(nn, ctx.stream), dL(n, ctx.stream);
@@ -318,6 +322,7 @@ int hfgpu_formG(int n, const double* P, const double* int2, double* G)
         HF_CHECK(n >= 1, HFGPU_ERR_INVALID, "n must be >= 1");
         check_ptr(P, "P"); check_ptr(int2, "int2"); check_ptr(G, "G");
         Context& ctx = context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
         const size_t nn = (size_t)n * n;
         DBuf<double> dP(nn, ctx.stream), dI(packed_size(n), ctx.stream), dG(nn, ctx.stream);
         dP.upload(P, nn);
@@ -337,6 +342,7 @@ int hfgpu_jk(int nbf, const int* nprim, const int* istart, const double* xc, con
         HF_CHECK(schwarz >= 0, HFGPU_ERR_INVALID, "schwarz must be >= 0");
         Basis b = basis_from_functions(nbf, nprim, istart, xc, yc, zc, lp, mp, np, n2, coef, alpha);
         Context& ctx = context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
         const size_t nn = (size_t)nbf * nbf;
         DBuf<double> dI(packed_size(nbf), ctx.stream), dP(nn, ctx.stream), dJ(nn, ctx.stream), dK(nn, ctx.stream);
         dI.zero();
@@ -365,6 +371,7 @@ int hfgpu_mp2_energy(int n, const double* int2, const double* C, const double* l
                  "precision must be HFGPU_MP2_FP64 or HFGPU_MP2_SPLIT_BF16");
         check_ptr(int2, "int2"); check_ptr(C, "C"); check_ptr(lam, "lam"); check_ptr(E2, "E2");
         Context& ctx = context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
         const size_t nn = (size_t)n * n;
         DBuf<double> dI(packed_size(n), ctx.stream), dC(nn, ctx.stream), dL(n, ctx.stream);
         dI.upload(int2, packed_size(n));
@@ -391,6 +398,7 @@ int hfgpu_transform_int2(int n, const double* int2, const double* C, double* moi
         HF_CHECK(n >= 1, HFGPU_ERR_INVALID, "n must be >= 1");
         check_ptr(int2, "int2"); check_ptr(C, "C"); check_ptr(moint2, "moint2");
         Context& ctx = context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
         const int64_t np = packed_size(n);
         DBuf<double> dI(np, ctx.stream), dC((size_t)n * n, ctx.stream), dM(np, ctx.stream);
         dI.upload(int2, np);
@@ -407,6 +415,7 @@ int hfgpu_mbpt2(int n, const double* moint2, const double* lam, int nocc, double
         HF_CHECK(n >= 1 && nocc >= 0 && nocc <= n, HFGPU_ERR_INVALID, "invalid sizes");
         check_ptr(moint2, "moint2"); check_ptr(lam, "lam"); check_ptr(E2, "E2");
         Context& ctx = context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
         const int64_t np = packed_size(n);
         DBuf<double> dM(np, ctx.stream), dL(n, ctx.stream);
         dM.upload(moint2, np);
@@ -421,6 +430,7 @@ int hfgpu_mbpt3(int n, const double* moint2, const double* lam, int nocc, double
         HF_CHECK(n >= 1 && nocc >= 0 && nocc <= n, HFGPU_ERR_INVALID, "invalid sizes");
         check_ptr(moint2, "moint2"); check_ptr(lam, "lam"); check_ptr(E3, "E3");
         Context& ctx = context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
         const int64_t np = packed_size(n);
         DBuf<double> dM(np, ctx.stream), dL(n, ctx.stream);
         dM.upload(moint2, np);
@@ -435,6 +445,7 @@ int hfgpu_dgemm_sliced(int64_t M, int N, int K, const double* A, const double* B
         HF_CHECK(M >= 1 && N >= 1 && K >= 1 && K <= 512, HFGPU_ERR_INVALID, "need M, N >= 1 and 1 <= K <= 512");
         check_ptr(A, "A"); check_ptr(Bt, "Bt"); check_ptr(C, "C");
         Context& ctx = context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
         DBuf<double> dA((size_t)M * K, ctx.stream), dB((size_t)N * K, ctx.stream), dC((size_t)M * N, ctx.stream);
         dA.upload(A, (size_t)M * K);
         dB.upload(Bt, (size_t)N * K);
@@ -451,6 +462,7 @@ int hfgpu_set_stream(void* stream)
 {
     return guard([&] {
         Context& ctx = context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
         ctx.stream = stream ? (cudaStream_t)stream : ctx.own_stream;
         HF_CUBLAS(cublasSetStream(ctx.blas, ctx.stream));
         HF_CUSOLVER(cusolverDnSetStream(ctx.solver, ctx.stream));
@@ -461,7 +473,9 @@ int hfgpu_probe_fp64_tflops(double* tflops)
 {
     return guard([&] {
         check_ptr(tflops, "tflops");
-        *tflops = probe_fp64_tflops(context());
+        Context& ctx = context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
+        *tflops = probe_fp64_tflops(ctx);
     });
 }
 

@@ -5,6 +5,7 @@
 #include <cusolverDn.h>
 
 #include <cstdint>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -134,6 +135,9 @@ struct Context {
     // kernel-time counters, reset by the pipeline entry points
     double stat_fock_ms = 0, stat_tc_ms = 0, stat_tc_flops = 0;
     bool tune = false;  // time candidate kernel shapes on first use (autotune.cpp)
+    // held by every public call for its whole duration: calls from several host
+    // threads on one context run one after another (handles and stream are shared)
+    std::recursive_mutex call_mutex;
 };
 Context& context();  // for the current device
 Context* context_acquire();        // a separate context on the current device (pooled)

@@ -17,6 +17,7 @@
 //       M1[ar][ct] = (ar|ct), M2[ar][ct] = (ac|rt),
 //       P1[ct][bs] = (bs|ct)/D_bc^st, P2[ct][bs] = (bt|cs)/D_bc^st.
 // Matrices are row-major; cuBLAS sees them as their column-major transposes.
+#include <algorithm>
 #include <vector>
 
 #include "internal.h"
@@ -45,13 +46,14 @@ __global__ void mp3_tu_kernel(int o, int v, const double* __restrict__ mo, const
     U[idx] = (2 * arbs - asbr) / D;
 }
 
-// W[rs][tu] = (rt|su) (v^2 x v^2)
-__global__ void mp3_w_kernel(int o, int v, const double* __restrict__ mo, double* W)
+// rows rs0 .. rs0 + nrows of W[rs][tu] = (rt|su) (v^2 columns)
+__global__ void mp3_w_kernel(int o, int v, int64_t rs0, int64_t nrows, const double* __restrict__ mo, double* W)
 {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t v2 = (int64_t)v * v;
-    if (idx >= v2 * v2) return;
-    const int u = (int)(idx % v), t = (int)((idx / v) % v), s = (int)((idx / v2) % v), r = (int)(idx / v2 / v);
+    if (idx >= nrows * v2) return;
+    const int64_t rs = rs0 + idx / v2;
+    const int u = (int)(idx % v), t = (int)((idx / v) % v), s = (int)(rs % v), r = (int)(rs / v);
     W[idx] = mo[pidx(o + r, o + t, o + s, o + u)];
 }
 
@@ -92,11 +94,17 @@ __global__ void mp3_ring_kernel(int o, int v, const double* __restrict__ mo, con
     P1c[idx] = 4 * p1 - 2 * p2;
 }
 
-// C[m][n] = alpha A[m][k] B[k][n] + beta C (row-major)
+// C[m][n] = alpha A[m][k] B[k][n] + beta C (row-major, leading dimensions lda, ldb, ldc)
+static void gemm_rm(Context& ctx, int m, int n, int k, double alpha, const double* A, int64_t lda, const double* B,
+                    int64_t ldb, double beta, double* C, int64_t ldc)
+{
+    HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, k, &alpha, B, (int)ldb, A, (int)lda, &beta, C,
+                          (int)ldc));
+}
 static void gemm_rm(Context& ctx, int m, int n, int k, double alpha, const double* A, const double* B, double beta,
                     double* C)
 {
-    HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, k, &alpha, B, n, A, k, &beta, C, n));
+    gemm_rm(ctx, m, n, k, alpha, A, k, B, n, beta, C, n);
 }
 
 static unsigned grid1(int64_t n) { return (unsigned)((n + 255) / 256); }
@@ -113,12 +121,17 @@ double mbpt3_packed(Context& ctx, int n, const double* d_mo, const double* d_lam
         mp3_tu_kernel<<<grid1(o2 * v2), 256, 0, st>>>(o, v, d_mo, d_lam, T.p, U.p);
         count_launch();
         HF_CUDA(cudaGetLastError());
-        {  // term3
-            DBuf<double> W(v2 * v2, st), Y(o2 * v2, st);
-            mp3_w_kernel<<<grid1(v2 * v2), 256, 0, st>>>(o, v, d_mo, W.p);
-            count_launch();
-            HF_CUDA(cudaGetLastError());
-            gemm_rm(ctx, (int)o2, (int)v2, (int)v2, 1.0, T.p, W.p, 0.0, Y.p);
+        {  // term3: W (v^4) in row blocks of at most 2^28 elements (2 GB)
+            const int64_t rows = std::max<int64_t>(1, std::min<int64_t>(v2, (1ll << 28) / v2));
+            DBuf<double> W(rows * v2, st), Y(o2 * v2, st);
+            for (int64_t rs0 = 0; rs0 < v2; rs0 += rows) {
+                const int64_t nr = std::min(rows, v2 - rs0);
+                mp3_w_kernel<<<grid1(nr * v2), 256, 0, st>>>(o, v, rs0, nr, d_mo, W.p);
+                count_launch();
+                HF_CUDA(cudaGetLastError());
+                // Y += T[:, rs0 .. rs0 + nr] W[rs0 .. rs0 + nr, :]
+                gemm_rm(ctx, (int)o2, (int)v2, (int)nr, 1.0, T.p + rs0, v2, W.p, v2, rs0 == 0 ? 0.0 : 1.0, Y.p, v2);
+            }
             E += device_dot(ctx, o2 * v2, Y.p, U.p);
         }
         {  // term2
