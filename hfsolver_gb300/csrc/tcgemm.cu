@@ -452,11 +452,11 @@ struct SymPairRows {  // rows (q, mu), k = nu of Zt[q * ldz + pair(mu, nu)] (Z t
 // K-major layout the MMA reads (16-byte chunk c of row r at chunk c ^ ((r >> 1) & 3)).
 // B still arrives by TMA.  Each tile first takes its rows' exponents (the
 // largest magnitude of each row, from the same gathers).
-// 512 threads: warp w produces rows 8w .. 8w+7 of every stage, lane k taking
-// column k of each (a packed row's contiguous runs then load coalesced), and
-// fetches the next stage's elements before it stores this one; thread 0 also
-// issues the B loads and the products; the 16 warps share the epilogue (warp w:
-// TMEM lanes 32 (w % 4), columns 16 (w / 4) .. +15).
+// 512 threads: thread t produces row t % 128, K quarter t / 128 (8 elements, one
+// 16-byte chunk per plane) of every stage, fetching the next stage's elements
+// before it stores this one; thread 0 also issues the B loads and the products;
+// the 16 warps share the epilogue (warp w: TMEM lanes 32 (w % 4), columns
+// 16 (w / 4) .. +15).
 constexpr int GATHER_THREADS = 512;
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
@@ -476,15 +476,16 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
     uint64_t* empty = full + STAGES;
     uint32_t* tslot = (uint32_t*)(empty + STAGES);
     __shared__ int s_ok;
-    constexpr int WARPS = GATHER_THREADS / 32;
-    constexpr int RPW = BM / WARPS;  // rows per warp (8): lane k of the warp takes element k of each
-    static_assert(RPW * WARPS == BM && BK == 32, "one lane per K column of a stage");
-    __shared__ typename Src::Row s_rows[BM];
-    __shared__ int s_exp[BM];  // row exponents of the current tile
+    constexpr int PARTS = GATHER_THREADS / BM;  // K parts of a stage per row
+    __shared__ unsigned long long s_amax[PARTS][BM];
+    __shared__ int s_exp[BM];  // row exponents of the current tile (for the epilogue)
     auto sA = [&](int s, int t) { return smem + s * STAGE_BYTES + t * A_TILE; };
     auto sB = [&](int s, int t) { return smem + s * STAGE_BYTES + NSL * A_TILE + t * B_TILE; };
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    constexpr int PK = BK / PARTS;              // elements per thread and stage (8: one 16-byte chunk)
+    static_assert(PK == 8, "one 16-byte chunk per thread and plane");
+    const int prow = tid & (BM - 1), part = tid / BM;
     if (tid == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(&full[s], GATHER_THREADS + 1);  // every producer + the B expect_tx
@@ -510,40 +511,34 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
     for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const int64_t m0 = (tile / ntn) * BM;
         const int n0 = (int)(tile % ntn) * BN;
-        // this warp's rows: contexts in shared memory, exponents from a warp-wide max
-        // (lanes over K: the contiguous runs of a packed row load coalesced)
-        bool live[RPW];
-        int e[RPW];
-#pragma unroll
-        for (int i = 0; i < RPW; ++i) {
-            const int r = warp * RPW + i;
-            const int64_t R = m0 + r;
-            live[i] = R < M;
-            if (lane == 0) s_rows[r] = src.row(live[i] ? R : 0);
-        }
-        __syncwarp();
-#pragma unroll
-        for (int i = 0; i < RPW; ++i) {
-            const int r = warp * RPW + i;
+        const int64_t R = m0 + prow;
+        const bool live = R < M;
+        const typename Src::Row row = src.row(live ? R : 0);
+        // the row's exponent: the PARTS threads of a row take every PARTS-th element
+        // (these reads also bring the row into L2 for the steps below)
+        {
             unsigned long long amax = 0;
-            if (live[i])
-                for (int k = lane; k < K; k += 32) {
+            if (live)
+                for (int k = part; k < K; k += PARTS) {
                     const unsigned long long m =
-                        (unsigned long long)__double_as_longlong(src.at(s_rows[r], k)) & 0x7FFFFFFFFFFFFFFFull;
+                        (unsigned long long)__double_as_longlong(src.at(row, k)) & 0x7FFFFFFFFFFFFFFFull;
                     amax = m > amax ? m : amax;
                 }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const unsigned long long w = __shfl_xor_sync(0xffffffffu, amax, o);
-                amax = w > amax ? w : amax;
-            }
-            e[i] = row_exponent(amax);
-            if (lane == 0) s_exp[r] = e[i];
+            s_amax[part][prow] = amax;
         }
-        // element `lane` of each row for step 0, fetched ahead
-        double x[RPW];
+        __syncthreads();
+        unsigned long long amax = s_amax[0][prow];
 #pragma unroll
-        for (int i = 0; i < RPW; ++i) x[i] = (live[i] && lane < K) ? src.at(s_rows[warp * RPW + i], lane) : 0.0;
+        for (int q = 1; q < PARTS; ++q) amax = s_amax[q][prow] > amax ? s_amax[q][prow] : amax;
+        const int e = row_exponent(amax);
+        if (part == 0) s_exp[prow] = e;
+        // this thread's 8 elements of step 0, fetched ahead
+        double x[PK];
+#pragma unroll
+        for (int j = 0; j < PK; ++j) {
+            const int k = part * PK + j;
+            x[j] = (live && k < K) ? src.at(row, k) : 0.0;
+        }
         for (int ks = 0; ks < ksteps && ok; ++ks) {
             const int64_t g = g0 + ks;
             const int s = (int)(g % STAGES);
@@ -557,22 +552,27 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
                 for (int t = 0; t < NSL; ++t) tma_load_2d(sB(s, t), &tmB, ks * BK, t * b_rows_pad + n0, &full[s]);
                 pend_b = g;
             }
+            uint32_t w[NSL][PK / 2];
 #pragma unroll
-            for (int i = 0; i < RPW; ++i) {
-                const int r = warp * RPW + i;
-                uint16_t d[NSL];
-                digits_bf16(x[i], e[i], d);
-                // 64-byte swizzle: 16-byte chunk c of row r sits at chunk c ^ ((r >> 1) & 3)
-                const int off = r * 64 + (((lane >> 3) ^ ((r >> 1) & 3)) << 4) + ((lane & 7) << 1);
+            for (int j = 0; j < PK; j += 2) {
+                uint16_t d0[NSL], d1[NSL];
+                digits_bf16(x[j], e, d0);
+                digits_bf16(x[j + 1], e, d1);
 #pragma unroll
-                for (int t = 0; t < NSL; ++t) *reinterpret_cast<uint16_t*>(sA(s, t) + off) = d[t];
+                for (int t = 0; t < NSL; ++t) w[t][j / 2] = (uint32_t)d0[t] | ((uint32_t)d1[t] << 16);
             }
-            // the next step's elements are in flight while this one is multiplied
+            // the next step's elements are in flight while this one is stored and multiplied
             if (ks + 1 < ksteps) {
-                const int k = (ks + 1) * BK + lane;
 #pragma unroll
-                for (int i = 0; i < RPW; ++i) x[i] = (live[i] && k < K) ? src.at(s_rows[warp * RPW + i], k) : 0.0;
+                for (int j = 0; j < PK; ++j) {
+                    const int k = (ks + 1) * BK + part * PK + j;
+                    x[j] = (live && k < K) ? src.at(row, k) : 0.0;
+                }
             }
+            const int c = part ^ ((prow >> 1) & 3);  // 64-byte swizzle: chunk c of row r at c ^ ((r >> 1) & 3)
+#pragma unroll
+            for (int t = 0; t < NSL; ++t)
+                *reinterpret_cast<uint4*>(sA(s, t) + prow * 64 + c * 16) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
             // the tensor core reads shared memory through the async proxy
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(&full[s]);
