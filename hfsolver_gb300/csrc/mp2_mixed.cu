@@ -52,10 +52,10 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
     slice_dense(ctx, C1, n1, n, n, B1, SLICE_TILE_B);  // rows of B^T = columns of C1
     slice_dense(ctx, C2, n2, n, n, B2, SLICE_TILE_B);
     const int64_t nq = (int64_t)n1 * n2;
-    // gather-fed GEMMs for steps 1 and 3 when C1's columns fit one output tile
-    // (measured: 8 waters, o = 40, 3.3 ms per block vs 3.5 ms for slicing + TMA;
-    // with two column tiles the rows would be gathered twice and lose)
-    const bool gather = n1 <= SLICE_TILE_B;
+    // gather-fed GEMMs for steps 1 and 3 when C1's columns fit one output tile of
+    // the gather kernel (64 or 80 columns); with two column tiles the rows would be
+    // gathered twice and the slicing + TMA path wins
+    const bool gather = n1 <= 80;
     DBuf<double> Z((size_t)npair * nq, st);
     // steps 1-2 over blocks of pairs
     const int64_t pb = std::max<int64_t>(1, SLICE_BUDGET_ROWS / n);

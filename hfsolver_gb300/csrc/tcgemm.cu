@@ -107,6 +107,13 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
 // kind::f16 instruction descriptor: BF16 x BF16 -> FP32, both K-major, M = 128, N = BN
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 
+__device__ __forceinline__ void umma_d(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+
 __device__ __forceinline__ void umma(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t acc)
 {
     asm volatile(
@@ -459,12 +466,28 @@ struct SymPairRows {  // rows (q, mu), k = nu of Zt[q * ldz + pair(mu, nu)] (Z t
 // 16 (w / 4) .. +15).
 constexpr int GATHER_THREADS = 512;
 
+// Output-tile width and pipeline depth of the gather-fed GEMM: 64 columns with
+// three stages, or 80 columns (16 waters: 80 occupied orbitals in one tile, so
+// the rows are gathered once) with two stages to stay within shared memory.
+template <int GBN_, int GST_>
+struct GatherCfg {
+    static constexpr int GBN = GBN_, GST = GST_;
+    static constexpr int B_T = GBN * BK * 2;
+    static constexpr int STAGE = NSL * (A_TILE + B_T);
+    static constexpr int SMEM = GST * STAGE + 1024 + 128;
+    static constexpr uint32_t IDESC =
+        (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(GBN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+    static_assert(GBN % 16 == 0 && NSL * GBN <= (int)TMEM_COLS, "tile width");
+};
+using Gather64 = GatherCfg<64, 3>;
+using Gather80 = GatherCfg<80, 2>;
+
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
 }
 
-template <class Src>
+template <class Src, class C>
 __global__ void __launch_bounds__(GATHER_THREADS, 1)
     sliced_gemm_gather_kernel(Src src, const __grid_constant__ CUtensorMap tmB,
                               int b_rows_pad, int K, int ksteps, const int* __restrict__ eb, int64_t M, int N,
@@ -472,22 +495,22 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
-    uint64_t* empty = full + STAGES;
-    uint32_t* tslot = (uint32_t*)(empty + STAGES);
+    uint64_t* full = (uint64_t*)(smem + C::GST * C::STAGE);
+    uint64_t* empty = full + C::GST;
+    uint32_t* tslot = (uint32_t*)(empty + C::GST);
     __shared__ int s_ok;
     constexpr int PARTS = GATHER_THREADS / BM;  // K parts of a stage per row
     __shared__ unsigned long long s_amax[PARTS][BM];
     __shared__ int s_exp[BM];  // row exponents of the current tile (for the epilogue)
-    auto sA = [&](int s, int t) { return smem + s * STAGE_BYTES + t * A_TILE; };
-    auto sB = [&](int s, int t) { return smem + s * STAGE_BYTES + NSL * A_TILE + t * B_TILE; };
+    auto sA = [&](int s, int t) { return smem + s * C::STAGE + t * A_TILE; };
+    auto sB = [&](int s, int t) { return smem + s * C::STAGE + NSL * A_TILE + t * C::B_T; };
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     constexpr int PK = BK / PARTS;              // elements per thread and stage (8: one 16-byte chunk)
     static_assert(PK == 8, "one 16-byte chunk per thread and plane");
     const int prow = tid & (BM - 1), part = tid / BM;
     if (tid == 0) {
-        for (int s = 0; s < STAGES; ++s) {
+        for (int s = 0; s < C::GST; ++s) {
             mbar_init(&full[s], GATHER_THREADS + 1);  // every producer + the B expect_tx
             mbar_init(&empty[s], 1);
         }
@@ -510,7 +533,7 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
     int64_t pend_b = -1;       // thread 0: last step whose B load was issued
     for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const int64_t m0 = (tile / ntn) * BM;
-        const int n0 = (int)(tile % ntn) * BN;
+        const int n0 = (int)(tile % ntn) * C::GBN;
         const int64_t R = m0 + prow;
         const bool live = R < M;
         const typename Src::Row row = src.row(live ? R : 0);
@@ -541,13 +564,13 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
         }
         for (int ks = 0; ks < ksteps && ok; ++ks) {
             const int64_t g = g0 + ks;
-            const int s = (int)(g % STAGES);
-            if (g >= STAGES && !mbar_wait(&empty[s], (uint32_t)(((g - STAGES) / STAGES) & 1))) {
+            const int s = (int)(g % C::GST);
+            if (g >= C::GST && !mbar_wait(&empty[s], (uint32_t)(((g - C::GST) / C::GST) & 1))) {
                 ok = false;
                 break;
             }
             if (tid == 0) {
-                mbar_expect_tx(&full[s], NSL * B_TILE);
+                mbar_expect_tx(&full[s], NSL * C::B_T);
 #pragma unroll
                 for (int t = 0; t < NSL; ++t) tma_load_2d(sB(s, t), &tmB, ks * BK, t * b_rows_pad + n0, &full[s]);
                 pend_b = g;
@@ -577,7 +600,7 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(&full[s]);
             if (tid == 0) {
-                if (!mbar_wait(&full[s], (uint32_t)((g / STAGES) & 1))) {
+                if (!mbar_wait(&full[s], (uint32_t)((g / C::GST) & 1))) {
                     ok = false;
                     break;
                 }
@@ -586,12 +609,12 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
                 for (int i = 0; i < NSL; ++i)
 #pragma unroll
                     for (int jj = 0; jj < NSL - i; ++jj) {
-                        const uint32_t dt = tmem + (uint32_t)((i + jj) * BN);
+                        const uint32_t dt = tmem + (uint32_t)((i + jj) * C::GBN);
 #pragma unroll
                         for (int kk = 0; kk < BK / 16; ++kk) {
                             const uint64_t ad = sdesc(su32(sA(s, i)) + kk * 32);
                             const uint64_t bd = sdesc(su32(sB(s, jj)) + kk * 32);
-                            umma(dt, ad, bd, (ks == 0 && i == 0 && kk == 0) ? 0u : 1u);
+                            umma_d(dt, ad, bd, C::IDESC, (ks == 0 && i == 0 && kk == 0) ? 0u : 1u);
                         }
                     }
                 umma_commit(&empty[s]);
@@ -602,22 +625,21 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
         __syncthreads();
         ok = s_ok != 0;
         const int64_t glast = g0 + ksteps - 1;
-        if (ok) ok = mbar_wait(&empty[glast % STAGES], (uint32_t)((glast / STAGES) & 1));
+        if (ok) ok = mbar_wait(&empty[glast % C::GST], (uint32_t)((glast / C::GST) & 1));
         ok = __syncthreads_and(ok);
         if (ok) {
             fence_after();
             // warp w: TMEM lanes 32 (w % 4), 16 columns starting at 16 (w / 4)
             const int64_t r = m0 + (warp & 3) * 32 + lane;
             const int er = s_exp[(warp & 3) * 32 + lane];
-            const int c0 = (warp >> 2) * 16;
-            if (c0 < BN && n0 + c0 < N) {
+            for (int c0 = (warp >> 2) * 16; c0 < C::GBN && n0 + c0 < N; c0 += 64) {
                 long long S[16];
 #pragma unroll
                 for (int i = 0; i < 16; ++i) S[i] = 0;
 #pragma unroll
                 for (int t = 0; t < NSL; ++t) {
                     float f[16];
-                    tmem_ld16(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(t * BN + c0), f);
+                    tmem_ld16(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(t * C::GBN + c0), f);
 #pragma unroll
                     for (int i = 0; i < 16; ++i) S[i] += (long long)__float2int_rn(f[i]) << (SL_BITS * (NSL - 1 - t));
                 }
@@ -639,8 +661,8 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
         if (lane == 0) atomicExch(err, 1);
         if (tid == 0) {
             // B copies and products still in flight land before shared memory and TMEM go (bounded)
-            if (pend_b >= 0) mbar_wait(&full[pend_b % STAGES], (uint32_t)((pend_b / STAGES) & 1));
-            if (last_commit >= 0) mbar_wait(&empty[last_commit % STAGES], (uint32_t)((last_commit / STAGES) & 1));
+            if (pend_b >= 0) mbar_wait(&full[pend_b % C::GST], (uint32_t)((pend_b / C::GST) & 1));
+            if (last_commit >= 0) mbar_wait(&empty[last_commit % C::GST], (uint32_t)((last_commit / C::GST) & 1));
         }
     }
     fence_before();
@@ -769,29 +791,29 @@ void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, Ou
 
 namespace hfgpu {
 
-template <class Src>
-static void gather_gemm(Context& ctx, const Src& src, int64_t M, int K, const Sliced& B, double* out, OutMap om)
+template <class Src, class C>
+static void gather_gemm_cfg(Context& ctx, const Src& src, int64_t M, int K, const Sliced& B, double* out, OutMap om)
 {
     HF_CHECK(K == B.K, HFGPU_ERR_INVALID, "gather GEMM: K mismatch");
-    HF_CHECK(B.rows_pad % BN == 0, HFGPU_ERR_INVALID, "gather GEMM: padding");
+    const int ntn = (int)((B.rows + C::GBN - 1) / C::GBN);
+    HF_CHECK((int64_t)ntn * C::GBN <= B.rows_pad, HFGPU_ERR_INVALID, "gather GEMM: padding");
     static bool attr = false;
     if (!attr) {
-        HF_CUDA(cudaFuncSetAttribute(sliced_gemm_gather_kernel<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     SMEM_BYTES));
+        HF_CUDA(cudaFuncSetAttribute(sliced_gemm_gather_kernel<Src, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     C::SMEM));
         attr = true;
     }
-    const CUtensorMap tb = make_map(B, BN);
+    const CUtensorMap tb = make_map(B, C::GBN);
     DBuf<int> err(1, ctx.stream);
     err.zero();
     cudaEvent_t e0, e1;
     HF_CUDA(cudaEventCreate(&e0));
     HF_CUDA(cudaEventCreate(&e1));
     HF_CUDA(cudaEventRecord(e0, ctx.stream));
-    const int ntn = (int)(B.rows_pad / BN);
     const int64_t ntiles = (M + BM - 1) / BM * ntn;
     HF_CHECK(ntiles > 0, HFGPU_ERR_INVALID, "gather GEMM: empty");
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, ctx.num_sms);
-    sliced_gemm_gather_kernel<Src><<<grid, GATHER_THREADS, SMEM_BYTES, ctx.stream>>>(
+    sliced_gemm_gather_kernel<Src, C><<<grid, GATHER_THREADS, C::SMEM, ctx.stream>>>(
         src, tb, (int)B.rows_pad, K, B.K_pad / BK, B.rexp.p, M, (int)B.rows, out, om, err.p, ntiles, ntn);
     count_launch();
     HF_CUDA(cudaGetLastError());
@@ -806,6 +828,16 @@ static void gather_gemm(Context& ctx, const Src& src, int64_t M, int K, const Sl
     ctx.stat_tc_ms += ms;
     ctx.stat_tc_flops += 2.0 * (NSL * (NSL + 1) / 2) * (double)M * (double)B.rows * (double)K;
     HF_CHECK(h == 0, HFGPU_ERR_CUDA, "gather GEMM: an mbarrier wait timed out");
+}
+
+// widest output tile first: every row is gathered once per column tile
+template <class Src>
+static void gather_gemm(Context& ctx, const Src& src, int64_t M, int K, const Sliced& B, double* out, OutMap om)
+{
+    if (B.rows <= Gather64::GBN)
+        gather_gemm_cfg<Src, Gather64>(ctx, src, M, K, B, out, om);
+    else
+        gather_gemm_cfg<Src, Gather80>(ctx, src, M, K, B, out, om);
 }
 
 void sliced_gemm_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n,
