@@ -23,7 +23,8 @@ class Options(ctypes.Structure):
                 ("tolP", ctypes.c_double), ("scf_accel", ctypes.c_int), ("diis_size", ctypes.c_int),
                 ("schwarz", ctypes.c_double), ("mp2", ctypes.c_int), ("mp2_nocc", ctypes.c_int),
                 ("purify", ctypes.c_int), ("batch_streams", ctypes.c_int), ("incremental", ctypes.c_int),
-                ("autotune", ctypes.c_int), ("guess", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("autotune", ctypes.c_int), ("guess", ctypes.c_int), ("eigensolver", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class Result(ctypes.Structure):
@@ -56,6 +57,8 @@ SIGNATURES = {
     "hfgpu_doscf": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp, _ip]),
     "hfgpu_formG": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
+    "hfgpu_eigh": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, _dp]),
+    "hfgpu_tridiag_eigen": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, _dp]),
     "hfgpu_jk": (ctypes.c_int, _BASIS + [_dp, ctypes.c_double, _dp, _dp]),
     "hfgpu_mp2_energy": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, ctypes.c_int, _dp]),
     "hfgpu_formG_device_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -165,6 +165,33 @@ def mp2_energy(int2, C, lam, Noccupied, precision="fp64"):
     return float(E2[0])
 
 
+def eigh(A, B):
+    """(lam, C) of A C = B C diag(lam) from the lower triangles (linalg.f90 eigh)."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    B = np.asfortranarray(B, dtype=np.float64)
+    n = A.shape[0]
+    if A.shape != (n, n) or B.shape != (n, n):
+        raise ValueError("A and B must be square and of the same size")
+    lam = np.zeros(n)
+    C = np.zeros((n, n), order="F")
+    _check(_lib.lib().hfgpu_eigh(n, A.ctypes.data_as(_dp), B.ctypes.data_as(_dp), _d(lam), C.ctypes.data_as(_dp)))
+    return lam, C
+
+
+def tridiag_eigen(d, e):
+    """(lam, Z) of the symmetric tridiagonal matrix (diagonal d, off-diagonal e); host only."""
+    d = _f64(d)
+    e = _f64(e)
+    n = d.size
+    if n < 1 or e.size != max(n - 1, 0):
+        raise ValueError("need n >= 1 diagonal and n - 1 off-diagonal elements")
+    lam = np.zeros(n)
+    Z = np.zeros((n, n), order="F")
+    _check(_lib.lib().hfgpu_tridiag_eigen(n, _d(d), _d(e) if e.size else _d(np.zeros(1)), _d(lam),
+                                          Z.ctypes.data_as(_dp)))
+    return lam, Z
+
+
 def formG(P, int2):
     """G = J - K/2 from the packed integrals (scf.f90:26-58)."""
     P = np.asfortranarray(P, dtype=np.float64)
@@ -217,6 +244,7 @@ class RHFOptions:
     incremental: bool = False  # Fock builds from screened density differences
     autotune: bool = False     # time candidate kernel shapes on first use, keep the fastest
     guess: str = "core"        # starting density: "core" (P = 0, the reference) | "sad" (atomic densities)
+    eigensolver: str = "own"   # "own" (GPU tridiagonalisation + host tridiagonal solve) | "cusolver" (dsygvd)
 
     def to_c(self):
         o = _lib.Options()
@@ -232,6 +260,7 @@ class RHFOptions:
         o.incremental = 1 if self.incremental else 0
         o.autotune = 1 if self.autotune else 0
         o.guess = {"core": 0, "sad": 1}[self.guess]
+        o.eigensolver = {"own": 0, "cusolver": 1}[self.eigensolver]
         return o
 
 

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "autotune.h"
+#include "eigh.h"
 #include "internal.h"
 #include "scf.h"
 #include "tcgemm.h"
@@ -120,6 +121,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
         cudaStream_t st = ctx.stream;
         ctx.settle_timers();  // drop timers a failed earlier call may have left
+        ctx.trace_begin();
         ctx.stat_fock_ms = ctx.stat_tc_ms = ctx.stat_tc_flops = 0;
         ctx.stat_fock_full_ms = ctx.stat_fock_full_n = 0;
         ctx.tune = opt.autotune != 0 || tune_env_enabled();
@@ -140,12 +142,14 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
             const double one = 1.0;
             HF_CUBLAS(cublasDgeam(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, &one, dT.p, n, &one, dV.p, n, dH.p, n));
         }
+        ctx.trace_mark("one-electron");
         // integrals, resident in HBM for the whole SCF
         DBuf<double> dI(packed_size(n), st);
         dI.zero();
         EriStats es;
         std::unique_ptr<EriPlan, void (*)(EriPlan*)> plan(eri_plan_create(ctx, b, opt.schwarz), eri_plan_destroy);
         res->ms_setup = total.ms();
+        ctx.trace_mark("pairs+schwarz");
         // the packed array feeds MBPT2; the screened quartet blocks feed every Fock build
         eri_compute(ctx, plan.get(), dI.p, true, &es);
         res->ms_eri = es.ms;
@@ -153,6 +157,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         res->n_bf_quartets = es.n_bf_quartets;
         res->n_prim_quartets = es.n_prim_quartets;
         res->eri_flops = es.flops;
+        ctx.trace_mark("eri");
         // SCF
         Timer ts(st);
         DBuf<double> dC(nn, st), dP(nn, st), dL(n, st);
@@ -161,6 +166,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         in.tolE = opt.tolE; in.tolP = opt.tolP; in.alpha = opt.mix_alpha;
         in.accel = opt.scf_accel; in.diis_size = opt.diis_size > 0 ? opt.diis_size : 8;
         in.purify = opt.purify != 0;
+        in.eigensolver = opt.eigensolver;
         in.direct_jk = [](Context& c, void* user, const double* P, double* G, double screen) {
             eri_digest(c, (EriPlan*)user, P, G, screen);
         };
@@ -171,6 +177,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
             dP0.alloc(nn, st);
             sad_guess(ctx, natoms, atno, n, dP0.p);
             in.dP0 = dP0.p;
+            ctx.trace_mark("guess");
         }
         ScfOut so = run_scf(ctx, in, dC.p, dP.p, dL.p);
         res->ms_scf = ts.ms();
@@ -202,13 +209,19 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
                 res->E2 = mp2_energy(ctx, mo, mv, iajb.p, dL.p);
             }
             res->ms_mp2 = tm.ms();
+            ctx.trace_mark("mp2");
         }
         // analytic nuclear gradient at the converged orbitals
-        if (conv && grad) rhf_gradient(ctx, plan.get(), natoms, atno, xyz, dC.p, dL.p, nocc, grad, &res->ms_grad);
+        if (conv && grad) {
+            rhf_gradient(ctx, plan.get(), natoms, atno, xyz, dC.p, dL.p, nocc, grad, &res->ms_grad);
+            ctx.trace_mark("gradient");
+        }
         if (C) dC.download(C, nn);
         if (lam) dL.download(lam, n);
         HF_CUDA(cudaStreamSynchronize(st));
         res->ms_total = total.ms();
+        ctx.trace_mark("download");
+        ctx.trace_report();
         ctx.settle_timers();
         res->ms_fock = ctx.stat_fock_ms;
         res->ms_fock_full = ctx.stat_fock_full_ms;
@@ -314,6 +327,36 @@ int hfgpu_doscf(int n, const double* H, const double* int2, const double* S, int
         return HFGPU_ERR_NOT_CONVERGED;
     }
     return rc;
+}
+
+int hfgpu_eigh(int n, const double* A, const double* B, double* lam, double* C)
+{
+    return guard([&] {
+        HF_CHECK(n >= 1, HFGPU_ERR_INVALID, "n must be >= 1");
+        check_ptr(A, "A"); check_ptr(B, "B"); check_ptr(lam, "lam"); check_ptr(C, "C");
+        Context& ctx = context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
+        const size_t nn = (size_t)n * n;
+        DBuf<double> dA(nn, ctx.stream), dB(nn, ctx.stream), dC(nn, ctx.stream), dL(n, ctx.stream);
+        dA.upload(A, nn);
+        dB.upload(B, nn);
+        eigh_generalized(ctx, n, dA.p, dB.p, dC.p, dL.p, 0);
+        dC.download(C, nn);
+        dL.download(lam, n);
+        HF_CUDA(cudaStreamSynchronize(ctx.stream));
+    });
+}
+
+int hfgpu_tridiag_eigen(int n, const double* d, const double* e, double* lam, double* Z)
+{
+    return guard([&] {
+        HF_CHECK(n >= 1, HFGPU_ERR_INVALID, "n must be >= 1");
+        check_ptr(d, "d"); check_ptr(lam, "lam"); check_ptr(Z, "Z");
+        if (n > 1) check_ptr(e, "e");
+        for (int i = 0; i < n; ++i) HF_CHECK(std::isfinite(d[i]), HFGPU_ERR_INVALID, "non-finite diagonal");
+        for (int i = 0; i + 1 < n; ++i) HF_CHECK(std::isfinite(e[i]), HFGPU_ERR_INVALID, "non-finite off-diagonal");
+        tridiag_eigen(n, d, e, lam, Z, n);
+    });
 }
 
 int hfgpu_formG(int n, const double* P, const double* int2, double* G)

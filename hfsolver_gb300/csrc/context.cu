@@ -1,5 +1,10 @@
 // Per-device context: stream, cuBLAS/cuSOLVER handles, Boys-function grid.
+#include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -116,6 +121,57 @@ void Context::settle_timers()
         cudaEventDestroy(e.b);
     }
     fock_events.clear();
+}
+
+static double host_now_ms()
+{
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+void Context::trace_begin()
+{
+    const char* e = std::getenv("HFGPU_TRACE");
+    trace_on = e && e[0] && e[0] != '0';
+    for (auto& m : trace) cudaEventDestroy(m.ev);
+    trace.clear();
+    trace_mark("begin");
+}
+
+void Context::trace_mark(const char* name)
+{
+    if (!trace_on) return;
+    TraceMark m{name, nullptr, host_now_ms()};
+    HF_CUDA(cudaEventCreate(&m.ev));
+    HF_CUDA(cudaEventRecord(m.ev, stream));
+    trace.push_back(m);
+}
+
+void Context::trace_report()
+{
+    if (!trace_on || trace.size() < 2) return;
+    HF_CUDA(cudaEventSynchronize(trace.back().ev));
+    struct Row {
+        const char* name;
+        double dev, host;
+        int count;
+    };
+    std::vector<Row> rows;
+    for (size_t i = 1; i < trace.size(); ++i) {
+        float ms = 0;
+        HF_CUDA(cudaEventElapsedTime(&ms, trace[i - 1].ev, trace[i].ev));
+        const double host = trace[i].host_ms - trace[i - 1].host_ms;
+        auto it = std::find_if(rows.begin(), rows.end(),
+                               [&](const Row& r) { return std::strcmp(r.name, trace[i].name) == 0; });
+        if (it == rows.end()) rows.push_back({trace[i].name, ms, host, 1});
+        else { it->dev += ms; it->host += host; it->count += 1; }
+    }
+    double tot = 0;
+    for (auto& r : rows) tot += r.dev;
+    std::fprintf(stderr, "hfgpu trace: %-14s %10s %10s %6s\n", "phase", "device ms", "host ms", "count");
+    for (auto& r : rows) std::fprintf(stderr, "hfgpu trace: %-14s %10.3f %10.3f %6d\n", r.name, r.dev, r.host, r.count);
+    std::fprintf(stderr, "hfgpu trace: %-14s %10.3f\n", "total", tot);
+    for (auto& m : trace) cudaEventDestroy(m.ev);
+    trace.clear();
 }
 
 void Context::join()

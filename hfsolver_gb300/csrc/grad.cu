@@ -686,6 +686,7 @@ void eri_gradient(Context& ctx, EriPlan* P, const double* dP, double* d_grad, fl
         HF_CUDA(cudaFuncSetAttribute(eri_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         attr_set[ctx.device & 63] = true;
     }
+    ctx.trace_mark("grad pair data");
     cudaEvent_t e0, e1;
     HF_CUDA(cudaEventCreate(&e0));
     HF_CUDA(cudaEventCreate(&e1));
@@ -808,8 +809,11 @@ void rhf_gradient(Context& ctx, EriPlan* plan, int natoms, const int* atno, cons
         dP.zero();
         dW.zero();
     }
+    ctx.trace_mark("grad densities");
     onee_gradient(ctx, b, natoms, atno, xyz, dP.p, dW.p, dg.p);
+    ctx.trace_mark("grad one-elec");
     eri_gradient(ctx, plan, dP.p, dg.p, nullptr);
+    ctx.trace_mark("grad two-elec");
     std::vector<double> g((size_t)3 * natoms);
     dg.download(g.data(), g.size());
     HF_CUDA(cudaEventRecord(e1, st));

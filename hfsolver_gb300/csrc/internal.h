@@ -135,6 +135,19 @@ struct Context {
     // kernel-time counters, reset by the pipeline entry points
     double stat_fock_ms = 0, stat_tc_ms = 0, stat_tc_flops = 0;
     bool tune = false;  // time candidate kernel shapes on first use (autotune.cpp)
+    // phase trace (HFGPU_TRACE=1 in the environment): an event on `stream` and a
+    // host clock reading at each named point of a pipeline call; trace_report()
+    // prints, per name, the device and host time since the previous point
+    struct TraceMark {
+        const char* name;
+        cudaEvent_t ev;
+        double host_ms;
+    };
+    bool trace_on = false;
+    std::vector<TraceMark> trace;
+    void trace_begin();
+    void trace_mark(const char* name);
+    void trace_report();
     // held by every public call for its whole duration: calls from several host
     // threads on one context run one after another (handles and stream are shared)
     std::recursive_mutex call_mutex;

@@ -51,6 +51,7 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
     Sliced B1, B2, A;
     slice_dense(ctx, C1, n1, n, n, B1, SLICE_TILE_B);  // rows of B^T = columns of C1
     slice_dense(ctx, C2, n2, n, n, B2, SLICE_TILE_B);
+    ctx.trace_mark("mp2 slice C");
     const int64_t nq = (int64_t)n1 * n2;
     // gather-fed GEMMs for steps 1 and 3 when C1's columns fit one output tile of
     // the gather kernel (64 or 80 columns); with two column tiles the rows would be
@@ -70,8 +71,10 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
             slice_packed(ctx, d_int2, pairs.p, p0, np, n, A);
             sliced_gemm(ctx, A, B1, Y.p, OutMap{n, n1}, false);
         }
+        ctx.trace_mark("mp2 step 1");
         slice_dense(ctx, Y.p, np * n1, n, n, A, SLICE_TILE_A);
         sliced_gemm(ctx, A, B2, Z.p + p0 * nq, OutMap{0, n2}, false);  // rows (p, j) -> Z[p][j][b]
+        ctx.trace_mark("mp2 step 2");
     }
     // Z^T: one contiguous row of pairs per q, so that the (q, mu) rows of step 3
     // gather from one L2-resident row instead of one cache line per element
@@ -83,6 +86,7 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
         HF_CUDA(cudaGetLastError());
         Z.release();
     }
+    ctx.trace_mark("mp2 transpose");
     // steps 3-4 over blocks of q
     const int64_t qb = std::max<int64_t>(1, SLICE_BUDGET_ROWS / std::max(n, n1));
     DBuf<double> W((size_t)std::min(qb, nq) * n1 * n, st);
@@ -95,8 +99,10 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
             slice_sympair(ctx, Zt.p + q0 * npair, npair, nqb, n, A);
             sliced_gemm(ctx, A, B1, W.p, OutMap{n, n1}, false);
         }
+        ctx.trace_mark("mp2 step 3");
         slice_dense(ctx, W.p, nqb * n1, n, n, A, SLICE_TILE_A);
         sliced_gemm(ctx, A, B2, T + q0 * n1 * n2, OutMap{0, n2}, false);  // rows (q, i) -> T[q][i][a]
+        ctx.trace_mark("mp2 step 4");
     }
 }
 

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "eigh.h"
 #include "scf.h"
 
 namespace hfgpu {
@@ -118,12 +119,6 @@ __global__ void gersh_kernel(int n, const double* __restrict__ A, double* b)
         b[0] = l;
         b[1] = h;
     }
-}
-
-__global__ void identity_kernel(int n, double* X)
-{
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx < (int64_t)n * n) X[idx] = (idx % n == idx / n) ? 1.0 : 0.0;
 }
 
 // X2 = X X for symmetric X (n <= 1024), upper-triangle 16x16 tiles mirrored;
@@ -372,23 +367,7 @@ struct Purifier {
         tr.alloc(4, st);
         // orthogonaliser X = L^-T from the Cholesky factor S = L L^T (X^T S X = I):
         // a factorisation and a triangular solve instead of an eigensolve
-        DBuf<double> L(nn, st);
-        DBuf<int> info(1, st);
-        HF_CUDA(cudaMemcpyAsync(L.p, dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
-        int lwork = 0;
-        HF_CUSOLVER(cusolverDnDpotrf_bufferSize(ctx.solver, CUBLAS_FILL_MODE_LOWER, n, L.p, n, &lwork));
-        DBuf<double> work(std::max(lwork, 1), st);
-        HF_CUSOLVER(cusolverDnDpotrf(ctx.solver, CUBLAS_FILL_MODE_LOWER, n, L.p, n, work.p, lwork, info.p));
-        int hinfo = 0;
-        info.download(&hinfo, 1);
-        HF_CUDA(cudaStreamSynchronize(st));
-        HF_CHECK(hinfo == 0, HFGPU_ERR_LINALG, "S is not positive definite");
-        identity_kernel<<<nblk(nn), 256, 0, st>>>(n, X.p);
-        count_launch();
-        const double one = 1.0;
-        // L^T X = I
-        HF_CUBLAS(cublasDtrsm(ctx.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n,
-                              n, &one, L.p, n, X.p, n));
+        cholesky_orthogonalizer(ctx, n, dS, X.p);
     }
     // One cooperative launch of the whole recursion on the iterate Xs, with
     // barrier state slot `which` (0: FP32 steps, 1: FP64 steps).
@@ -545,6 +524,7 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
     HF_CHECK(in.nocc >= 0 && in.nocc <= n, HFGPU_ERR_INVALID, "nocc out of range");
     DBuf<double> G(nn, st), F(nn, st), Fw(nn, st), Sw(nn, st), Pold(nn, st), scal(4, st);
     DBuf<int> info(1, st);
+    info.zero();  // written by dsygvd; the own eigensolver reports errors by exception
     if (in.dP0)
         HF_CUDA(cudaMemcpyAsync(dP, in.dP0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
     else
@@ -568,6 +548,34 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
 
     Purifier pur;
     if (in.purify) pur.setup(ctx, n, in.nocc, in.dS);
+    // eigensolver: our own (eigh.cu) where it fits, with the purifier's X or one
+    // made here; cuSOLVER's dsygvd otherwise
+    Eigh eig;
+    DBuf<double> Xown;
+    const double* Xorth = nullptr;
+    const bool own_eigh = in.eigensolver == 0 && Eigh::supported(ctx, n);
+    if (own_eigh) {
+        eig.setup(ctx, n);
+        if (in.purify) {
+            Xorth = pur.X.p;
+        } else {
+            Xown.alloc(nn, st);
+            cholesky_orthogonalizer(ctx, n, in.dS, Xown.p);
+            Xorth = Xown.p;
+        }
+    }
+    // orbitals C (may alias F) and energies of F C = S C diag(lam); with the own
+    // eigensolver only the lowest ncol orbitals are formed (ncol <= 0: all)
+    auto eigh = [&](const double* Fm, double* Cm, int ncol) {
+        if (own_eigh) {
+            eig.solve(ctx, Xorth, Fm, Cm, dLam, ncol);
+            return;
+        }
+        if (Cm != Fm) HF_CUDA(cudaMemcpyAsync(Cm, Fm, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+        HF_CUDA(cudaMemcpyAsync(Sw.p, in.dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+        HF_CUSOLVER(cusolverDnDsygvd(ctx.solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                     n, Cm, n, Sw.p, n, dLam, work.p, lwork, info.p));
+    };
 
     std::vector<double> Escf;
     ScfOut out;
@@ -583,6 +591,8 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
     int since_full = 0;
     bool last_full = true, endgame = false;
     double last_dP = 1.0;
+    const double* last_F = nullptr;  // the Fock matrix of the last eigensolve
+    ctx.trace_mark("scf setup");
     for (int it = 1; it <= in.nscf; ++it) {
         const double* Gcur = G.p;
         if (inc) {
@@ -605,6 +615,7 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
         } else {
             jk_from_packed(ctx, n, in.d_int2, dP, G.p);
         }
+        ctx.trace_mark("fock");
         add_kernel<<<nblk(nn), 256, 0, st>>>(nn, in.dH, Gcur, F.p);
         count_launch();
         reduce(ctx, 0, nn, dP, in.dH, F.p, scal.p);  // E0
@@ -626,6 +637,7 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
             std::vector<double> row(nd);
             bvec.download(row.data(), nd);
             HF_CUDA(cudaStreamSynchronize(st));
+            ctx.trace_mark("diis error");
             for (int k = 0; k < nhist; k++) {
                 B[(size_t)head * nd + k] = row[k];
                 B[(size_t)k * nd + head] = row[k];
@@ -652,6 +664,7 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
                 }
             }
             head = (head + 1) % nd;
+            ctx.trace_mark("diis extrap");
         }
         HF_CUDA(cudaMemcpyAsync(Pold.p, dP, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
         if (in.purify) {
@@ -660,12 +673,12 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
             pur.density(ctx, Fw.p, dP, it > 1 && !endgame && last_dP > 1e-4);
             HF_CUDA(cudaMemsetAsync(info.p, 0, sizeof(int), st));
         } else {
-            HF_CUDA(cudaMemcpyAsync(Fw.p, Fsolve, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
-            HF_CUDA(cudaMemcpyAsync(Sw.p, in.dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
-            HF_CUSOLVER(cusolverDnDsygvd(ctx.solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
-                                         CUBLAS_FILL_MODE_LOWER, n, Fw.p, n, Sw.p, n, dLam, work.p, lwork, info.p));
+            // the density needs the occupied orbitals only; all are formed once converged
+            eigh(Fsolve, Fw.p, in.nocc);
             form_density(ctx, n, in.nocc, Fw.p, dP);
         }
+        last_F = Fsolve;
+        ctx.trace_mark("density");
         reduce(ctx, 1, nn, dP, Pold.p, nullptr, scal.p + 1);  // dP
         double h[2];
         int hinfo = 0;
@@ -673,6 +686,7 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
         info.download(&hinfo, 1);
         HF_CUDA(cudaStreamSynchronize(st));
         if (in.purify) pur.check();
+        ctx.trace_mark("convergence");
         HF_CHECK(hinfo == 0, HFGPU_ERR_LINALG,
                  "eigh: dsygvd returned info = " + std::to_string(hinfo) +
                      (hinfo > n ? " (S is not positive definite)" : ""));
@@ -691,17 +705,17 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
             } else if (dPv < in.tolP && emax - emin < in.tolE) {
                 if (in.purify) {
                     // orbitals and orbital energies of the last Fock matrix, as the reference returns them
-                    HF_CUDA(cudaMemcpyAsync(Sw.p, in.dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
-                    HF_CUSOLVER(cusolverDnDsygvd(ctx.solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
-                                                 CUBLAS_FILL_MODE_LOWER, n, Fw.p, n, Sw.p, n, dLam, work.p, lwork,
-                                                 info.p));
+                    eigh(Fw.p, Fw.p, 0);
                     form_density(ctx, n, in.nocc, Fw.p, dP);
                     info.download(&hinfo, 1);
                     HF_CUDA(cudaStreamSynchronize(st));
                     HF_CHECK(hinfo == 0, HFGPU_ERR_LINALG, "eigh: dsygvd returned info = " + std::to_string(hinfo));
+                } else if (own_eigh && in.nocc < n) {
+                    eigh(last_F, Fw.p, 0);  // the virtual orbitals too (same occupied ones)
                 }
                 HF_CUDA(cudaMemcpyAsync(dC, Fw.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
                 HF_CUDA(cudaStreamSynchronize(st));
+                ctx.trace_mark("orbitals");
                 out.converged = true;
                 return out;
             }
@@ -711,11 +725,9 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
             count_launch();
         }
     }
-    if (in.purify) {  // orbitals of the last Fock matrix
-        HF_CUDA(cudaMemcpyAsync(Sw.p, in.dS, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
-        HF_CUSOLVER(cusolverDnDsygvd(ctx.solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
-                                     CUBLAS_FILL_MODE_LOWER, n, Fw.p, n, Sw.p, n, dLam, work.p, lwork, info.p));
-    }
+    // orbitals of the last Fock matrix
+    if (in.purify) eigh(Fw.p, Fw.p, 0);
+    else if (own_eigh && last_F) eigh(last_F, Fw.p, 0);
     HF_CUDA(cudaMemcpyAsync(dC, Fw.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
     HF_CUDA(cudaStreamSynchronize(st));
     out.converged = false;

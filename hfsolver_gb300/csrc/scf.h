@@ -27,6 +27,9 @@ struct ScfIn {
     int inc_rebuild = 8;
     // starting density (device, n x n); null: P = 0 as in the reference's doscf
     const double* dP0 = nullptr;
+    // eigensolver: 0 = own (eigh.cu: GPU tridiagonalisation, host tridiagonal
+    // solve) where it fits (3 <= n <= 1024), else cuSOLVER dsygvd; 1 = dsygvd
+    int eigensolver = 0;
 };
 
 struct ScfOut {

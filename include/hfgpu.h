@@ -112,6 +112,21 @@ int hfgpu_jk(int nbf, const int *nprim, const int *istart, const double *xcenter
              const int *npower, int n2, const double *coef, const double *alpha, const double *P,
              double schwarz, double *J, double *K);
 
+/* replaces eigh (deigh_generalized, src/linalg.f90:241-275, LAPACK dsygvd): all
+ * eigenvalues lam (ascending) and eigenvectors C (column-major, C^T B C = I) of
+ * A C = B C diag(lam), A symmetric and B symmetric positive definite, both n x n
+ * column-major with only their lower triangles read.  The GPU tridiagonalises
+ * X^T A X (X = L^-T, B = L L^T) in one cooperative kernel and the host solves the
+ * tridiagonal problem; cuSOLVER dsygvd for n < 3 or n > 1024. */
+int hfgpu_eigh(int n, const double *A, const double *B, double *lam, double *C);
+
+/* the host half of hfgpu_eigh: eigenvalues lam (ascending) and orthonormal
+ * eigenvectors Z (n x n, column-major) of the symmetric tridiagonal matrix with
+ * diagonal d (n) and off-diagonal e (n - 1).  Implicit QL for the eigenvalues,
+ * inverse iteration with reorthogonalisation inside clusters for the vectors.
+ * Host memory only; needs no GPU. */
+int hfgpu_tridiag_eigen(int n, const double *d, const double *e, double *lam, double *Z);
+
 /* replaces formG / formG2, src/scf.f90:26-58: G(i,j) = sum_kl P(k,l) [(ij|kl) - (il|kj)/2]
  * from the packed integrals, without the reference's dense TT(n,n,n,n)
  * (src/scf.f90:79-105); P and G column-major n x n. */
@@ -191,7 +206,9 @@ typedef struct {
                             environment sets HFGPU_AUTOTUNE=1 */
     int guess;           /* starting density: 0 = P = 0 (the reference's doscf), 1 = superposition
                             of free-atom densities (closer start, fewer iterations) */
-    int reserved[3];
+    int eigensolver;     /* 0: own generalized eigensolver (as hfgpu_eigh) for 3 <= n <= 1024,
+                            else cuSOLVER dsygvd; 1: cuSOLVER dsygvd always */
+    int reserved[2];
 } hfgpu_options;
 
 typedef struct {
