@@ -57,6 +57,16 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
     // the gather kernel (64 or 80 columns); with two column tiles the rows would be
     // gathered twice and the slicing + TMA path wins
     const bool gather = n1 <= 80;
+    // row maxima of the gathered rows (exponents of their slices), by coalesced
+    // passes over the packed array instead of a second gather inside the GEMM
+    DBuf<unsigned long long> rmax;
+    if (gather) {
+        // reused by steps 3-4 for blocks of at most qb rows q
+        const int64_t qb_rows = std::max<int64_t>(1, SLICE_BUDGET_ROWS / std::max(n, n1));
+        rmax.alloc((size_t)std::max(npair, std::min(qb_rows, nq)) * n, st);
+        packed_row_max(ctx, d_int2, n, rmax.p);
+        ctx.trace_mark("mp2 row max");
+    }
     DBuf<double> Z((size_t)npair * nq, st);
     // steps 1-2 over blocks of pairs
     const int64_t pb = std::max<int64_t>(1, SLICE_BUDGET_ROWS / n);
@@ -66,7 +76,7 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
         // rows (p, la) -> Y[p][j][la]; with one output column tile the ERIs are
         // sliced inside the GEMM (gathered once), else through bf16 planes
         if (gather) {
-            sliced_gemm_packed(ctx, d_int2, pairs.p, p0, np, n, B1, Y.p, OutMap{n, n1});
+            sliced_gemm_packed(ctx, d_int2, pairs.p, p0, np, n, rmax.p, B1, Y.p, OutMap{n, n1});
         } else {
             slice_packed(ctx, d_int2, pairs.p, p0, np, n, A);
             sliced_gemm(ctx, A, B1, Y.p, OutMap{n, n1}, false);
@@ -94,7 +104,8 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
         const int64_t nqb = std::min(qb, nq - q0);
         // rows (q, mu) over nu of Zt[q0 + q][pair(mu, nu)] -> W[q][i][mu]
         if (gather) {
-            sliced_gemm_sympair(ctx, Zt.p + q0 * npair, npair, nqb, n, B1, W.p, OutMap{n, n1});
+            sympair_row_max(ctx, Zt.p + q0 * npair, npair, nqb, n, rmax.p);
+            sliced_gemm_sympair(ctx, Zt.p + q0 * npair, npair, nqb, n, rmax.p, B1, W.p, OutMap{n, n1});
         } else {
             slice_sympair(ctx, Zt.p + q0 * npair, npair, nqb, n, A);
             sliced_gemm(ctx, A, B1, W.p, OutMap{n, n1}, false);

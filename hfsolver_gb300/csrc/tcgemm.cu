@@ -412,6 +412,8 @@ struct PackedRows {  // rows (pair p, la), k = si of the packed (mu nu|la si), p
     const int2* pairs;
     int64_t p0;
     int n;
+    const unsigned long long* rmax = nullptr;  // row maxima |x| (bits) of every pair row, [p][la] (gather GEMM)
+    __device__ unsigned long long row_max(int64_t r) const { return rmax[p0 * n + r]; }
     struct Row {
         int64_t ij, ij_base;  // pair index of (mu, nu) and ij (ij + 1) / 2
         int la;
@@ -435,6 +437,8 @@ struct SymPairRows {  // rows (q, mu), k = nu of Zt[q * ldz + pair(mu, nu)] (Z t
     const double* Zt;
     int64_t ldz;
     int n;
+    const unsigned long long* rmax = nullptr;  // row maxima |x| (bits), [q][mu] (gather GEMM)
+    __device__ unsigned long long row_max(int64_t r) const { return rmax[r]; }
     struct Row {
         const double* z;
         int mu;
@@ -500,7 +504,6 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
     uint32_t* tslot = (uint32_t*)(empty + C::GST);
     __shared__ int s_ok;
     constexpr int PARTS = GATHER_THREADS / BM;  // K parts of a stage per row
-    __shared__ unsigned long long s_amax[PARTS][BM];
     __shared__ int s_exp[BM];  // row exponents of the current tile (for the epilogue)
     auto sA = [&](int s, int t) { return smem + s * C::STAGE + t * A_TILE; };
     auto sB = [&](int s, int t) { return smem + s * C::STAGE + NSL * A_TILE + t * C::B_T; };
@@ -537,22 +540,10 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
         const int64_t R = m0 + prow;
         const bool live = R < M;
         const typename Src::Row row = src.row(live ? R : 0);
-        // the row's exponent: the PARTS threads of a row take every PARTS-th element
-        // (these reads also bring the row into L2 for the steps below)
-        {
-            unsigned long long amax = 0;
-            if (live)
-                for (int k = part; k < K; k += PARTS) {
-                    const unsigned long long m =
-                        (unsigned long long)__double_as_longlong(src.at(row, k)) & 0x7FFFFFFFFFFFFFFFull;
-                    amax = m > amax ? m : amax;
-                }
-            s_amax[part][prow] = amax;
-        }
+        // the row's exponent from the precomputed row maximum (row_max kernels);
+        // the barrier keeps this tile's s_exp writes behind the last epilogue's reads
+        const unsigned long long amax = live ? src.row_max(R) : 0ull;
         __syncthreads();
-        unsigned long long amax = s_amax[0][prow];
-#pragma unroll
-        for (int q = 1; q < PARTS; ++q) amax = s_amax[q][prow] > amax ? s_amax[q][prow] : amax;
         const int e = row_exponent(amax);
         if (part == 0) s_exp[prow] = e;
         // this thread's 8 elements of step 0, fetched ahead
@@ -840,16 +831,134 @@ static void gather_gemm(Context& ctx, const Src& src, int64_t M, int K, const Sl
         gather_gemm_cfg<Src, Gather80>(ctx, src, M, K, B, out, om);
 }
 
-void sliced_gemm_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n,
-                        const Sliced& B, double* out, OutMap om)
+// ---- row maxima for the gather-fed GEMM
+// A row of the gather GEMM is (pair a, la) over si of M[a][pair(la, si)], or
+// (q, mu) over nu of Zt[q][pair(mu, nu)]: the maximum |x| over si is the
+// maximum over the elements of the symmetric pair-row a whose pair contains la.
+// Folding a stored row (elements kl = (la, si), la >= si, kl < len) onto basis
+// indices: a warp takes one run kl = tri(la) .. tri(la) + la (consecutive si,
+// coalesced loads); each element counts for si (shared-memory atomicMax, distinct
+// per lane) and, as the run's maximum, for la.
+__device__ __forceinline__ unsigned long long abs_bits(double x)
 {
-    gather_gemm(ctx, PackedRows{ints, pairs, p0, n}, npairs * n, n, B, out, om);
+    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
 }
 
-void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, const Sliced& B,
-                         double* out, OutMap om)
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 {
-    gather_gemm(ctx, SymPairRows{Zt, ldz, n}, nq * n, n, B, out, om);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// one CTA per stored row a: PACKED rows are the lower triangle of the packed
+// integrals (row a = M[a][0 .. a], at a (a + 1) / 2); otherwise rows of length
+// len_full at src + a * ld.  out[a * n + idx] = folded maximum.
+template <bool PACKED>
+__global__ void row_max_tri_kernel(const double* __restrict__ src, int64_t ld, int64_t len_full, int n,
+                                   unsigned long long* out)
+{
+    extern __shared__ unsigned long long smax[];
+    const int64_t a = blockIdx.x;
+    const double* row = PACKED ? src + a * (a + 1) / 2 : src + a * ld;
+    const int64_t len = PACKED ? a + 1 : len_full;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) smax[i] = 0ull;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int la = warp; la < n; la += nw) {
+        const int64_t t0 = (int64_t)la * (la + 1) / 2;
+        if (t0 >= len) break;  // later runs start further out
+        const int smx = (int)(len - 1 - t0 < la ? len - 1 - t0 : la);
+        unsigned long long m = 0ull;
+        for (int si = lane; si <= smx; si += 32) {
+            const unsigned long long v = abs_bits(__ldg(row + t0 + si));
+            atomicMax(&smax[si], v);
+            m = v > m ? v : m;
+        }
+        m = warp_max_u64(m);
+        if (lane == 0) atomicMax(&smax[la], m);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) out[a * n + i] = smax[i];
+}
+
+// the column part of the packed rows: M[a][b] = M[b][a] for b > a lives in
+// stored row b.  A CTA takes 32 consecutive a (one per lane, so a warp's loads of
+// row b are one 256-byte segment); its warps stride over b.  Each element counts
+// for both indices of pair b, in shared memory laid out [idx][lane] (padded);
+// the block's maxima are merged into out by atomicMax.
+__global__ void row_max_cols_kernel(const double* __restrict__ ints, int64_t npair, int n, unsigned long long* out)
+{
+    extern __shared__ unsigned long long smax[];  // n x 33
+    const int64_t a0 = (int64_t)blockIdx.x * 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = threadIdx.x; i < n * 33; i += blockDim.x) smax[i] = 0ull;
+    __syncthreads();
+    const int64_t a = a0 + lane;
+#pragma unroll 4
+    for (int64_t b = a0 + 1 + warp; b < npair; b += nw) {
+        // pair b = (la, si), la >= si: la = floor((sqrt(8 b + 1) - 1) / 2), corrected
+        int la = (int)((sqrtf(8.0f * (float)b + 1.0f) - 1.0f) * 0.5f);
+        while ((int64_t)la * (la + 1) / 2 > b) --la;
+        while ((int64_t)(la + 1) * (la + 2) / 2 <= b) ++la;
+        const int si = (int)(b - (int64_t)la * (la + 1) / 2);
+        if (a < b) {
+            const unsigned long long v = abs_bits(__ldg(ints + b * (b + 1) / 2 + a));
+            atomicMax(&smax[la * 33 + lane], v);
+            atomicMax(&smax[si * 33 + lane], v);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n * 32; i += blockDim.x) {
+        const int idx = i >> 5, l = i & 31;
+        const unsigned long long v = smax[idx * 33 + l];
+        if (a0 + l < npair && v) atomicMax(out + (a0 + l) * n + idx, v);
+    }
+}
+
+void packed_row_max(Context& ctx, const double* ints, int n, unsigned long long* out)
+{
+    const int64_t npair = (int64_t)n * (n + 1) / 2;
+    row_max_tri_kernel<true><<<(unsigned)npair, 256, n * sizeof(unsigned long long), ctx.stream>>>(ints, 0, 0, n, out);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+    const size_t smem = (size_t)n * 33 * sizeof(unsigned long long);
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(row_max_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    });
+    HF_CHECK(smem <= 200 * 1024, HFGPU_ERR_UNSUPPORTED, "row maxima: basis too large");
+    row_max_cols_kernel<<<(unsigned)((npair + 31) / 32), 1024, smem, ctx.stream>>>(ints, npair, n, out);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+}
+
+void sympair_row_max(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, unsigned long long* out)
+{
+    const int64_t npair = (int64_t)n * (n + 1) / 2;
+    row_max_tri_kernel<false><<<(unsigned)nq, 256, n * sizeof(unsigned long long), ctx.stream>>>(Zt, ldz, npair, n,
+                                                                                              out);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+}
+
+void sliced_gemm_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n,
+                        const unsigned long long* rmax, const Sliced& B, double* out, OutMap om)
+{
+    PackedRows src{ints, pairs, p0, n};
+    src.rmax = rmax;
+    gather_gemm(ctx, src, npairs * n, n, B, out, om);
+}
+
+void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n,
+                         const unsigned long long* rmax, const Sliced& B, double* out, OutMap om)
+{
+    SymPairRows src{Zt, ldz, n};
+    src.rmax = rmax;
+    gather_gemm(ctx, src, nq * n, n, B, out, om);
 }
 
 }  // namespace hfgpu

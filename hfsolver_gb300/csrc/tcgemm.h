@@ -35,10 +35,16 @@ void slice_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int 
 void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, OutMap om, bool accumulate);
 // out = A B^T with A's rows gathered and sliced inside the GEMM (no A planes in
 // HBM): rows (pair p, la) over si of the packed (mu nu|la si) ...
+// (rmax: the rows' maxima from packed_row_max, for all pairs) ...
 void sliced_gemm_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n,
-                        const Sliced& B, double* out, OutMap om);
-// ... or rows (q, mu), q < nq, over nu of Zt[q * ldz + pair(mu, nu)]
-void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, const Sliced& B,
-                         double* out, OutMap om);
+                        const unsigned long long* rmax, const Sliced& B, double* out, OutMap om);
+// ... or rows (q, mu), q < nq, over nu of Zt[q * ldz + pair(mu, nu)] (rmax from
+// sympair_row_max for these nq rows)
+void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n,
+                         const unsigned long long* rmax, const Sliced& B, double* out, OutMap om);
+// max |x| (IEEE bits) of every gather row: packed integrals, rows (pair p, la) of
+// all n (n + 1) / 2 pairs -> out[p * n + la]; Zt rows (q, mu) -> out[q * n + mu]
+void packed_row_max(Context& ctx, const double* ints, int n, unsigned long long* out);
+void sympair_row_max(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, unsigned long long* out);
 
 }  // namespace hfgpu
