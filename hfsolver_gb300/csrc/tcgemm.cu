@@ -412,8 +412,6 @@ struct PackedRows {  // rows (pair p, la), k = si of the packed (mu nu|la si), p
     const int2* pairs;
     int64_t p0;
     int n;
-    const unsigned long long* rmax = nullptr;  // row maxima |x| (bits) of every pair row, [p][la] (gather GEMM)
-    __device__ unsigned long long row_max(int64_t r) const { return rmax[p0 * n + r]; }
     struct Row {
         int64_t ij, ij_base;  // pair index of (mu, nu) and ij (ij + 1) / 2
         int la;
@@ -433,12 +431,73 @@ struct PackedRows {  // rows (pair p, la), k = si of the packed (mu nu|la si), p
     }
 };
 
+// The same rows for the gather-fed GEMM, in 2-D blocks: a warp's 32 rows are 8
+// consecutive pairs x 4 consecutive indices la, a 128-row tile 8 pairs x 16
+// indices.  For a fixed si, the elements with pair(la, si) > pair p sit in one
+// stored row at consecutive p (one 64-byte run per la), and those with
+// pair(la, si) <= p in runs over consecutive la or si: about 40% fewer memory
+// transactions per load than rows running over la alone.  Rows past the last
+// pair or index are dead (not loaded, not stored).
+struct PackedRowsBlocked {
+    const double* ints;
+    const int2* pairs;
+    int64_t p0, np;  // pairs[p0 .. p0 + np)
+    int n, nlg;      // nlg = ceil(n / 16) index groups
+    const unsigned long long* rmax;  // row maxima |x| (bits) of every pair row, [p][la]
+    using Row = PackedRows::Row;
+    __device__ void decode(int64_t r, int64_t& p, int& la) const
+    {
+        const int64_t t = r >> 7;
+        const int q = (int)(r & 127), w = q >> 5, l = q & 31;
+        p = (t / nlg) * 8 + (l & 7);
+        la = (int)(t % nlg) * 16 + w * 4 + (l >> 3);
+    }
+    __device__ bool live(int64_t r) const
+    {
+        int64_t p;
+        int la;
+        decode(r, p, la);
+        return p < np && la < n;
+    }
+    __device__ int64_t out_row(int64_t r) const  // the row's place in p-major order (p n + la)
+    {
+        int64_t p;
+        int la;
+        decode(r, p, la);
+        return p * n + la;
+    }
+    __device__ Row row(int64_t r) const
+    {
+        int64_t p;
+        int la;
+        decode(r, p, la);
+        const int2 mn = pairs[p0 + p];
+        const int64_t ij = (int64_t)mn.x * (mn.x + 1) / 2 + mn.y;
+        return Row{ij, ij * (ij + 1) / 2, la};
+    }
+    __device__ unsigned long long row_max(int64_t r) const
+    {
+        int64_t p;
+        int la;
+        decode(r, p, la);
+        return rmax[(p0 + p) * n + la];
+    }
+    __device__ double at(const Row& w, int si) const
+    {
+        const int c = w.la > si ? w.la : si, d = w.la > si ? si : w.la;
+        const int64_t kl = (int64_t)(c * (c + 1) / 2 + d);
+        return __ldg(ints + (w.ij >= kl ? w.ij_base + kl : kl * (kl + 1) / 2 + w.ij));
+    }
+};
+
 struct SymPairRows {  // rows (q, mu), k = nu of Zt[q * ldz + pair(mu, nu)] (Z transposed: one row per q)
     const double* Zt;
     int64_t ldz;
     int n;
     const unsigned long long* rmax = nullptr;  // row maxima |x| (bits), [q][mu] (gather GEMM)
     __device__ unsigned long long row_max(int64_t r) const { return rmax[r]; }
+    __device__ bool live(int64_t) const { return true; }
+    __device__ int64_t out_row(int64_t r) const { return r; }
     struct Row {
         const double* z;
         int mu;
@@ -538,7 +597,7 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
         const int64_t m0 = (tile / ntn) * BM;
         const int n0 = (int)(tile % ntn) * C::GBN;
         const int64_t R = m0 + prow;
-        const bool live = R < M;
+        const bool live = R < M && src.live(R);
         const typename Src::Row row = src.row(live ? R : 0);
         // the row's exponent from the precomputed row maximum (row_max kernels);
         // the barrier keeps this tile's s_exp writes behind the last epilogue's reads
@@ -634,11 +693,12 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
 #pragma unroll
                     for (int i = 0; i < 16; ++i) S[i] += (long long)__float2int_rn(f[i]) << (SL_BITS * (NSL - 1 - t));
                 }
-                if (r < M) {
+                if (r < M && src.live(r)) {
+                    const int64_t ro = src.out_row(r);
 #pragma unroll
                     for (int i = 0; i < 16; ++i) {
                         const int c = n0 + c0 + i;
-                        if (c < N) out[out_index(om, r, c)] = (double)S[i] * pow2(er + eb[c] - SL_BITS * (NSL + 1));
+                        if (c < N) out[out_index(om, ro, c)] = (double)S[i] * pow2(er + eb[c] - SL_BITS * (NSL + 1));
                     }
                 }
             }
@@ -783,7 +843,8 @@ void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, Ou
 namespace hfgpu {
 
 template <class Src, class C>
-static void gather_gemm_cfg(Context& ctx, const Src& src, int64_t M, int K, const Sliced& B, double* out, OutMap om)
+static void gather_gemm_cfg(Context& ctx, const Src& src, int64_t M, int64_t M_rows, int K, const Sliced& B, double* out,
+                            OutMap om)
 {
     HF_CHECK(K == B.K, HFGPU_ERR_INVALID, "gather GEMM: K mismatch");
     const int ntn = (int)((B.rows + C::GBN - 1) / C::GBN);
@@ -817,18 +878,20 @@ static void gather_gemm_cfg(Context& ctx, const Src& src, int64_t M, int K, cons
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     ctx.stat_tc_ms += ms;
-    ctx.stat_tc_flops += 2.0 * (NSL * (NSL + 1) / 2) * (double)M * (double)B.rows * (double)K;
+    ctx.stat_tc_flops += 2.0 * (NSL * (NSL + 1) / 2) * (double)M_rows * (double)B.rows * (double)K;
     HF_CHECK(h == 0, HFGPU_ERR_CUDA, "gather GEMM: an mbarrier wait timed out");
 }
 
 // widest output tile first: every row is gathered once per column tile
+// (M: rows of the launch, dead ones included; M_rows: the live rows, for the flop count)
 template <class Src>
-static void gather_gemm(Context& ctx, const Src& src, int64_t M, int K, const Sliced& B, double* out, OutMap om)
+static void gather_gemm(Context& ctx, const Src& src, int64_t M, int64_t M_rows, int K, const Sliced& B, double* out,
+                        OutMap om)
 {
     if (B.rows <= Gather64::GBN)
-        gather_gemm_cfg<Src, Gather64>(ctx, src, M, K, B, out, om);
+        gather_gemm_cfg<Src, Gather64>(ctx, src, M, M_rows, K, B, out, om);
     else
-        gather_gemm_cfg<Src, Gather80>(ctx, src, M, K, B, out, om);
+        gather_gemm_cfg<Src, Gather80>(ctx, src, M, M_rows, K, B, out, om);
 }
 
 // ---- row maxima for the gather-fed GEMM
@@ -948,9 +1011,9 @@ void sympair_row_max(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, in
 void sliced_gemm_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n,
                         const unsigned long long* rmax, const Sliced& B, double* out, OutMap om)
 {
-    PackedRows src{ints, pairs, p0, n};
-    src.rmax = rmax;
-    gather_gemm(ctx, src, npairs * n, n, B, out, om);
+    const int nlg = (n + 15) / 16;
+    const PackedRowsBlocked src{ints, pairs, p0, npairs, n, nlg, rmax};
+    gather_gemm(ctx, src, (npairs + 7) / 8 * nlg * 128, npairs * n, n, B, out, om);
 }
 
 void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n,
@@ -958,7 +1021,7 @@ void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq
 {
     SymPairRows src{Zt, ldz, n};
     src.rmax = rmax;
-    gather_gemm(ctx, src, nq * n, n, B, out, om);
+    gather_gemm(ctx, src, nq * n, nq * n, n, B, out, om);
 }
 
 }  // namespace hfgpu
