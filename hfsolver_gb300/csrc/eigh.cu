@@ -318,8 +318,8 @@ void Eigh::solve(Context& ctx, const double* X, const double* F, double* C, doub
     if (ncol <= 0 || ncol > n) ncol = n;
     const double one = 1.0, zero = 0.0, mone = -1.0;
     // F' = X^T F X
-    HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, X, n, F, n, &zero, T1.p, n));
-    HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, T1.p, n, X, n, &zero, Fp.p, n));
+    gemm(ctx, true, false, n, n, n, 1.0, X, n, F, n, 0.0, T1.p, n);
+    gemm(ctx, false, false, n, n, n, 1.0, T1.p, n, X, n, 0.0, Fp.p, n);
     ctx.trace_mark("eigh X^T F X");
     // tridiagonalisation
     {
@@ -348,8 +348,8 @@ void Eigh::solve(Context& ctx, const double* X, const double* F, double* C, doub
     count_launch();
     wy_tw_kernel<<<m, 128, (size_t)m * sizeof(double), st>>>(m, Tinv.p, Tw.p);
     count_launch();
-    HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &one, X, n, V.p, n, &zero, XV.p, n));
-    HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, XV.p, n, Tw.p, m, &zero, M.p, n));
+    gemm(ctx, false, false, n, m, n, 1.0, X, n, V.p, n, 0.0, XV.p, n);
+    gemm(ctx, false, false, n, m, m, 1.0, XV.p, n, Tw.p, m, 0.0, M.p, n);
     HF_CUDA(cudaEventSynchronize(ready));
     ctx.trace_mark("eigh tridiag");
     HF_CHECK(hs->err == 0, HFGPU_ERR_CUDA, "eigh: tridiagonalisation grid barrier timed out");
@@ -359,9 +359,9 @@ void Eigh::solve(Context& ctx, const double* X, const double* F, double* C, doub
     HF_CUDA(cudaMemcpyAsync(T1.p, hZ, sizeof(double) * n * ncol, cudaMemcpyHostToDevice, st));
     HF_CUDA(cudaMemcpyAsync(lam, hlam, sizeof(double) * n, cudaMemcpyHostToDevice, st));
     // W = V^T Z; C = X Z - M W
-    HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_T, CUBLAS_OP_N, m, ncol, n, &one, V.p, n, T1.p, n, &zero, W.p, m));
-    HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, ncol, n, &one, X, n, T1.p, n, &zero, C, n));
-    HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, ncol, m, &mone, M.p, n, W.p, m, &one, C, n));
+    gemm(ctx, true, false, m, ncol, n, 1.0, V.p, n, T1.p, n, 0.0, W.p, m);
+    gemm(ctx, false, false, n, ncol, n, 1.0, X, n, T1.p, n, 0.0, C, n);
+    gemm(ctx, false, false, n, ncol, m, -1.0, M.p, n, W.p, m, 1.0, C, n);
     ctx.trace_mark("eigh back");
     // the next solve writes the host buffers only after its own event, which
     // follows these uploads on the stream

@@ -152,6 +152,10 @@ struct Context {
     // threads on one context run one after another (handles and stream are shared)
     std::recursive_mutex call_mutex;
 };
+// C = alpha op(A) op(B) + beta C in FP64, column-major: the own small-matrix
+// kernel for m, n, k <= 512 (gemm_small.cu), cuBLAS beyond
+void gemm(Context& ctx, bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda,
+          const double* B, int ldb, double beta, double* C, int ldc);
 Context& context();  // for the current device
 Context* context_acquire();        // a separate context on the current device (pooled)
 void context_release(Context* c);  // back to the pool

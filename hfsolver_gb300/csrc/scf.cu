@@ -217,28 +217,32 @@ __device__ __forceinline__ void block_add(double v, double* dst)
 // tr[2k] = tr X_k and tr[2k+1] = ||X_k||_F^2 = tr X_k^2 (X_k symmetric) are
 // reduced while X_k is written, so every block can choose X^2 or 2X - X^2 for
 // step k before it squares.  The iterate alternates between X0 and X1; a block
-// squares its 16 x 16 upper-triangle tile from its 16 rows and 16 columns of X_k,
+// squares its tt x tt upper-triangle tile from its tt rows and tt columns of X_k,
 // staged whole in shared memory (stride n + 1: no bank conflicts).  The result
-// ends in X0.  T = float for the coarse steps of early SCF iterations.
+// ends in X0.  T = float for the coarse steps of early SCF iterations.  The tile
+// edge tt (8 .. 16) is chosen so that the tiles spread the FP64 work evenly over
+// the SMs (sp2_tile).
 template <typename T>
-__global__ void __launch_bounds__(SQ_T* SQ_T) sp2_persistent_kernel(int n, int nocc, T* X0, T* X1, double* tr, int maxs,
-                                                                    double tol_idem, double tol_n, Sp2Sync* sync)
+__global__ void __launch_bounds__(256) sp2_persistent_kernel(int n, int nocc, int tt, T* X0, T* X1, double* tr,
+                                                             int maxs, double tol_idem, double tol_n, Sp2Sync* sync)
 {
     extern __shared__ __align__(16) unsigned char sp2_smem[];
     const int ld = n + 1;
-    T* Ar = (T*)sp2_smem;  // rows i0 .. i0+15 of X_k, all k
-    T* Bc = Ar + SQ_T * ld;  // columns j0 .. j0+15 (rows by symmetry)
-    const int nt = (n + SQ_T - 1) / SQ_T;
+    T* Ar = (T*)sp2_smem;  // rows i0 .. i0+tt-1 of X_k, all k
+    T* Bc = Ar + tt * ld;  // columns j0 .. j0+tt-1 (rows by symmetry)
+    const int nt = (n + tt - 1) / tt;
     int b = blockIdx.x, ti = 0;
     while (b >= nt - ti) {
         b -= nt - ti;
         ++ti;
     }
     const int tj = ti + b;
-    const int i0 = ti * SQ_T, j0 = tj * SQ_T;
-    const int ty = threadIdx.x / SQ_T, tx = threadIdx.x % SQ_T;
+    const int i0 = ti * tt, j0 = tj * tt;
+    // tt x tt workers; the block is rounded up to whole warps for the reductions
+    const bool worker = (int)threadIdx.x < tt * tt;
+    const int ty = threadIdx.x / tt, tx = threadIdx.x % tt;
     const int i = i0 + ty, j = j0 + tx;
-    const bool own = i < n && j < n;
+    const bool own = worker && i < n && j < n;
     for (int it = 0; it < maxs; ++it) {
         T* Xc = (it & 1) ? X1 : X0;
         T* Xn = (it & 1) ? X0 : X1;
@@ -252,16 +256,18 @@ __global__ void __launch_bounds__(SQ_T* SQ_T) sp2_persistent_kernel(int n, int n
             return;
         }
         const bool square = fabs(t1 - nocc) <= fabs(2 * t0 - t1 - nocc);
-        for (int e = threadIdx.x; e < SQ_T * n; e += SQ_T * SQ_T) {
-            const int r = e % SQ_T, k = e / SQ_T;  // r fastest: 16 consecutive doubles of a column
+        for (int e = threadIdx.x; e < tt * n; e += blockDim.x) {
+            const int r = e % tt, k = e / tt;  // r fastest: tt consecutive elements of a column
             Ar[r * ld + k] = (i0 + r < n) ? __ldcg(Xc + i0 + r + (int64_t)k * n) : T(0);
             Bc[r * ld + k] = (j0 + r < n) ? __ldcg(Xc + j0 + r + (int64_t)k * n) : T(0);
         }
         __syncthreads();
         T acc = 0;
-        const T* ar = Ar + ty * ld;
-        const T* bc = Bc + tx * ld;
-        for (int k = 0; k < n; ++k) acc = fma(ar[k], bc[k], acc);
+        if (worker) {
+            const T* ar = Ar + ty * ld;
+            const T* bc = Bc + tx * ld;
+            for (int k = 0; k < n; ++k) acc = fma(ar[k], bc[k], acc);
+        }
         double pt = 0.0, pn = 0.0;
         if (own) {
             const T x = square ? acc : T(2) * __ldcg(Xc + i + (int64_t)j * n) - acc;
@@ -325,32 +331,62 @@ __global__ void sp2_step_kernel(int n, int nocc, const double* __restrict__ t, c
     if (i == j) atomicAdd(tnext, x);
 }
 
-// can all `blocks` blocks of the persistent SP2 kernel be resident at once?
-static bool coop_ok(Context& ctx, int n, unsigned blocks)
+static int sp2_threads(int tt) { return (tt * tt + 31) / 32 * 32; }
+static size_t sp2_smem_bytes(int n, int tt, size_t elem) { return 2 * (size_t)tt * (n + 1) * elem; }
+static unsigned sp2_tiles(int n, int tt)
+{
+    const int nt = (n + tt - 1) / tt;
+    return (unsigned)(nt * (nt + 1) / 2);
+}
+
+// can all blocks of the persistent SP2 kernel with tile edge tt be resident at once?
+static bool coop_ok(Context& ctx, int n, int tt)
 {
     int coop = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx.device) != cudaSuccess || !coop) return false;
-    // the attribute is per process: set it once, for the largest n (512), so that
-    // concurrent molecules of other sizes never lower it under each other
+    // the attribute is per process: set it once, for the largest case (n = 512,
+    // tt = 16), so that concurrent molecules of other sizes never lower it
     static std::once_flag once;
     static bool attr_ok = false;
     std::call_once(once, [] {
-        const int most = (int)(2 * SQ_T * (size_t)(512 + 1) * sizeof(double));
+        const int most = (int)sp2_smem_bytes(512, 16, sizeof(double));
         attr_ok = cudaFuncSetAttribute(sp2_persistent_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        most) == cudaSuccess &&
                   cudaFuncSetAttribute(sp2_persistent_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        most) == cudaSuccess;
     });
-    const size_t smem = 2 * SQ_T * (size_t)(n + 1) * sizeof(double);
     if (!attr_ok || n > 512) return false;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sp2_persistent_kernel<double>, SQ_T * SQ_T, smem) !=
-        cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sp2_persistent_kernel<double>, sp2_threads(tt),
+                                                      sp2_smem_bytes(n, tt, sizeof(double))) != cudaSuccess)
         return false;
-    return (int64_t)per_sm * ctx.num_sms >= (int64_t)blocks;
+    return (int64_t)per_sm * ctx.num_sms >= (int64_t)sp2_tiles(n, tt);
+}
+
+// tile edge of the persistent SP2 kernel.  Per step, the busiest SM squares
+// ceil(tiles / SMs) tiles of tt^2 length-n dot products (~n/2 cycles each at
+// two FP64 FMAs per cycle), and every block adds ~40 cycles of atomics at the
+// barrier and the trace sums; take the tt in 8 .. 16 with the least of both
+// among those whose grid can be co-resident.  0: none fits.
+static int sp2_tile(Context& ctx, int n)
+{
+    int best = 0;
+    int64_t best_cost = 0;
+    for (int tt = 16; tt >= 8; --tt) {
+        if (!coop_ok(ctx, n, tt)) continue;
+        const int64_t tiles = sp2_tiles(n, tt);
+        const int64_t per_sm = (tiles + ctx.num_sms - 1) / ctx.num_sms;
+        const int64_t cost = per_sm * tt * tt * n / 2 + 40 * tiles;
+        if (best == 0 || cost < best_cost) {
+            best = tt;
+            best_cost = cost;
+        }
+    }
+    return best;
 }
 
 struct Purifier {
     int n = 0, nocc = 0;
+    int tile = 0;  // persistent-kernel tile edge (sp2_tile); -1: per-step fallback
     DBuf<double> X, T1, T2, B, tr;  // orthogonaliser S^-1/2 and work
     DBuf<float> Xf;                 // FP32 iterate of the coarse steps
     DBuf<Sp2Sync> sync;
@@ -372,17 +408,16 @@ struct Purifier {
     // One cooperative launch of the whole recursion on the iterate Xs, with
     // barrier state slot `which` (0: FP32 steps, 1: FP64 steps).
     template <typename T>
-    void run_persistent(Context& ctx, T* Xs, T* Xw, double* trs, int maxs, double tol_idem, double tol_n,
-                        unsigned tiles, int which)
+    void run_persistent(Context& ctx, T* Xs, T* Xw, double* trs, int maxs, double tol_idem, double tol_n, int tt,
+                        int which)
     {
         cudaStream_t st = ctx.stream;
         HF_CUDA(cudaMemsetAsync(sync.p + which, 0, sizeof(Sp2Sync), st));
-        int n_ = n, nocc_ = nocc;
+        int n_ = n, nocc_ = nocc, tt_ = tt;
         Sp2Sync* sp = sync.p + which;
-        void* args[] = {&n_, &nocc_, &Xs, &Xw, &trs, &maxs, &tol_idem, &tol_n, &sp};
-        const size_t smem = 2 * SQ_T * (size_t)(n + 1) * sizeof(T);
-        HF_CUDA(cudaLaunchCooperativeKernel((const void*)sp2_persistent_kernel<T>, dim3(tiles), dim3(SQ_T * SQ_T),
-                                            args, smem, st));
+        void* args[] = {&n_, &nocc_, &tt_, &Xs, &Xw, &trs, &maxs, &tol_idem, &tol_n, &sp};
+        HF_CUDA(cudaLaunchCooperativeKernel((const void*)sp2_persistent_kernel<T>, dim3(sp2_tiles(n, tt)),
+                                            dim3(sp2_threads(tt)), args, sp2_smem_bytes(n, tt, sizeof(T)), st));
         count_launch();
     }
     // The outcome of the last cooperative purification (barrier timeouts, final
@@ -417,8 +452,8 @@ struct Purifier {
         const int64_t nn = (int64_t)n * n;
         cudaStream_t st = ctx.stream;
         const double one = 1.0, zero = 0.0, two = 2.0;
-        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, X.p, n, dF, n, &zero, T1.p, n));
-        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, T1.p, n, X.p, n, &zero, T2.p, n));
+        gemm(ctx, true, false, n, n, n, 1.0, X.p, n, dF, n, 0.0, T1.p, n);
+        gemm(ctx, false, false, n, n, n, 1.0, T1.p, n, X.p, n, 0.0, T2.p, n);
         gersh_kernel<<<1, 1024, 0, st>>>(n, T2.p, B.p);
         count_launch();
         // per-step trace slots [step][tr X, tr X^2], zeroed once
@@ -427,11 +462,16 @@ struct Purifier {
         HF_CUDA(cudaMemsetAsync(tr.p, 0, sizeof(double) * 4 * (MAXS + 1), st));
         sp2_init2_kernel<<<nblk(nn), 256, 0, st>>>(n, T2.p, B.p, T1.p, tr.p);  // T1 = iterate
         count_launch();
+        ctx.trace_mark("sp2 X^T F X");
         const int nt = (n + SQ_T - 1) / SQ_T;
-        const unsigned tiles = (unsigned)(nt * (nt + 1) / 2);
+        const unsigned tiles = (unsigned)(nt * (nt + 1) / 2);  // of the per-step fallback
         double h[2] = {0, 1};
         bool done = false;
-        if (coop_ok(ctx, n, tiles)) {
+        if (tile == 0) {
+            tile = sp2_tile(ctx, n);
+            if (tile == 0) tile = -1;
+        }
+        if (tile > 0) {
             if (!sync.p) {
                 sync.alloc(2, st);
                 HF_CUDA(cudaMemsetAsync(sync.p, 0, 2 * sizeof(Sp2Sync), st));
@@ -444,7 +484,8 @@ struct Purifier {
                 double* trf = tr.p + 2 * (MAXS + 1);
                 convert_trace_kernel<double, float><<<nblk(nn), 256, 0, st>>>(n, T1.p, Xf.p, trf);
                 count_launch();
-                run_persistent<float>(ctx, Xf.p, Xf.p + nn, trf, MAXS, 1e-3, 1e-3, tiles, 0);
+                run_persistent<float>(ctx, Xf.p, Xf.p + nn, trf, MAXS, 1e-3, 1e-3, tile, 0);
+                ctx.trace_mark("sp2 fp32");
                 HF_CUDA(cudaMemsetAsync(tr64, 0, sizeof(double) * 2 * (MAXS + 1), st));
                 convert_trace_kernel<float, double><<<nblk(nn), 256, 0, st>>>(n, Xf.p, T1.p, tr64);
                 count_launch();
@@ -452,7 +493,8 @@ struct Purifier {
                 HF_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(Sp2Sync), st));  // no FP32 phase this time
             }
             // T2 (X^T F X) is free once the first iterate is built: the second buffer
-            run_persistent<double>(ctx, T1.p, T2.p, tr64, MAXS, 1e-13 * n, 1e-6, tiles, 1);
+            run_persistent<double>(ctx, T1.p, T2.p, tr64, MAXS, 1e-13 * n, 1e-6, tile, 1);
+            ctx.trace_mark("sp2 fp64");
             HF_CUDA(cudaMemcpyAsync(hsync, sync.p, 2 * sizeof(Sp2Sync), cudaMemcpyDeviceToHost, st));
             HF_CUDA(cudaMemcpyAsync(htr, tr64, 2 * (MAXS + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
             pending = true;
@@ -474,8 +516,8 @@ struct Purifier {
             }
         }
         HF_CHECK(fabs(h[0] - nocc) < 1e-6, HFGPU_ERR_LINALG, "density purification did not converge (no gap?)");
-        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, X.p, n, T1.p, n, &zero, T2.p, n));
-        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, n, &two, T2.p, n, X.p, n, &zero, dP, n));
+        gemm(ctx, false, false, n, n, n, 1.0, X.p, n, T1.p, n, 0.0, T2.p, n);
+        gemm(ctx, false, true, n, n, n, 2.0, T2.p, n, X.p, n, 0.0, dP, n);
     }
 };
 
@@ -487,7 +529,7 @@ static void form_density(Context& ctx, int n, int nocc, const double* C, double*
         HF_CUDA(cudaMemsetAsync(P, 0, sizeof(double) * n * n, ctx.stream));
         return;
     }
-    HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, nocc, &two, C, n, C, n, &zero, P, n));
+    gemm(ctx, false, true, n, n, nocc, 2.0, C, n, C, n, 0.0, P, n);
 }
 
 // small dense solve with partial pivoting (DIIS system, size <= 21)
@@ -625,8 +667,8 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
         if (diis && (it >= 2 || in.dP0)) {
             const double one = 1.0, zero = 0.0;
             // error = F P S - S P F = Y - Y^T with Y = F P S
-            HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, F.p, n, dP, n, &zero, G.p, n));
-            HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, G.p, n, in.dS, n, &zero, Y.p, n));
+            gemm(ctx, false, false, n, n, n, 1.0, F.p, n, dP, n, 0.0, G.p, n);
+            gemm(ctx, false, false, n, n, n, 1.0, G.p, n, in.dS, n, 0.0, Y.p, n);
             double* ek = Eh.p + (size_t)head * nn;
             comm_kernel<<<nblk(nn), 256, 0, st>>>(n, Y.p, ek);
             count_launch();
