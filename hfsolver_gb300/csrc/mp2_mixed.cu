@@ -59,7 +59,7 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
     const bool gather = n1 <= 80;
     // row maxima of the gathered rows (exponents of their slices), by coalesced
     // passes over the packed array instead of a second gather inside the GEMM
-    DBuf<unsigned long long> rmax;
+    DBuf<unsigned> rmax;
     if (gather) {
         // reused by steps 3-4 for blocks of at most qb rows q
         const int64_t qb_rows = std::max<int64_t>(1, SLICE_BUDGET_ROWS / std::max(n, n1));

@@ -443,8 +443,12 @@ struct PackedRowsBlocked {
     const int2* pairs;
     int64_t p0, np;  // pairs[p0 .. p0 + np)
     int n, nlg;      // nlg = ceil(n / 16) index groups
-    const unsigned long long* rmax;  // row maxima |x| (bits) of every pair row, [p][la]
-    using Row = PackedRows::Row;
+    const unsigned* rmax;  // row maxima (upper word of |x|) of every pair row, [p][la]
+    struct Row {
+        int ij;          // pair index of (mu, nu) (< 2^31 for n <= 512)
+        int64_t ij_base;  // ij (ij + 1) / 2
+        int la;
+    };
     __device__ void decode(int64_t r, int64_t& p, int& la) const
     {
         const int64_t t = r >> 7;
@@ -472,21 +476,23 @@ struct PackedRowsBlocked {
         int la;
         decode(r, p, la);
         const int2 mn = pairs[p0 + p];
-        const int64_t ij = (int64_t)mn.x * (mn.x + 1) / 2 + mn.y;
-        return Row{ij, ij * (ij + 1) / 2, la};
+        const int ij = mn.x * (mn.x + 1) / 2 + mn.y;
+        return Row{ij, ((int64_t)ij * (ij + 1)) >> 1, la};
     }
     __device__ unsigned long long row_max(int64_t r) const
     {
         int64_t p;
         int la;
         decode(r, p, la);
-        return rmax[(p0 + p) * n + la];
+        return (unsigned long long)rmax[(p0 + p) * n + la] << 32;
     }
+    // 32-bit index arithmetic up to the final address (64-bit compares would run
+    // on the FP64 pipe)
     __device__ double at(const Row& w, int si) const
     {
-        const int c = w.la > si ? w.la : si, d = w.la > si ? si : w.la;
-        const int64_t kl = (int64_t)(c * (c + 1) / 2 + d);
-        return __ldg(ints + (w.ij >= kl ? w.ij_base + kl : kl * (kl + 1) / 2 + w.ij));
+        const int c = max(w.la, si), d = min(w.la, si);
+        const int kl = c * (c + 1) / 2 + d;
+        return __ldg(ints + (w.ij >= kl ? w.ij_base + kl : (((int64_t)kl * (kl + 1)) >> 1) + w.ij));
     }
 };
 
@@ -494,8 +500,8 @@ struct SymPairRows {  // rows (q, mu), k = nu of Zt[q * ldz + pair(mu, nu)] (Z t
     const double* Zt;
     int64_t ldz;
     int n;
-    const unsigned long long* rmax = nullptr;  // row maxima |x| (bits), [q][mu] (gather GEMM)
-    __device__ unsigned long long row_max(int64_t r) const { return rmax[r]; }
+    const unsigned* rmax = nullptr;  // row maxima (upper word of |x|), [q][mu] (gather GEMM)
+    __device__ unsigned long long row_max(int64_t r) const { return (unsigned long long)rmax[r] << 32; }
     __device__ bool live(int64_t) const { return true; }
     __device__ int64_t out_row(int64_t r) const { return r; }
     struct Row {
@@ -898,22 +904,20 @@ static void gather_gemm(Context& ctx, const Src& src, int64_t M, int64_t M_rows,
 // A row of the gather GEMM is (pair a, la) over si of M[a][pair(la, si)], or
 // (q, mu) over nu of Zt[q][pair(mu, nu)]: the maximum |x| over si is the
 // maximum over the elements of the symmetric pair-row a whose pair contains la.
+// Only its exponent is used (row_exponent), so the maxima are kept as the upper
+// 32 bits of |x| (sign cleared), which order like |x| down to the exponent and
+// stay on 32-bit integer instructions (64-bit compares and conversions run on
+// this GPU's narrow FP64 pipe).
 // Folding a stored row (elements kl = (la, si), la >= si, kl < len) onto basis
 // indices: a warp takes one run kl = tri(la) .. tri(la) + la (consecutive si,
-// coalesced loads); each element counts for si (shared-memory atomicMax, distinct
-// per lane) and, as the run's maximum, for la.
-__device__ __forceinline__ unsigned long long abs_bits(double x)
-{
-    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
-}
+// coalesced loads); each element counts for si (shared-memory atomicMax,
+// distinct per lane) and, as the run's maximum, for la.
+__device__ __forceinline__ unsigned abs_hi(double x) { return (unsigned)__double2hiint(x) & 0x7FFFFFFFu; }
 
-__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
+__device__ __forceinline__ unsigned warp_max_u32(unsigned v)
 {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
-        v = w > v ? w : v;
-    }
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
 
@@ -921,31 +925,30 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 // integrals (row a = M[a][0 .. a], at a (a + 1) / 2); otherwise rows of length
 // len_full at src + a * ld.  out[a * n + idx] = folded maximum.
 template <bool PACKED>
-__global__ void row_max_tri_kernel(const double* __restrict__ src, int64_t ld, int64_t len_full, int n,
-                                   unsigned long long* out)
+__global__ void row_max_tri_kernel(const double* __restrict__ src, int64_t ld, int len_full, int n, unsigned* out)
 {
-    extern __shared__ unsigned long long smax[];
-    const int64_t a = blockIdx.x;
-    const double* row = PACKED ? src + a * (a + 1) / 2 : src + a * ld;
-    const int64_t len = PACKED ? a + 1 : len_full;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) smax[i] = 0ull;
+    extern __shared__ unsigned smax32[];
+    const int a = blockIdx.x;
+    const double* row = PACKED ? src + (int64_t)a * (a + 1) / 2 : src + (int64_t)a * ld;
+    const int len = PACKED ? a + 1 : len_full;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) smax32[i] = 0u;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int la = warp; la < n; la += nw) {
-        const int64_t t0 = (int64_t)la * (la + 1) / 2;
+        const int t0 = la * (la + 1) / 2;
         if (t0 >= len) break;  // later runs start further out
-        const int smx = (int)(len - 1 - t0 < la ? len - 1 - t0 : la);
-        unsigned long long m = 0ull;
+        const int smx = min(len - 1 - t0, la);
+        unsigned m = 0u;
         for (int si = lane; si <= smx; si += 32) {
-            const unsigned long long v = abs_bits(__ldg(row + t0 + si));
-            atomicMax(&smax[si], v);
-            m = v > m ? v : m;
+            const unsigned v = abs_hi(__ldg(row + t0 + si));
+            atomicMax(&smax32[si], v);
+            m = max(m, v);
         }
-        m = warp_max_u64(m);
-        if (lane == 0) atomicMax(&smax[la], m);
+        m = warp_max_u32(m);
+        if (lane == 0) atomicMax(&smax32[la], m);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) out[a * n + i] = smax[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) out[(int64_t)a * n + i] = smax32[i];
 }
 
 // the column part of the packed rows: M[a][b] = M[b][a] for b > a lives in
@@ -953,42 +956,42 @@ __global__ void row_max_tri_kernel(const double* __restrict__ src, int64_t ld, i
 // row b are one 256-byte segment); its warps stride over b.  Each element counts
 // for both indices of pair b, in shared memory laid out [idx][lane] (padded);
 // the block's maxima are merged into out by atomicMax.
-__global__ void row_max_cols_kernel(const double* __restrict__ ints, int64_t npair, int n, unsigned long long* out)
+__global__ void row_max_cols_kernel(const double* __restrict__ ints, int npair, int n, unsigned* out)
 {
-    extern __shared__ unsigned long long smax[];  // n x 33
-    const int64_t a0 = (int64_t)blockIdx.x * 32;
+    extern __shared__ unsigned smax32[];  // n x 33
+    const int a0 = blockIdx.x * 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int i = threadIdx.x; i < n * 33; i += blockDim.x) smax[i] = 0ull;
+    for (int i = threadIdx.x; i < n * 33; i += blockDim.x) smax32[i] = 0u;
     __syncthreads();
-    const int64_t a = a0 + lane;
+    const int a = a0 + lane;
 #pragma unroll 4
-    for (int64_t b = a0 + 1 + warp; b < npair; b += nw) {
+    for (int b = a0 + 1 + warp; b < npair; b += nw) {
         // pair b = (la, si), la >= si: la = floor((sqrt(8 b + 1) - 1) / 2), corrected
         int la = (int)((sqrtf(8.0f * (float)b + 1.0f) - 1.0f) * 0.5f);
-        while ((int64_t)la * (la + 1) / 2 > b) --la;
-        while ((int64_t)(la + 1) * (la + 2) / 2 <= b) ++la;
-        const int si = (int)(b - (int64_t)la * (la + 1) / 2);
+        while (la * (la + 1) / 2 > b) --la;
+        while ((la + 1) * (la + 2) / 2 <= b) ++la;
+        const int si = b - la * (la + 1) / 2;
         if (a < b) {
-            const unsigned long long v = abs_bits(__ldg(ints + b * (b + 1) / 2 + a));
-            atomicMax(&smax[la * 33 + lane], v);
-            atomicMax(&smax[si * 33 + lane], v);
+            const unsigned v = abs_hi(__ldg(ints + (int64_t)b * (b + 1) / 2 + a));
+            atomicMax(&smax32[la * 33 + lane], v);
+            atomicMax(&smax32[si * 33 + lane], v);
         }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < n * 32; i += blockDim.x) {
         const int idx = i >> 5, l = i & 31;
-        const unsigned long long v = smax[idx * 33 + l];
-        if (a0 + l < npair && v) atomicMax(out + (a0 + l) * n + idx, v);
+        const unsigned v = smax32[idx * 33 + l];
+        if (a0 + l < npair && v) atomicMax(out + (int64_t)(a0 + l) * n + idx, v);
     }
 }
 
-void packed_row_max(Context& ctx, const double* ints, int n, unsigned long long* out)
+void packed_row_max(Context& ctx, const double* ints, int n, unsigned* out)
 {
-    const int64_t npair = (int64_t)n * (n + 1) / 2;
-    row_max_tri_kernel<true><<<(unsigned)npair, 256, n * sizeof(unsigned long long), ctx.stream>>>(ints, 0, 0, n, out);
+    const int npair = n * (n + 1) / 2;
+    row_max_tri_kernel<true><<<(unsigned)npair, 256, n * sizeof(unsigned), ctx.stream>>>(ints, 0, 0, n, out);
     count_launch();
     HF_CUDA(cudaGetLastError());
-    const size_t smem = (size_t)n * 33 * sizeof(unsigned long long);
+    const size_t smem = (size_t)n * 33 * sizeof(unsigned);
     static std::once_flag once;
     std::call_once(once, [] {
         cudaFuncSetAttribute(row_max_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -999,25 +1002,24 @@ void packed_row_max(Context& ctx, const double* ints, int n, unsigned long long*
     HF_CUDA(cudaGetLastError());
 }
 
-void sympair_row_max(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, unsigned long long* out)
+void sympair_row_max(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, unsigned* out)
 {
-    const int64_t npair = (int64_t)n * (n + 1) / 2;
-    row_max_tri_kernel<false><<<(unsigned)nq, 256, n * sizeof(unsigned long long), ctx.stream>>>(Zt, ldz, npair, n,
-                                                                                              out);
+    const int npair = n * (n + 1) / 2;
+    row_max_tri_kernel<false><<<(unsigned)nq, 256, n * sizeof(unsigned), ctx.stream>>>(Zt, ldz, npair, n, out);
     count_launch();
     HF_CUDA(cudaGetLastError());
 }
 
 void sliced_gemm_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n,
-                        const unsigned long long* rmax, const Sliced& B, double* out, OutMap om)
+                        const unsigned* rmax, const Sliced& B, double* out, OutMap om)
 {
     const int nlg = (n + 15) / 16;
     const PackedRowsBlocked src{ints, pairs, p0, npairs, n, nlg, rmax};
     gather_gemm(ctx, src, (npairs + 7) / 8 * nlg * 128, npairs * n, n, B, out, om);
 }
 
-void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n,
-                         const unsigned long long* rmax, const Sliced& B, double* out, OutMap om)
+void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, const unsigned* rmax,
+                         const Sliced& B, double* out, OutMap om)
 {
     SymPairRows src{Zt, ldz, n};
     src.rmax = rmax;

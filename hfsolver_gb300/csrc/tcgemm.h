@@ -37,14 +37,15 @@ void sliced_gemm(Context& ctx, const Sliced& A, const Sliced& B, double* out, Ou
 // HBM): rows (pair p, la) over si of the packed (mu nu|la si) ...
 // (rmax: the rows' maxima from packed_row_max, for all pairs) ...
 void sliced_gemm_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n,
-                        const unsigned long long* rmax, const Sliced& B, double* out, OutMap om);
+                        const unsigned* rmax, const Sliced& B, double* out, OutMap om);
 // ... or rows (q, mu), q < nq, over nu of Zt[q * ldz + pair(mu, nu)] (rmax from
 // sympair_row_max for these nq rows)
-void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n,
-                         const unsigned long long* rmax, const Sliced& B, double* out, OutMap om);
-// max |x| (IEEE bits) of every gather row: packed integrals, rows (pair p, la) of
-// all n (n + 1) / 2 pairs -> out[p * n + la]; Zt rows (q, mu) -> out[q * n + mu]
-void packed_row_max(Context& ctx, const double* ints, int n, unsigned long long* out);
-void sympair_row_max(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, unsigned long long* out);
+void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, const unsigned* rmax,
+                         const Sliced& B, double* out, OutMap om);
+// max |x| of every gather row, as the upper 32 bits of |x| (enough for its
+// exponent): packed integrals, rows (pair p, la) of all n (n + 1) / 2 pairs ->
+// out[p * n + la]; Zt rows (q, mu) -> out[q * n + mu]
+void packed_row_max(Context& ctx, const double* ints, int n, unsigned* out);
+void sympair_row_max(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, unsigned* out);
 
 }  // namespace hfgpu
