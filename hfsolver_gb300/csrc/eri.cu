@@ -411,6 +411,9 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
                     }
                 }
                 if (!c.segs.empty()) {
+                    // the kernels index quartets, warps and prefix sums of a class in 32 bits
+                    HF_CHECK(c.nq < (1ll << 31) && c.nwarps < (1ll << 30), HFGPU_ERR_UNSUPPORTED,
+                             "quartet class too large for 32-bit indexing");
                     c.dsegs = to_device(c.segs, st);
                     P->classes.push_back(std::move(c));
                 }
@@ -590,6 +593,7 @@ static void layout_class(Context& ctx, ClassPlan& c, int target)
         const int64_t qpw = 32 / s.split;
         c.nwarps += (s.nq + qpw - 1) / qpw * G_;
     }
+    HF_CHECK(c.nwarps < (1ll << 30), HFGPU_ERR_UNSUPPORTED, "quartet class too large for 32-bit indexing");
     c.dsegs.upload(c.segs.data(), c.segs.size());
     c.lane_target = target;
 }

@@ -142,14 +142,15 @@ __device__ __forceinline__ void run_chunk(const EriArgs& a, int bra, int ket, bo
             const int icd = CH * CI::NCD + s;
             const int k = fc[icd / ncart(CI::LD)], l = fd[icd % ncart(CI::LD)];
             if (k < 0 || l < 0 || (sameCD && k < l)) continue;
-            const int64_t kh = k > l ? k : l, kl = kh * (kh + 1) / 2 + (k > l ? l : k);
+            const int kh = k > l ? k : l, kl = kh * (kh + 1) / 2 + (k > l ? l : k);
 #pragma unroll
             for (int ab = 0; ab < CI::NAB; ++ab) {
                 const int i = fa[ab / ncart(CI::LB)], j = fb[ab % ncart(CI::LB)];
                 if (i < 0 || j < 0 || (sameAB && i < j)) continue;
-                const int64_t ih = i > j ? i : j, ij = ih * (ih + 1) / 2 + (i > j ? j : i);
+                const int ih = i > j ? i : j, ij = ih * (ih + 1) / 2 + (i > j ? j : i);
                 if (sameBK && ij < kl) continue;
-                const int64_t idx = ij >= kl ? ij * (ij + 1) / 2 + kl : kl * (kl + 1) / 2 + ij;
+                // pair indices fit 32 bits (n <= 512); only the packed position needs 64
+                const int64_t idx = ij >= kl ? (((int64_t)ij * (ij + 1)) >> 1) + kl : (((int64_t)kl * (kl + 1)) >> 1) + ij;
                 a.out[idx] = acc[ab * CI::NCD + s];
             }
         }
@@ -174,22 +175,25 @@ template <int TB, int TK, int MODE>
 __global__ void __launch_bounds__(ERI_BLOCK) eri_class_kernel(EriArgs a)
 {
     using CI = ClassInfo<TB, TK>;
-    const int64_t w = (int64_t)blockIdx.x * (ERI_BLOCK / 32) + threadIdx.x / 32;
-    if (w >= a.nwarps) return;
+    // warp, quartet and prefix-sum values of a class stay below 2^31 (checked when
+    // the plan is made): the searches compare in 32 bits (64-bit compares run on
+    // this GPU's narrow FP64 pipe, which the integrals need)
+    const int w = blockIdx.x * (ERI_BLOCK / 32) + threadIdx.x / 32;
+    if (w >= (int)a.nwarps) return;
     const int lane = threadIdx.x & 31;
     int lo = 0, hi = a.nseg - 1;  // last segment with warp0 <= w
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (a.segs[mid].warp0 <= w) lo = mid; else hi = mid - 1;
+        if ((int)a.segs[mid].warp0 <= w) lo = mid; else hi = mid - 1;
     }
     const Seg sg = a.segs[lo];
-    const int64_t lw = w - sg.warp0;
-    const int chunk = (int)(lw % CI::G);
+    const int lw = w - (int)sg.warp0;
+    const int chunk = lw % CI::G;
     const int split = sg.split;
     const int sub = lane & (split - 1);
-    int64_t q = (lw / CI::G) * (32 / split) + lane / split;
-    const bool active = q < sg.nq;
-    if (!active) q = sg.nq - 1;
+    int q = (lw / CI::G) * (32 / split) + lane / split;
+    const bool active = q < (int)sg.nq;
+    if (!active) q = (int)sg.nq - 1;
     int bra, ket;
     if (sg.list) {
         const int2 e = a.list[sg.pref0 + q];
@@ -200,10 +204,10 @@ __global__ void __launch_bounds__(ERI_BLOCK) eri_class_kernel(EriArgs a)
         int l2 = 0, h2 = sg.nbra - 1;  // last bra i with pf[i] <= q
         while (l2 < h2) {
             const int mid = (l2 + h2 + 1) >> 1;
-            if (pf[mid] <= q) l2 = mid; else h2 = mid - 1;
+            if ((int)pf[mid] <= q) l2 = mid; else h2 = mid - 1;
         }
         bra = a.gpairs[sg.bra0 + l2];
-        ket = a.gpairs[sg.ket0 + (int)(q - pf[l2])];
+        ket = a.gpairs[sg.ket0 + (q - (int)pf[l2])];
     }
     dispatch_chunk<TB, TK, MODE, CI::G, 0>(a, chunk, bra, ket, active, sg.qoff + q, sub, split);
 }

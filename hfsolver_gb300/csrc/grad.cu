@@ -187,25 +187,26 @@ __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
     const unsigned mask = tm == 32 ? 0xffffffffu : (((1u << tm) - 1u) << (lane & ~(unsigned)(tm - 1)));
     const int64_t qg = ((int64_t)blockIdx.x * GRAD_BLOCK + tid) / tm;
     if (qg >= g.nq) return;  // the whole team leaves together
+    const int qg32 = (int)qg;
     double* ws = sm + (int64_t)(tid / tm) * g.smem_team;
 
     int lo = 0, hi = g.nseg - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (g.segs[mid].qoff <= qg) lo = mid; else hi = mid - 1;
+        if ((int)(g.segs[mid].qoff) <= qg32) lo = mid; else hi = mid - 1;
     }
     const Seg sg = g.segs[lo];
-    const int64_t q = qg - sg.qoff;
+    const int q = qg32 - (int)sg.qoff;  // class quartet counts stay below 2^31 (plan check)
     int bra, ket;
     {
         const int64_t* pf = g.prefix + sg.pref0;
         int l2 = 0, h2 = sg.nbra - 1;
         while (l2 < h2) {
             const int mid = (l2 + h2 + 1) >> 1;
-            if (pf[mid] <= q) l2 = mid; else h2 = mid - 1;
+            if ((int)pf[mid] <= q) l2 = mid; else h2 = mid - 1;
         }
         bra = g.gpairs[sg.bra0 + l2];
-        ket = g.gpairs[sg.ket0 + (int)(q - pf[l2])];
+        ket = g.gpairs[sg.ket0 + (q - (int)pf[l2])];
     }
     const int A = g.pA[bra], B = g.pB[bra], C = g.pA[ket], D = g.pB[ket];
     const int la = g.la, lb = g.lb, lc = g.lc, ld = g.ld;

@@ -61,13 +61,14 @@ __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
     constexpr int NA = ncart(CI::LA), NB = ncart(CI::LB), NC = ncart(CI::LC), ND = ncart(CI::LD);
     const int64_t qg = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (qg >= a.nq) return;
+    const int qg32 = (int)qg;
     int lo = 0, hi = a.nseg - 1;  // last segment with qoff <= qg
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (a.segs[mid].qoff <= qg) lo = mid; else hi = mid - 1;
+        if ((int)(a.segs[mid].qoff) <= qg32) lo = mid; else hi = mid - 1;
     }
     const Seg sg = a.segs[lo];
-    const int64_t q = qg - sg.qoff;
+    const int q = qg32 - (int)sg.qoff;  // class quartet counts stay below 2^31 (plan check)
     int bra, ket;
     if (sg.list) {
         const int2 e = a.list[sg.pref0 + q];
@@ -78,10 +79,10 @@ __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
         int l2 = 0, h2 = sg.nbra - 1;
         while (l2 < h2) {
             const int mid = (l2 + h2 + 1) >> 1;
-            if (pf[mid] <= q) l2 = mid; else h2 = mid - 1;
+            if ((int)pf[mid] <= q) l2 = mid; else h2 = mid - 1;
         }
         bra = a.gpairs[sg.bra0 + l2];
-        ket = a.gpairs[sg.ket0 + (int)(q - pf[l2])];
+        ket = a.gpairs[sg.ket0 + (q - (int)pf[l2])];
     }
     const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
     if (digest_skip(a, bra, ket, A, B, C, D)) return;
@@ -202,23 +203,24 @@ __global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
     const unsigned mask = split == 32 ? 0xffffffffu : (((1u << split) - 1u) << (lane & ~(unsigned)(split - 1)));
     const int64_t qg = tid / split;
     if (qg >= a.nq) return;  // all lanes of a quartet leave together
+    const int qg32 = (int)qg;
     int lo = 0, hi = a.nseg - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (a.segs[mid].qoff <= qg) lo = mid; else hi = mid - 1;
+        if ((int)(a.segs[mid].qoff) <= qg32) lo = mid; else hi = mid - 1;
     }
     const Seg sg = a.segs[lo];
-    const int64_t q = qg - sg.qoff;
+    const int q = qg32 - (int)sg.qoff;  // class quartet counts stay below 2^31 (plan check)
     int bra, ket;
     {
         const int64_t* pf = a.prefix + sg.pref0;
         int l2 = 0, h2 = sg.nbra - 1;
         while (l2 < h2) {
             const int mid = (l2 + h2 + 1) >> 1;
-            if (pf[mid] <= q) l2 = mid; else h2 = mid - 1;
+            if ((int)pf[mid] <= q) l2 = mid; else h2 = mid - 1;
         }
         bra = a.gpairs[sg.bra0 + l2];
-        ket = a.gpairs[sg.ket0 + (int)(q - pf[l2])];
+        ket = a.gpairs[sg.ket0 + (q - (int)pf[l2])];
     }
     const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
     if (digest_skip(a, bra, ket, A, B, C, D)) return;  // same answer for all lanes of the quartet
