@@ -30,6 +30,7 @@
 // Hermite sums with the Hellmann-Feynman term of each nucleus C obtained by
 // translational invariance, dV/dC = -(dV/dA + dV/dB).
 #include <algorithm>
+#include <mutex>
 #include <cmath>
 #include <vector>
 
@@ -177,6 +178,12 @@ struct GradArgs {
 
 __device__ __forceinline__ int tq(int c, int s) { return (c >> s) & 15; }
 
+// PRIV = false: the team's lanes split each primitive quartet's component loops
+// (classes with many components).  PRIV = true: each lane takes every tm-th
+// primitive quartet with a private workspace, the density blocks shared (light
+// classes such as (ss|ss), whose 1 - 9 components would leave most lanes idle
+// while one walks up to 36 x 36 primitive quartets).
+template <bool PRIV>
 __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
 {
     extern __shared__ double sm[];
@@ -221,7 +228,10 @@ __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
     double* PBD = PAC + NA * NC;
     double* PAD = PBD + NB * ND;
     double* PBC = PAD + NA * ND;
-    double* sab = PBC + NB * NC;
+    // per-primitive workspace: the team's, or this lane's own
+    const int nshared = NAB + NCD + NA * NC + NB * ND + NA * ND + NB * NC;
+    const int npriv = NAB + NCD + 2 * nR + (NCD * nHp > NAB * nHq ? NCD * nHp : NAB * nHq);
+    double* sab = PBC + NB * NC + (PRIV ? lt * npriv : 0);
     double* scd = sab + NAB;
     double* R0 = scd + NCD;
     double* R1 = R0 + nR;
@@ -232,6 +242,11 @@ __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
     const int* fc = g.comp_fn + g.cfn0[C];
     const int* fd = g.comp_fn + g.cfn0[D];
     const int n = g.n;
+    // component loops: split over the team, or whole in each lane
+    const int c0 = PRIV ? 0 : lt, cs = PRIV ? 1 : tm;
+    auto team_sync = [&]() {
+        if (!PRIV) __syncwarp(mask);
+    };
     auto Pv = [&](int x, int y) -> double { return (x < 0 || y < 0) ? 0.0 : __ldg(g.P + x + (int64_t)y * n); };
     for (int e = lt; e < NAB; e += tm) PAB[e] = Pv(fa[e / NB], fb[e % NB]);
     for (int e = lt; e < NCD; e += tm) PCD[e] = Pv(fc[e / ND], fd[e % ND]);
@@ -239,6 +254,7 @@ __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
     for (int e = lt; e < NB * ND; e += tm) PBD[e] = Pv(fb[e / ND], fd[e % ND]);
     for (int e = lt; e < NA * ND; e += tm) PAD[e] = Pv(fa[e / ND], fd[e % ND]);
     for (int e = lt; e < NB * NC; e += tm) PBC[e] = Pv(fb[e / NC], fc[e % NC]);
+    __syncwarp(mask);
 
     const int kb = g.pK[bra], kk = g.pK[ket];
     const int npA = g.snp[A], npB = g.snp[B], npC = g.snp[C], npD = g.snp[D];
@@ -254,8 +270,9 @@ __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
 #pragma unroll
     for (int k = 0; k < 12; ++k) gr[k] = 0.0;
 
-    for (int pb = 0; pb < kb; ++pb)
-        for (int pk = 0; pk < kk; ++pk) {
+    for (int pq = PRIV ? lt : 0; pq < kb * kk; pq += PRIV ? tm : 1) {
+        {
+            const int pb = pq / kk, pk = pq - pb * kk;
             const double* rb = g.gp + (g.goff[bra] + pb) * GP_STRIDE;
             const double* rk = g.gp + (g.goff[ket] + pk) * GP_STRIDE;
             const double p = __ldg(rb + 2), q_ = __ldg(rk + 2);
@@ -269,17 +286,17 @@ __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
             {
                 const int ia = pb / npB, ib = pb - ia * npB, ic = pk / npD, id = pk - ic * npD;
                 const double kab = __ldg(rb + 6), kcd = __ldg(rk + 6);
-                for (int e = lt; e < NAB; e += tm) sab[e] = cA[(e / NB) * npA + ia] * cB[(e % NB) * npB + ib] * kab;
-                for (int e = lt; e < NCD; e += tm) scd[e] = cC[(e / ND) * npC + ic] * cD[(e % ND) * npD + id] * kcd;
+                for (int e = c0; e < NAB; e += cs) sab[e] = cA[(e / NB) * npA + ia] * cB[(e % NB) * npB + ib] * kab;
+                for (int e = c0; e < NCD; e += cs) scd[e] = cC[(e / ND) * npC + ic] * cD[(e % ND) * npD + id] * kcd;
             }
             // R^{(m)}_{tuv}, from m = L+1 down to m = 0
             double* cur = R0;
             double* nxt = R1;
-            if (lt == 0) cur[0] = F[L + 1];
-            __syncwarp(mask);
+            if (PRIV || lt == 0) cur[0] = F[L + 1];
+            team_sync();
             for (int m = L; m >= 0; --m) {
                 const int cnt = nherm(L + 1 - m);
-                for (int h = lt; h < cnt; h += tm) {
+                for (int h = c0; h < cnt; h += cs) {
                     const int c = __ldg(g.herm + h);
                     const int t = tq(c, 0), u = tq(c, 4), v = tq(c, 8);
                     double val;
@@ -297,7 +314,7 @@ __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
                     }
                     nxt[h] = val;
                 }
-                __syncwarp(mask);
+                team_sync();
                 double* tmp = cur;
                 cur = nxt;
                 nxt = tmp;
@@ -311,7 +328,7 @@ __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
             const double* Kz = Ky + GE_DIM;
 
             // ---- bra centres A, B
-            for (int it = lt; it < NCD * nHp; it += tm) {
+            for (int it = c0; it < NCD * nHp; it += cs) {
                 const int cd = it / nHp, h = it - cd * nHp;
                 const int c = cd / ND, d = cd - c * ND;
                 const int cc = clc[c], dc = cld[d], hc = __ldg(g.herm + h);
@@ -332,10 +349,10 @@ __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
                 }
                 H[it] = acc * scd[cd];
             }
-            __syncwarp(mask);
+            team_sync();
             {
                 const double al = __ldg(rb), be = __ldg(rb + 1);
-                for (int it = lt; it < NAB * nHp; it += tm) {
+                for (int it = c0; it < NAB * nHp; it += cs) {
                     const int ab = it / nHp, h = it - ab * nHp;
                     const int a = ab / NB, b = ab - a * NB;
                     const int ac = cla[a], bc = clb[b], hc = __ldg(g.herm + h);
@@ -370,10 +387,10 @@ __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
                     gr[5] = fma(w, ex * ey * dbz, gr[5]);
                 }
             }
-            __syncwarp(mask);
+            team_sync();
 
             // ---- ket centres C, D
-            for (int it = lt; it < NAB * nHq; it += tm) {
+            for (int it = c0; it < NAB * nHq; it += cs) {
                 const int ab = it / nHq, h = it - ab * nHq;
                 const int a = ab / NB, b = ab - a * NB;
                 const int ac = cla[a], bc = clb[b], hc = __ldg(g.herm + h);
@@ -391,10 +408,10 @@ __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
                 }
                 H[it] = ((t + u + v) & 1 ? -acc : acc) * sab[ab];
             }
-            __syncwarp(mask);
+            team_sync();
             {
                 const double gc = __ldg(rk), gd = __ldg(rk + 1);
-                for (int it = lt; it < NCD * nHq; it += tm) {
+                for (int it = c0; it < NCD * nHq; it += cs) {
                     const int cd = it / nHq, h = it - cd * nHq;
                     const int c = cd / ND, d = cd - c * ND;
                     const int cc = clc[c], dc = cld[d], hc = __ldg(g.herm + h);
@@ -429,8 +446,9 @@ __global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
                     gr[11] = fma(w, ex * ey * ddz, gr[11]);
                 }
             }
-            __syncwarp(mask);
+            team_sync();
         }
+    }
     for (int o = tm >> 1; o > 0; o >>= 1)
 #pragma unroll
         for (int k = 0; k < 12; ++k) gr[k] += __shfl_xor_sync(mask, gr[k], o);
@@ -630,12 +648,25 @@ static int grad_team(int la, int lb, int lc, int ld)
     return 4;
 }
 
-static int grad_smem_team(int la, int lb, int lc, int ld)
+// classes with at most this many component quartets run the primitive loop one
+// primitive quartet per lane (eri_grad_kernel<true>), 8 lanes per shell quartet
+constexpr int GRAD_PRIV_MAX = 9, GRAD_PRIV_TEAM = 8;
+
+static bool grad_priv(int la, int lb, int lc, int ld)
+{
+    return ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) <= GRAD_PRIV_MAX;
+}
+
+// doubles of shared memory per team: the six density blocks, then the
+// per-primitive workspace (one per lane in the private mode)
+static int grad_smem_team(int la, int lb, int lc, int ld, bool priv, int team)
 {
     const int NA = ncart(la), NB = ncart(lb), NC = ncart(lc), ND = ncart(ld);
     const int NAB = NA * NB, NCD = NC * ND;
     const int nHp = nherm(la + lb + 1), nHq = nherm(lc + ld + 1), nR = nherm(la + lb + lc + ld + 1);
-    return NAB + NCD + NA * NC + NB * ND + NA * ND + NB * NC + NAB + NCD + 2 * nR + std::max(NCD * nHp, NAB * nHq);
+    const int shared = NAB + NCD + NA * NC + NB * ND + NA * ND + NB * NC;
+    const int work = NAB + NCD + 2 * nR + std::max(NCD * nHp, NAB * nHq);
+    return shared + (priv ? team : 1) * work;
 }
 
 void eri_gradient(Context& ctx, EriPlan* P, const double* dP, double* d_grad, float* ms_out)
@@ -682,11 +713,11 @@ void eri_gradient(Context& ctx, EriPlan* P, const double* dP, double* d_grad, fl
     DBuf<int> dherm = to_device(herm, st), dcart = to_device(cartc, st), dsat = to_device(sat, st);
     DBuf<int64_t> dgoff = to_device(goff, st);
 
-    static bool attr_set[64] = {false};
-    if (!attr_set[ctx.device & 63]) {
-        HF_CUDA(cudaFuncSetAttribute(eri_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        attr_set[ctx.device & 63] = true;
-    }
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(eri_grad_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(eri_grad_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    });
     ctx.trace_mark("grad pair data");
     cudaEvent_t e0, e1;
     HF_CUDA(cudaEventCreate(&e0));
@@ -705,15 +736,17 @@ void eri_gradient(Context& ctx, EriPlan* P, const double* dP, double* d_grad, fl
         a.herm = dherm.p; a.cartc = dcart.p;
         a.P = dP; a.n = b.nbf; a.grad = d_grad;
         a.la = ptype_la(c.tb); a.lb = ptype_lb(c.tb); a.lc = ptype_la(c.tk); a.ld = ptype_lb(c.tk);
-        int team = grad_team(a.la, a.lb, a.lc, a.ld);
-        const int smt = grad_smem_team(a.la, a.lb, a.lc, a.ld);
-        while (team < 32 && (size_t)(GRAD_BLOCK / team) * smt * sizeof(double) > 200 * 1024) team <<= 1;
+        const bool priv = grad_priv(a.la, a.lb, a.lc, a.ld);
+        int team = priv ? GRAD_PRIV_TEAM : grad_team(a.la, a.lb, a.lc, a.ld);
+        int smt = grad_smem_team(a.la, a.lb, a.lc, a.ld, priv, team);
+        while (!priv && team < 32 && (size_t)(GRAD_BLOCK / team) * smt * sizeof(double) > 200 * 1024) team <<= 1;
         const size_t smem = (size_t)(GRAD_BLOCK / team) * smt * sizeof(double);
         HF_CHECK(smem <= 200 * 1024, HFGPU_ERR_UNSUPPORTED, "gradient workspace exceeds shared memory");
         a.team = team;
         a.smem_team = smt;
         const int64_t blocks = (c.nq * team + GRAD_BLOCK - 1) / GRAD_BLOCK;
-        eri_grad_kernel<<<(unsigned)blocks, GRAD_BLOCK, smem, st>>>(a);
+        if (priv) eri_grad_kernel<true><<<(unsigned)blocks, GRAD_BLOCK, smem, st>>>(a);
+        else eri_grad_kernel<false><<<(unsigned)blocks, GRAD_BLOCK, smem, st>>>(a);
         count_launch();
         HF_CUDA(cudaGetLastError());
     }
