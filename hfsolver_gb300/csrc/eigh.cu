@@ -31,17 +31,11 @@
 #include <string>
 
 #include "eigh.h"
+#include "gridsync.cuh"
 
 namespace hfgpu {
 
 namespace {
-
-__device__ __forceinline__ uint64_t global_ns()
-{
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
 
 __device__ __forceinline__ double warp_sum(double x)
 {
@@ -50,46 +44,12 @@ __device__ __forceinline__ double warp_sum(double x)
     return x;
 }
 
-__device__ __forceinline__ unsigned atom_add_release(unsigned* p, unsigned v)
-{
-    unsigned old;
-    asm volatile("atom.add.release.gpu.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-    return old;
-}
-
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
-{
-    unsigned v;
-    asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// grid barrier for one-warp blocks on a counter that only grows: barrier number
-// `epoch` (1, 2, ...) completes when the count reaches epoch * nblocks.  The
-// arrival is a release and the wait an acquire, so the writes each block made
-// before the barrier are visible to every block after it.  Gives up after 2 s
-// (error flag) so that a grid that was not co-resident cannot spin forever.
+// grid barrier for one-warp blocks (gridsync.cuh)
 __device__ bool trd_barrier(TrdSync* s, unsigned nblocks, unsigned epoch)
 {
-    int ok = 1;
     __syncwarp();
-    if (threadIdx.x == 0) {
-        atom_add_release(&s->count, 1u);
-        const unsigned target = epoch * nblocks;
-        unsigned spins = 0;
-        uint64_t t0 = 0;
-        while ((int)(ld_acquire(&s->count) - target) < 0) {
-            if ((++spins & 1023u) == 0) {
-                if (t0 == 0) {
-                    t0 = global_ns();
-                } else if (global_ns() - t0 > 2000000000ull) {
-                    atomicExch(&s->err, 1);
-                    break;
-                }
-            }
-        }
-        ok = *(volatile int*)&s->err == 0;
-    }
+    int ok = 1;
+    if (threadIdx.x == 0) ok = grid_arrive_wait(&s->count, &s->err, nblocks, epoch);
     ok = __shfl_sync(0xffffffffu, ok, 0);
     return ok != 0;
 }

@@ -218,6 +218,16 @@ static void launch_class(Context& ctx, EriPlan* P, ClassPlan& c, int mode, doubl
     HF_CUDA(cudaGetLastError());
 }
 
+// Schwarz factor of each shell pair from its diagonal quartet block (36 slots)
+__global__ void pair_qmax_kernel(int npair, const double* __restrict__ diag, double* Q)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= npair) return;
+    double m = 0.0;
+    for (int k = 0; k < 36; ++k) m = fmax(m, fabs(diag[(int64_t)id * 36 + k]));
+    Q[id] = sqrt(m);
+}
+
 EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
 {
     cudaStream_t st = ctx.stream;
@@ -235,6 +245,7 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
         P->sL = to_device(L, st); P->snp = to_device(np, st); P->sp0 = to_device(p0, st);
         P->sc0 = to_device(c0, st); P->scf = to_device(f0, st); P->cfn = to_device(b.comp_fn, st);
         P->sxyz = to_device(xyz, st); P->alpha = to_device(b.alpha, st); P->coef = to_device(b.coef, st);
+        ctx.trace_mark("plan shells");
 
         // shell pairs, larger angular momentum first
         int64_t off = 0;
@@ -274,6 +285,7 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
             HF_CUDA(cudaGetLastError());
         }
 
+        ctx.trace_mark("plan pair data");
         // groups: (pair type, primitive count)
         std::map<std::pair<int, int>, std::vector<int>> gmap;
         for (int id = 0; id < P->npair; id++) gmap[{P->pT[id], P->pK[id]}].push_back(id);
@@ -315,19 +327,19 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
                 c.dsegs = to_device(c.segs, st);
                 launch_class(ctx, P, c, MODE_DIAG, diag.p, ddl.p);
             }
-            std::vector<double> hd((size_t)P->npair * 36);
-            diag.download(hd.data(), hd.size());
+            // Q = sqrt(max |(ab|ab)|) per pair on the device; only Q comes back
+            DBuf<double> dq(P->npair, st);
+            pair_qmax_kernel<<<(P->npair + 127) / 128, 128, 0, st>>>(P->npair, diag.p, dq.p);
+            count_launch();
+            HF_CUDA(cudaGetLastError());
+            dq.download(P->Q.data(), P->npair);
             HF_CUDA(cudaStreamSynchronize(st));
-            for (int id = 0; id < P->npair; id++) {
-                double m = 0;
-                for (int k = 0; k < 36; k++) m = std::max(m, std::fabs(hd[(size_t)id * 36 + k]));
-                P->Q[id] = std::sqrt(m);
-            }
             for (auto& g : gmap)
                 std::stable_sort(g.second.begin(), g.second.end(),
                                  [&](int x, int y) { return P->Q[x] > P->Q[y]; });
         }
 
+        ctx.trace_mark("plan schwarz");
         // flatten the groups
         std::vector<int> gp;
         struct G { int t, k, off, n; std::vector<double> q; std::vector<int64_t> eff; };
@@ -421,6 +433,7 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
         P->prefix = to_device(prefix, st);
         P->stats = stt;
         HF_CUDA(cudaStreamSynchronize(st));
+        ctx.trace_mark("plan classes");
         return P;
     } catch (...) {
         delete P;

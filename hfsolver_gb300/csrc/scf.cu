@@ -17,6 +17,7 @@
 
 #include "internal.h"
 #include "eigh.h"
+#include "gridsync.cuh"
 #include "scf.h"
 
 namespace hfgpu {
@@ -167,31 +168,12 @@ struct Sp2Sync {
     int err, steps;
 };
 
-__device__ bool sp2_grid_barrier(Sp2Sync* s, unsigned nblocks)
+// grid barrier number `epoch` of one SP2 launch (gridsync.cuh)
+__device__ bool sp2_grid_barrier(Sp2Sync* s, unsigned nblocks, unsigned epoch)
 {
     __shared__ int ok;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned* vgen = &s->gen;
-        const unsigned g = *vgen;
-        __threadfence();
-        if (atomicAdd(&s->count, 1u) == nblocks - 1) {
-            atomicExch(&s->count, 0u);
-            __threadfence();
-            atomicAdd(&s->gen, 1u);
-        } else {
-            long spins = 0;
-            while (*vgen == g) {
-                if (++spins > (1L << 24)) {  // ~1 s: other streams may hold SMs for a while
-                    atomicExch(&s->err, 1);
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        ok = *(volatile int*)&s->err == 0;
-    }
+    if (threadIdx.x == 0) ok = grid_arrive_wait(&s->count, &s->err, nblocks, epoch);
     __syncthreads();
     return ok;
 }
@@ -278,7 +260,7 @@ __global__ void __launch_bounds__(256) sp2_persistent_kernel(int n, int nocc, in
         }
         block_add(pt, tr + 2 * (it + 1));  // (its __syncthreads also guard Ar/Bc reuse)
         block_add(pn, tr + 2 * (it + 1) + 1);
-        if (!sp2_grid_barrier(sync, gridDim.x)) return;
+        if (!sp2_grid_barrier(sync, gridDim.x, (unsigned)it + 1)) return;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) sync->steps = maxs;
 }
