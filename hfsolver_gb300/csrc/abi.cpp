@@ -137,19 +137,22 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         std::vector<double> x(natoms), y(natoms), z(natoms);
         for (int i = 0; i < natoms; i++) { x[i] = xyz[3 * i]; y[i] = xyz[3 * i + 1]; z[i] = xyz[3 * i + 2]; }
         DBuf<double> dS(nn, st), dT(nn, st), dV(nn, st), dH(nn, st);
-        onee_compute(ctx, b, natoms, atno, x.data(), y.data(), z.data(), dS.p, dT.p, dV.p);
-        {
-            const double one = 1.0;
-            HF_CUBLAS(cublasDgeam(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, &one, dT.p, n, &one, dV.p, n, dH.p, n));
-        }
-        ctx.trace_mark("one-electron");
+        // the one-electron integrals run on a side stream, under the ERI plan's
+        // host work (pair lists, quartet classes); joined before H is formed
+        ctx.fork();
+        onee_compute(ctx, b, natoms, atno, x.data(), y.data(), z.data(), dS.p, dT.p, dV.p, ctx.aux[0]);
         // integrals, resident in HBM for the whole SCF
         DBuf<double> dI(packed_size(n), st);
         dI.zero();
         EriStats es;
         std::unique_ptr<EriPlan, void (*)(EriPlan*)> plan(eri_plan_create(ctx, b, opt.schwarz), eri_plan_destroy);
+        ctx.join();
+        {
+            const double one = 1.0;
+            HF_CUBLAS(cublasDgeam(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, &one, dT.p, n, &one, dV.p, n, dH.p, n));
+        }
         res->ms_setup = total.ms();
-        ctx.trace_mark("pairs+schwarz");
+        ctx.trace_mark("one-electron + plan");
         // the packed array feeds MBPT2; the screened quartet blocks feed every Fock build
         eri_compute(ctx, plan.get(), dI.p, true, &es);
         res->ms_eri = es.ms;

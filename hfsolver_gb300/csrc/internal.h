@@ -216,8 +216,10 @@ void eri_compute(Context& ctx, EriPlan* p, double* d_out, bool keep_blocks, EriS
 void eri_digest(Context& ctx, EriPlan* p, const double* dP, double* dG, double screen = 0.0);
 
 // one-electron integrals (onee.cu): S, T, V on the device (n x n, symmetric)
+// (on: the stream to run on, ctx.stream if null; the results are ready in stream
+// order there, the host does not wait)
 void onee_compute(Context& ctx, const Basis& b, int natoms, const int* atno, const double* x,
-                  const double* y, const double* z, double* dS, double* dT, double* dV);
+                  const double* y, const double* z, double* dS, double* dT, double* dV, cudaStream_t on = nullptr);
 
 // J/K (jk.cu): G = J - K/2 from packed integrals and density P (device)
 void jk_from_packed(Context& ctx, int n, const double* d_int2, const double* dP, double* dG);

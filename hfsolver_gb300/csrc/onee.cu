@@ -163,9 +163,9 @@ __global__ void onee_kernel(FnDev f, int n, int nat, const int* __restrict__ Z, 
 }
 
 void onee_compute(Context& ctx, const Basis& b, int nat, const int* atno, const double* x, const double* y,
-                  const double* z, double* dS, double* dT, double* dV)
+                  const double* z, double* dS, double* dT, double* dV, cudaStream_t on)
 {
-    cudaStream_t st = ctx.stream;
+    cudaStream_t st = on ? on : ctx.stream;
     int n = b.nbf;
     std::vector<int> lmn(3 * n), np(n), a0(n), c0(n);
     std::vector<double> xyz(3 * n);
@@ -202,7 +202,6 @@ void onee_compute(Context& ctx, const Basis& b, int nat, const int* atno, const 
     onee_kernel<<<grid, 128, 0, st>>>(f, n, nat, dZ.p, dC.p, ctx.boys, dS, dT, dV);
     count_launch();
     HF_CUDA(cudaGetLastError());
-    HF_CUDA(cudaStreamSynchronize(st));
 }
 
 }  // namespace hfgpu
