@@ -1,5 +1,6 @@
 // extern "C" entry points of libhfgpu (declared in include/hfgpu.h).
 #include <chrono>
+#include <cstdlib>
 #include <memory>
 #include <cmath>
 #include <cstring>
@@ -173,7 +174,10 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         in.direct_jk = [](Context& c, void* user, const double* P, double* G, double screen) {
             eri_digest(c, (EriPlan*)user, P, G, screen);
         };
-        if (opt.incremental) in.inc_screen = opt.schwarz > 0 ? opt.schwarz : 1e-12;
+        // density-difference builds skip quartets whose bounded contribution is below
+        // 1e-10 (or the Schwarz threshold, if larger); the full builds of the last
+        // iterations remove what they left out before convergence is accepted
+        if (opt.incremental) in.inc_screen = std::max(opt.schwarz, 1e-10);
         in.direct_ctx = plan.get();
         DBuf<double> dP0;
         if (opt.guess == 1) {  // superposition of atomic densities instead of P = 0

@@ -117,19 +117,44 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
     }
 }
 
-// one block per (i, j): sum_ab (ia|jb) [2 (ia|jb) - (ib|ja)] / (e_i + e_j - e_a - e_b), T[j][b][i][a]
-__global__ void mp2_jbia_kernel(int o, int v, const double* __restrict__ T, const double* __restrict__ eps,
-                                double* partial)
+// one block per (i, j): sum_ab (ia|jb) [2 (ia|jb) - (ib|ja)] / (e_i + e_j - e_a - e_b)
+// from T[j][b][i][a] (relative error of each term ~1e-14 from the refined reciprocal).  For fixed (i, j) the v x v block X[b][a] = (ia|jb) has rows
+// of consecutive a; (ib|ja) = X[a][b] is its transpose.  32 x 32 tiles of X and of
+// the mirrored tile are staged in shared memory with coalesced row reads, so T is
+// read with unit stride instead of one scattered element per (ib|ja).
+__global__ void __launch_bounds__(256) mp2_pair_energy_kernel(int o, int v, const double* __restrict__ T,
+                                                             const double* __restrict__ eps, double* partial)
 {
+    __shared__ double A[32][33], B[32][33];
     const int i = blockIdx.x % o, j = blockIdx.x / o;
     const double eij = eps[i] + eps[j];
+    const int64_t rs = (int64_t)o * v;  // stride between consecutive b (rows of X)
+    const double* X = T + ((int64_t)j * v * o + i) * v;  // X[b][a] = X[b * rs + a]
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
     double s = 0.0;
-    for (int e = threadIdx.x; e < v * v; e += blockDim.x) {
-        const int a = e % v, b = e / v;
-        const double x = T[(((int64_t)j * v + b) * o + i) * v + a];
-        const double y = T[(((int64_t)j * v + a) * o + i) * v + b];
-        s += x * (2 * x - y) / (eij - eps[o + a] - eps[o + b]);
-    }
+    for (int b0 = 0; b0 < v; b0 += 32)
+        for (int a0 = 0; a0 < v; a0 += 32) {
+            for (int r = ty; r < 32; r += 8) {
+                const int b = b0 + r, a = a0 + tx;
+                A[r][tx] = (b < v && a < v) ? X[b * rs + a] : 0.0;    // X[b0 + r][a0 + tx]
+                const int bb = a0 + r, aa = b0 + tx;
+                B[r][tx] = (bb < v && aa < v) ? X[bb * rs + aa] : 0.0;  // X[a0 + r][b0 + tx]
+            }
+            __syncthreads();
+            for (int r = ty; r < 32; r += 8) {
+                const int b = b0 + r, a = a0 + tx;
+                if (b < v && a < v) {
+                    const double x = A[r][tx], y = B[tx][r];  // (ia|jb), (ib|ja)
+                    const double d = eij - eps[o + a] - eps[o + b];
+                    // 1/d: FP32 reciprocal (24 bits) and one Newton step in FP64
+                    // (~48 bits), instead of an FP64 division on the narrow FP64 pipe
+                    const double r0 = (double)__frcp_rn((float)d);
+                    const double rd = r0 * fma(-d, r0, 2.0);
+                    s = fma(x * (2 * x - y), rd, s);
+                }
+            }
+            __syncthreads();
+        }
     __shared__ double sh[256];
     sh[threadIdx.x] = s;
     __syncthreads();
@@ -147,7 +172,7 @@ double mp2_energy_mixed(Context& ctx, int n, const double* d_int2, const double*
     DBuf<double> T((size_t)o * v * o * v, ctx.stream);
     ao2mo_sliced(ctx, n, d_int2, dC, o, dC + (size_t)n * o, v, T.p);
     DBuf<double> part((size_t)o * o, ctx.stream);
-    mp2_jbia_kernel<<<o * o, 256, 0, ctx.stream>>>(o, v, T.p, d_eps, part.p);
+    mp2_pair_energy_kernel<<<o * o, 256, 0, ctx.stream>>>(o, v, T.p, d_eps, part.p);
     count_launch();
     HF_CUDA(cudaGetLastError());
     std::vector<double> h((size_t)o * o);

@@ -197,9 +197,10 @@ typedef struct {
                             final dsygvd for the orbitals; 0: dsygvd every iteration (reference) */
     int batch_streams;   /* hfgpu_rhf_batch: molecules in flight at once, each on its own
                             streams; <= 0: 8 */
-    int incremental;     /* 1: Fock builds from density differences, screened at the Schwarz
-                            threshold (1e-12 if none), a full build every 8 iterations and
-                            near convergence; 0: full builds (reference) */
+    int incremental;     /* 1: Fock builds from density differences, each quartet's bounded
+                            contribution screened at 1e-10 (or the Schwarz threshold if larger),
+                            a full build every 8 iterations and near convergence; 0: full
+                            builds (reference) */
     int autotune;        /* 1: time the candidate quartet-tile shapes of the ERI and Fock
                             kernels the first time a (class, size) is met and keep the
                             fastest (process-wide table); 0: built-in rules, unless the
