@@ -64,3 +64,19 @@ def test_graded(hf):
 def test_invalid_input_is_a_status(hf):
     with pytest.raises(hf.HFGPUError):
         hf.tridiag_eigen(np.array([1.0, np.nan]), np.array([0.5]))
+
+
+def test_concurrent_calls_share_the_pool(hf):
+    """Batched molecules solve their tridiagonal problems from several host threads
+    at once; the shared worker pool must give each call its own, unchanged result."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    rng = np.random.default_rng(11)
+    cases = [(rng.standard_normal(n), rng.standard_normal(n - 1)) for n in (150, 200, 260, 199, 64, 300)]
+    serial = [hf.tridiag_eigen(d, e) for d, e in cases]
+    with ThreadPoolExecutor(max_workers=6) as ex:
+        for _ in range(3):
+            got = list(ex.map(lambda c: hf.tridiag_eigen(*c), cases))
+            for (l0, z0), (l1, z1) in zip(serial, got):
+                assert np.array_equal(l0, l1)
+                assert np.array_equal(z0, z1)
