@@ -68,8 +68,16 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
         ctx.trace_mark("mp2 row max");
     }
     DBuf<double> Z((size_t)npair * nq, st);
+    // steps 2 and 4 (N = v) read their FP64 rows straight into the gather-fed GEMM
+    // (coalesced rows, no slice planes through HBM) while the virtual block spans
+    // at most DENSE_GATHER_TILES output tiles of 80 columns; wider ones use slicing + TMA
+    constexpr int DENSE_GATHER_TILES = 2;
+    const bool dense_gather = n2 <= 80 * DENSE_GATHER_TILES;
     // steps 1-2 over blocks of pairs
     const int64_t pb = std::max<int64_t>(1, SLICE_BUDGET_ROWS / n);
+    const int64_t qb_rows2 = std::max<int64_t>(1, SLICE_BUDGET_ROWS / std::max(n, n1));
+    DBuf<unsigned> dmax;
+    if (dense_gather) dmax.alloc((size_t)std::max(std::min(pb, npair), std::min(qb_rows2, nq)) * n1, st);
     DBuf<double> Y((size_t)std::min(pb, npair) * n1 * n, st);
     for (int64_t p0 = 0; p0 < npair; p0 += pb) {
         const int64_t np = std::min(pb, npair - p0);
@@ -82,8 +90,13 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
             sliced_gemm(ctx, A, B1, Y.p, OutMap{n, n1}, false);
         }
         ctx.trace_mark("mp2 step 1");
-        slice_dense(ctx, Y.p, np * n1, n, n, A, SLICE_TILE_A);
-        sliced_gemm(ctx, A, B2, Z.p + p0 * nq, OutMap{0, n2}, false);  // rows (p, j) -> Z[p][j][b]
+        if (dense_gather) {  // rows (p, j) -> Z[p][j][b]
+            dense_row_max(ctx, Y.p, np * n1, n, n, dmax.p);
+            sliced_gemm_dense_gather(ctx, Y.p, np * n1, n, n, dmax.p, B2, Z.p + p0 * nq, OutMap{0, n2});
+        } else {
+            slice_dense(ctx, Y.p, np * n1, n, n, A, SLICE_TILE_A);
+            sliced_gemm(ctx, A, B2, Z.p + p0 * nq, OutMap{0, n2}, false);
+        }
         ctx.trace_mark("mp2 step 2");
     }
     // Z^T: one contiguous row of pairs per q, so that the (q, mu) rows of step 3
@@ -111,8 +124,13 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
             sliced_gemm(ctx, A, B1, W.p, OutMap{n, n1}, false);
         }
         ctx.trace_mark("mp2 step 3");
-        slice_dense(ctx, W.p, nqb * n1, n, n, A, SLICE_TILE_A);
-        sliced_gemm(ctx, A, B2, T + q0 * n1 * n2, OutMap{0, n2}, false);  // rows (q, i) -> T[q][i][a]
+        if (dense_gather) {  // rows (q, i) -> T[q][i][a]
+            dense_row_max(ctx, W.p, nqb * n1, n, n, dmax.p);
+            sliced_gemm_dense_gather(ctx, W.p, nqb * n1, n, n, dmax.p, B2, T + q0 * n1 * n2, OutMap{0, n2});
+        } else {
+            slice_dense(ctx, W.p, nqb * n1, n, n, A, SLICE_TILE_A);
+            sliced_gemm(ctx, A, B2, T + q0 * n1 * n2, OutMap{0, n2}, false);
+        }
         ctx.trace_mark("mp2 step 4");
     }
 }

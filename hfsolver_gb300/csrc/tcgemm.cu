@@ -407,6 +407,19 @@ struct DenseRows {  // row-major rows with stride ld
     __device__ double at(Row w, int k) const { return __ldg(w + k); }
 };
 
+// dense row-major rows for the gather-fed GEMM (row maxima from dense_row_max)
+struct DenseRowsG {
+    const double* p;
+    int64_t ld;
+    const unsigned* rmax;
+    using Row = const double*;
+    __device__ Row row(int64_t r) const { return p + r * ld; }
+    __device__ double at(Row w, int k) const { return __ldg(w + k); }
+    __device__ unsigned long long row_max(int64_t r) const { return (unsigned long long)rmax[r] << 32; }
+    __device__ bool live(int64_t) const { return true; }
+    __device__ int64_t out_row(int64_t r) const { return r; }
+};
+
 struct PackedRows {  // rows (pair p, la), k = si of the packed (mu nu|la si), pairs mu >= nu from p0
     const double* ints;
     const int2* pairs;
@@ -1008,6 +1021,33 @@ void sympair_row_max(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, in
     row_max_tri_kernel<false><<<(unsigned)nq, 256, n * sizeof(unsigned), ctx.stream>>>(Zt, ldz, npair, n, out);
     count_launch();
     HF_CUDA(cudaGetLastError());
+}
+
+// one warp per row: the upper word of max |x| over the row's K elements
+__global__ void dense_row_max_kernel(const double* __restrict__ A, int64_t rows, int K, int64_t ld, unsigned* out)
+{
+    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (r >= rows) return;
+    const double* row = A + r * ld;
+    unsigned m = 0u;
+    for (int k = lane; k < K; k += 32) m = max(m, abs_hi(__ldg(row + k)));
+    m = warp_max_u32(m);
+    if (lane == 0) out[r] = m;
+}
+
+void dense_row_max(Context& ctx, const double* A, int64_t rows, int K, int64_t ld, unsigned* out)
+{
+    dense_row_max_kernel<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, ctx.stream>>>(A, rows, K, ld, out);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+}
+
+void sliced_gemm_dense_gather(Context& ctx, const double* A, int64_t rows, int K, int64_t ld, const unsigned* rmax,
+                              const Sliced& B, double* out, OutMap om)
+{
+    const DenseRowsG src{A, ld, rmax};
+    gather_gemm(ctx, src, rows, rows, K, B, out, om);
 }
 
 void sliced_gemm_packed(Context& ctx, const double* ints, const int2* pairs, int64_t p0, int64_t npairs, int n,

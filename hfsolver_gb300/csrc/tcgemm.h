@@ -46,6 +46,11 @@ void sliced_gemm_sympair(Context& ctx, const double* Zt, int64_t ldz, int64_t nq
 // exponent): packed integrals, rows (pair p, la) of all n (n + 1) / 2 pairs ->
 // out[p * n + la]; Zt rows (q, mu) -> out[q * n + mu]
 void packed_row_max(Context& ctx, const double* ints, int n, unsigned* out);
+// dense row-major rows (rows x K, stride ld): their maxima, and the gather-fed GEMM
+// over them (no A planes in HBM; B may span several 64/80-column tiles)
+void dense_row_max(Context& ctx, const double* A, int64_t rows, int K, int64_t ld, unsigned* out);
+void sliced_gemm_dense_gather(Context& ctx, const double* A, int64_t rows, int K, int64_t ld, const unsigned* rmax,
+                              const Sliced& B, double* out, OutMap om);
 void sympair_row_max(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, unsigned* out);
 
 }  // namespace hfgpu
