@@ -64,8 +64,9 @@ void ql_eigenvalues(int nb, double* d, double* e)
                     deflated = true;
                     break;
                 }
-                s = f / r;
-                c = g / r;
+                const double ri = 1.0 / r;  // one division for both rotation entries
+                s = f * ri;
+                c = g * ri;
                 g = d[i + 1] - p;
                 r = (d[i] - g) * s + 2.0 * c * b;
                 p = s * r;
