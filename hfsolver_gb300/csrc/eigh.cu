@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(32) trd_kernel(int n, const double* __restrict
     double* vs = rows + (size_t)rpb * n;  // reflector, indexed by column
     double* ws = vs + n;                  // p, then w
     double* xs = ws + n;                  // row k of the current matrix
+    double* rs = xs + n;                  // the published row k+1, fetched with p
     for (int r = 0; r < nown; ++r) {
         const double* src = A + (size_t)(b + r * G) * n;  // column = row (symmetric)
         for (int j = lane; j < n; j += 32) rows[(size_t)r * n + j] = src[j];
@@ -110,10 +111,13 @@ __global__ void __launch_bounds__(32) trd_kernel(int n, const double* __restrict
             if (lane == 0) pk[i] = t * acc;
         }
         if (!trd_barrier(sync, G, (unsigned)k + 1)) return;
-        // w = p - (tau/2)(p.v) v
+        // w = p - (tau/2)(p.v) v; the published row k+1 (as it was before this
+        // column) is fetched in the same pass, so its L2 latency overlaps p's
+        const double* prow = k == 0 ? A + n : pub + (size_t)(k & 1) * n;
         double pv = 0.0;
         for (int j = base + lane; j < n; j += 32) {
             const double p = __ldcg(pk + j);
+            rs[j] = __ldcg(prow + j);
             ws[j] = p;
             pv = fma(p, vs[j], pv);
         }
@@ -129,10 +133,9 @@ __global__ void __launch_bounds__(32) trd_kernel(int n, const double* __restrict
             const double vi = vs[i], wi = ws[i];
             for (int j = base + lane; j < n; j += 32) row[j] -= fma(vi, ws[j], wi * vs[j]);
         }
-        // row k+1 of the updated matrix (v[base] = 1), as published before this column
-        const double* prow = k == 0 ? A + n : pub + (size_t)(k & 1) * n;
+        // row k+1 of the updated matrix (v[base] = 1)
         const double w0 = ws[base];
-        for (int j = base + lane; j < n; j += 32) xs[j] = __ldcg(prow + j) - fma(w0, vs[j], ws[j]);
+        for (int j = base + lane; j < n; j += 32) xs[j] = rs[j] - fma(w0, vs[j], ws[j]);
         // the owner of row k+2 publishes it for the next column
         const int nxt = base + 1;
         if (nxt < n && nxt % G == b) {
@@ -198,7 +201,7 @@ constexpr int TRD_MAX_N = 1024;
 
 int trd_blocks(const Context& ctx, int n) { return std::max(1, std::min(ctx.num_sms, n / 2)); }
 
-size_t trd_smem(int n, int G) { return ((size_t)(n + G - 1) / G + 3) * n * sizeof(double); }
+size_t trd_smem(int n, int G) { return ((size_t)(n + G - 1) / G + 4) * n * sizeof(double); }
 
 }  // namespace
 

@@ -49,8 +49,15 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
         for (int j = 0; j <= i; j++) hp[(size_t)i * (i + 1) / 2 + j] = make_int2(i, j);
     DBuf<int2> pairs = to_device(hp, st);
     Sliced B1, B2, A;
+    // steps 2 and 4 (N = v) read their FP64 rows straight into the gather-fed GEMM
+    // (coalesced rows, no slice planes through HBM) while the virtual block spans
+    // at most DENSE_GATHER_TILES output tiles of 80 columns; wider ones use slicing
+    // + TMA.  The gather GEMM walks whole 80-column tiles of B, so C2's slices are
+    // then padded to a multiple of 80 rows.
+    constexpr int DENSE_GATHER_TILES = 2;
+    const bool dense_gather = n2 <= 80 * DENSE_GATHER_TILES;
     slice_dense(ctx, C1, n1, n, n, B1, SLICE_TILE_B);  // rows of B^T = columns of C1
-    slice_dense(ctx, C2, n2, n, n, B2, SLICE_TILE_B);
+    slice_dense(ctx, C2, n2, n, n, B2, dense_gather ? 80 : SLICE_TILE_B);
     ctx.trace_mark("mp2 slice C");
     const int64_t nq = (int64_t)n1 * n2;
     // gather-fed GEMMs for steps 1 and 3 when C1's columns fit one output tile of
@@ -68,11 +75,6 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
         ctx.trace_mark("mp2 row max");
     }
     DBuf<double> Z((size_t)npair * nq, st);
-    // steps 2 and 4 (N = v) read their FP64 rows straight into the gather-fed GEMM
-    // (coalesced rows, no slice planes through HBM) while the virtual block spans
-    // at most DENSE_GATHER_TILES output tiles of 80 columns; wider ones use slicing + TMA
-    constexpr int DENSE_GATHER_TILES = 2;
-    const bool dense_gather = n2 <= 80 * DENSE_GATHER_TILES;
     // steps 1-2 over blocks of pairs
     const int64_t pb = std::max<int64_t>(1, SLICE_BUDGET_ROWS / n);
     const int64_t qb_rows2 = std::max<int64_t>(1, SLICE_BUDGET_ROWS / std::max(n, n1));

@@ -47,7 +47,10 @@ def test_sliced_gemm_exact_on_small_integers():
     assert np.array_equal(sliced(A, B), A @ B)
 
 
-@pytest.mark.parametrize("nw,seed", [(2, 3), (4, 0)])
+# 2 and 4 waters: 40 and 80 virtual orbitals (one 64- or 80-column tile); 5 and 7 waters:
+# 100 and 140 (two 80-column tiles of the gather-fed steps 2 and 4, with the virtual
+# slices padded to whole tiles); 1 water: 20 virtual orbitals
+@pytest.mark.parametrize("nw,seed", [(1, 0), (2, 3), (4, 0), (5, 1), (7, 2)])
 def test_mixed_mp2_matches_fp64(nw, seed):
     from hfsolver_gb300.clusters import water_cluster
 
