@@ -59,6 +59,7 @@ SIGNATURES = {
     "hfgpu_formG": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
     "hfgpu_eigh": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, _dp]),
     "hfgpu_tridiag_eigen": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, _dp]),
+    "hfgpu_md_flops": (ctypes.c_double, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "hfgpu_jk": (ctypes.c_int, _BASIS + [_dp, ctypes.c_double, _dp, _dp]),
     "hfgpu_mp2_energy": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, ctypes.c_int, _dp]),
     "hfgpu_formG_device_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -354,6 +354,12 @@ int hfgpu_eigh(int n, const double* A, const double* B, double* lam, double* C)
     });
 }
 
+double hfgpu_md_flops(int la, int lb, int lc, int ld)
+{
+    if (la < 0 || lb < 0 || lc < 0 || ld < 0) return 0.0;
+    return md_flops(la, lb, lc, ld);
+}
+
 int hfgpu_tridiag_eigen(int n, const double* d, const double* e, double* lam, double* Z)
 {
     return guard([&] {

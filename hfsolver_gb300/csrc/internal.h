@@ -156,6 +156,9 @@ struct Context {
 // kernel for m, n, k <= 512 (gemm_small.cu), cuBLAS beyond
 void gemm(Context& ctx, bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda,
           const double* B, int ldb, double beta, double* C, int ldc);
+// algorithmic FP64 flops of one primitive shell quartet (la lb | lc ld): the fixed
+// McMurchie-Davidson count of the ERI roofline (eri.cu)
+double md_flops(int la, int lb, int lc, int ld);
 Context& context();  // for the current device
 Context* context_acquire();        // a separate context on the current device (pooled)
 void context_release(Context* c);  // back to the pool

@@ -120,6 +120,11 @@ int hfgpu_jk(int nbf, const int *nprim, const int *istart, const double *xcenter
  * tridiagonal problem; cuSOLVER dsygvd for n < 3 or n > 1024. */
 int hfgpu_eigh(int n, const double *A, const double *B, double *lam, double *C);
 
+/* the algorithmic FP64 flop count of one primitive shell quartet of angular momenta
+ * (la lb | lc ld) used for the ERI roofline (McMurchie-Davidson count,
+ * hfsolver_gb300/roofline.py states the same formula); host only */
+double hfgpu_md_flops(int la, int lb, int lc, int ld);
+
 /* the host half of hfgpu_eigh: eigenvalues lam (ascending) and orthonormal
  * eigenvectors Z (n x n, column-major) of the symmetric tridiagonal matrix with
  * diagonal d (n) and off-diagonal e (n - 1).  Implicit QL for the eigenvalues,
