@@ -88,3 +88,20 @@ def test_invalid_input_is_a_status_not_an_abort(L):
     rc = Lb.hfgpu_getints2(n, arr_i, arr_i, arr_d, arr_p, 1, c1, c1, out, 7)
     assert rc == _lib.ERR_INVALID
     assert b"m(m+1)/2" in Lb.hfgpu_last_error()
+
+
+def test_eigh_rejects_bad_arguments_before_the_gpu(L):
+    """hfgpu_eigh validates sizes and pointers on the host (no device work)."""
+    import hfsolver_gb300 as hf
+    from hfsolver_gb300 import _lib
+
+    buf = (ctypes.c_double * 4)()
+    assert L.hfgpu_eigh(0, buf, buf, buf, buf) == _lib.ERR_INVALID
+    assert L.hfgpu_eigh(2, None, buf, buf, buf) == _lib.ERR_INVALID
+    assert L.hfgpu_eigh(2, buf, buf, buf, None) == _lib.ERR_INVALID
+    with pytest.raises(ValueError):
+        hf.eigh(np.eye(3), np.eye(2))
+    # the host tridiagonal solver: sizes and non-finite input
+    assert L.hfgpu_tridiag_eigen(0, buf, buf, buf, buf) == _lib.ERR_INVALID
+    with pytest.raises(ValueError):
+        hf.tridiag_eigen([1.0, 2.0], [])
