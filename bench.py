@@ -43,6 +43,20 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(values):
+    """Element-wise maximum of a list of floats over the ranks of the process group
+    (the slowest replica sets a whole-job time); the values unchanged with one rank."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.cpu()]
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -258,9 +272,7 @@ def run_gpu(args):
     ms_o, res_o, _ = timed_steps(L, stream, max(1, args.steps // 2), lambda: hf.rhf(atno, xyz, opt_other))
     barrier()
     if world > 1:
-        t = torch.tensor([ms, ms_e2e, ms_o], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, ms_e2e, ms_o = (float(x) for x in t)
+        ms, ms_e2e, ms_o = max_over_ranks([ms, ms_e2e, ms_o])
     if rank != 0:
         return 0
     r = results[-1]
@@ -382,9 +394,7 @@ def run_batch(args):
     torch.cuda.synchronize()
     wall_plain = time.perf_counter() - t1
     if world > 1:
-        t = torch.tensor([wall, wall_plain], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        wall, wall_plain = (float(x) for x in t)
+        wall, wall_plain = max_over_ranks([wall, wall_plain])
     if rank != 0:
         return 0
     failed = sum(1 for r in res if r["niter"] <= 0)
