@@ -78,6 +78,8 @@ SIGNATURES = {
                                           _dp]),
     "hfgpu_autotune_table": (ctypes.c_int64, [ctypes.c_char_p, ctypes.c_int64]),
     "hfgpu_autotune_clear": (None, []),
+    "hfgpu_boys": (ctypes.c_int, [ctypes.c_int, ctypes.c_int64, _dp, _dp]),
+    "hfgpu_grid_barrier_check": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp]),
 }
 
 _LIB = None

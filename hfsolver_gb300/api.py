@@ -192,6 +192,15 @@ def tridiag_eigen(d, e):
     return lam, Z
 
 
+def boys(maxm, T):
+    """F_0..F_maxm at each T, by the ERI kernels' device routine (diagnostic);
+    array of shape (len(T), maxm + 1)."""
+    T = _f64(np.atleast_1d(T))
+    F = np.zeros((T.size, maxm + 1))
+    _check(_lib.lib().hfgpu_boys(int(maxm), T.size, _d(T), F.ctypes.data_as(_dp)))
+    return F
+
+
 def formG(P, int2):
     """G = J - K/2 from the packed integrals (scf.f90:26-58)."""
     P = np.asfortranarray(P, dtype=np.float64)

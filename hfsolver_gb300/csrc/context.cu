@@ -97,6 +97,7 @@ static Context* make_context(int dev)
     boys_make_table(tab.data());
     HF_CUDA(cudaMalloc((void**)&c->boys, tab.size() * sizeof(double)));
     HF_CUDA(cudaMemcpy(c->boys, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+    noalloc_prepare(dev);
     return c;
 }
 

@@ -2,8 +2,9 @@
 // Barrier number `epoch` (1, 2, ...) completes when the count reaches
 // epoch * nblocks; the arrival is a release and the wait an acquire, so the
 // writes a block made before the barrier are visible to every block after it
-// (no separate fences).  The wait gives up after 2 s and sets *err, so a grid
-// that was not co-resident cannot spin forever.
+// (no separate fences).  The wait gives up after limit_ns (2 s unless the caller
+// says otherwise) and sets *err, so a grid that was not co-resident cannot spin
+// forever.
 #pragma once
 #include <cstdint>
 
@@ -29,7 +30,8 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
 }
 
 // called by one thread per block; true unless the wait timed out (then *err = 1)
-__device__ __forceinline__ bool grid_arrive_wait(unsigned* count, int* err, unsigned nblocks, unsigned epoch)
+__device__ __forceinline__ bool grid_arrive_wait(unsigned* count, int* err, unsigned nblocks, unsigned epoch,
+                                                 uint64_t limit_ns = 2000000000ull)
 {
     red_add_release(count, 1u);
     const unsigned target = epoch * nblocks;
@@ -39,7 +41,7 @@ __device__ __forceinline__ bool grid_arrive_wait(unsigned* count, int* err, unsi
         if ((++spins & 1023u) == 0) {
             if (t0 == 0) {
                 t0 = global_ns();
-            } else if (global_ns() - t0 > 2000000000ull) {
+            } else if (global_ns() - t0 > limit_ns) {
                 atomicExch(err, 1);
                 break;
             }

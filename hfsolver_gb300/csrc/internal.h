@@ -243,4 +243,10 @@ void rhf_gradient(Context& ctx, EriPlan* plan, int natoms, const int* atno, cons
 // probe.cu: measured FP64 FMA rate (TFLOP/s)
 double probe_fp64_tflops(Context& ctx);
 
+// noalloc.cu: load the module that holds the allocation-free Fock build's fixed
+// scratch array on device dev (the current device) and cache its device
+// address; called when a device context is created, so that the array's device
+// memory is taken then and not at the first allocation-free call
+void noalloc_prepare(int dev);
+
 }  // namespace hfgpu

@@ -6,8 +6,8 @@
 // process running under a fixed device-memory quota, or a caller inside a
 // latency-critical loop where a cudaMalloc would synchronise the device.  They
 // pass device pointers for the inputs and the output; the only extra memory is
-// the scratch array below, a fixed 2 MiB per device, created when the library
-// is loaded and held until the process exits.
+// the scratch array below, a fixed 2 MiB per device, taken when this module is
+// loaded on the device (see noalloc_setup) and held until the process exits.
 //
 // The computation is the Fock two-electron term of hfgpu_formG (same
 // arithmetic as jk.cu: each unique packed integral is read once and scattered
@@ -85,7 +85,13 @@ __global__ void noalloc_symmetrize_kernel(int n, const double* __restrict__ Gh, 
 }
 
 // Device address of the scratch array, looked up once per device with that
-// device current (the host-side name g_formG_scratch is only a stand-in).
+// device current (the host-side name g_formG_scratch is only a stand-in).  The
+// lookup loads this file's module on the device, which is when the 2 MiB array
+// is allocated (CUDA loads modules lazily by default).  Every libhfgpu entry
+// point that creates the library's device context does this, and so does the
+// first allocation-free call on a device that has no context yet.  The cached
+// address belongs to the device's current primary context: calls must not cross
+// a cudaDeviceReset.
 static std::mutex g_noalloc_mutex;
 static double* g_noalloc_ptr[64] = {nullptr};
 static int g_noalloc_sms[64] = {0};
@@ -96,16 +102,26 @@ static void noalloc_setup(int dev, double** ptr, int* sms)
     HF_CHECK(dev >= 0 && dev < 64, HFGPU_ERR_INVALID, "device ordinal out of range");
     if (!g_noalloc_ptr[dev]) {
         double* p = nullptr;
-        HF_CUDA(cudaGetSymbolAddress((void**)&p, g_formG_scratch));
+        const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_formG_scratch);
+        if (e == cudaErrorMemoryAllocation) {
+            cudaGetLastError();
+            throw Error(HFGPU_ERR_NOMEM,
+                        "hfgpu_formG_device_noalloc: no device memory left for its fixed 2 MiB scratch array "
+                        "(taken when the library's module is first loaded on the device; make the first "
+                        "libhfgpu call before reserving the device's memory)");
+        }
+        HF_CUDA(e);
         HF_CHECK(p != nullptr, HFGPU_ERR_CUDA, "cudaGetSymbolAddress returned no address");
         int s = 0;
         HF_CUDA(cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev));
         g_noalloc_sms[dev] = s;
         g_noalloc_ptr[dev] = p;
     }
-    *ptr = g_noalloc_ptr[dev];
-    *sms = g_noalloc_sms[dev];
+    if (ptr) *ptr = g_noalloc_ptr[dev];
+    if (sms) *sms = g_noalloc_sms[dev];
 }
+
+void noalloc_prepare(int dev) { noalloc_setup(dev, nullptr, nullptr); }
 
 }  // namespace hfgpu
 
@@ -119,6 +135,12 @@ extern "C" int hfgpu_formG_device_noalloc(int n, const double* d_int2, const dou
                  "hfgpu_formG_device_noalloc: n = " + std::to_string(n) + " exceeds its fixed scratch limit of " +
                      std::to_string(NOALLOC_MAX_N) + " basis functions");
         HF_CHECK(d_int2 && d_P && d_G, HFGPU_ERR_INVALID, "device pointers must not be NULL");
+        // an error left by the caller's own earlier asynchronous work is reported as
+        // such and left pending, not taken for a failure of this call
+        const cudaError_t pending = cudaPeekAtLastError();
+        if (pending != cudaSuccess)
+            throw Error(HFGPU_ERR_CUDA, std::string("hfgpu_formG_device_noalloc: a CUDA error was already pending "
+                                                    "before this call: ") + cudaGetErrorString(pending));
         int dev = 0;
         HF_CUDA(cudaGetDevice(&dev));
         double* Gh = nullptr;

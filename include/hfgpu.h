@@ -134,7 +134,9 @@ int hfgpu_tridiag_eigen(int n, const double *d, const double *e, double *lam, do
 
 /* replaces formG / formG2, src/scf.f90:26-58: G(i,j) = sum_kl P(k,l) [(ij|kl) - (il|kj)/2]
  * from the packed integrals, without the reference's dense TT(n,n,n,n)
- * (src/scf.f90:79-105); P and G column-major n x n. */
+ * (src/scf.f90:79-105); P and G column-major n x n.  P must be symmetric (a
+ * density always is): the kernel reads both triangles and folds the
+ * permutational copies of each integral assuming P(k,l) = P(l,k). */
 int hfgpu_formG(int n, const double *P, const double *int2, double *G);
 
 /* Allocation-free variant of hfgpu_formG; it has no counterpart in the
@@ -143,14 +145,20 @@ int hfgpu_formG(int n, const double *P, const double *int2, double *G);
  * framework's caching allocator that has reserved the GPU) or by a fixed
  * quota, or a latency-critical loop where a cudaMalloc would synchronise the
  * device.  Inputs and output are DEVICE pointers owned by the caller:
- * d_int2 (packed, m(m+1)/2 doubles), d_P and d_G (n x n, column-major).  The
- * work is enqueued on cuda_stream (a cudaStream_t; NULL = the legacy default
- * stream) and the call returns without waiting for it.  The only scratch is a
- * fixed array of 512 x 512 doubles (2 MiB) per device that is created when the
- * library is loaded and kept until the process exits, so n <= 512 (larger n
- * returns HFGPU_ERR_INVALID).  The first call on a device looks up that
- * array's device address, so make it before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race. */
+ * d_int2 (packed, m(m+1)/2 doubles), d_P and d_G (n x n, column-major; P
+ * symmetric, as for hfgpu_formG).  The work is enqueued on cuda_stream (a
+ * cudaStream_t; NULL = the legacy default stream) and the call returns without
+ * waiting for it.  The only scratch is a fixed array of 512 x 512 doubles
+ * (2 MiB) per device, kept until the process exits, so n <= 512 (larger n
+ * returns HFGPU_ERR_INVALID).  That array's memory is taken when the library's
+ * module is loaded on the device: by any libhfgpu call that sets up the
+ * library on that device, or else by the first call of this function there,
+ * which also looks up the array's device address.  Make that first call before
+ * reserving the device's memory (HFGPU_ERR_NOMEM otherwise) and before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race.  An error already pending in the CUDA runtime when the call starts is
+ * returned as HFGPU_ERR_CUDA without launching anything.  Calls must not cross
+ * a cudaDeviceReset (the cached address belongs to the device's context). */
 int hfgpu_formG_device_noalloc(int n, const double *d_int2, const double *d_P, double *d_G, void *cuda_stream);
 
 /* replaces transform_int2, src/mbpt.f90:11-79: (mu nu|la si) -> (ij|kl) over
@@ -279,6 +287,27 @@ void hfgpu_autotune_clear(void);
 
 /* number of basis functions hfgpu_rhf will use for these atoms (0 on error) */
 int hfgpu_basis_size(int natoms, const int *atno);
+
+/* ---- Diagnostics: device routines of the kernels, one at a time ------------ */
+
+/* The Boys function F_0(T) .. F_maxm(T) (0 <= maxm <= 12) for nt values T[t] >= 0,
+ * evaluated by the device routine the ERI kernels use: F[t (maxm+1) + m] =
+ * F_m(T[t]).  The same quantity as the reference's Fm
+ * (src/special_functions.f90:189-248, called through src/cints.c:28-33);
+ * host arrays.  HFGPU_ERR_INVALID for T < 0 or non-finite, as the reference
+ * stops there (src/special_functions.f90:218-221). */
+int hfgpu_boys(int maxm, int64_t nt, const double *T, double *F);
+
+/* The bounded grid barrier of the cooperative SP2 and tridiagonalisation
+ * kernels, with a caller-set time limit: launched_blocks blocks (at most one
+ * per SM, so all are resident) arrive at a barrier that waits for
+ * expected_blocks.  HFGPU_OK when the barrier completed; with fewer blocks
+ * launched than expected the wait runs out after limit_ms (0 < limit_ms <=
+ * 2000), every block returns with the error flag set and the call returns
+ * HFGPU_ERR_CUDA, the device staying usable.  elapsed_ms (may be NULL) gets
+ * the kernel's duration.  No counterpart in the reference, which has no device
+ * code; it tests the failure path that replaces a hang. */
+int hfgpu_grid_barrier_check(int launched_blocks, int expected_blocks, double limit_ms, double *elapsed_ms);
 
 #ifdef __cplusplus
 }

@@ -13,7 +13,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = os.environ.get("HFSOLVER_REFERENCE_SRC", "/root/reference/src")
+# the reference checkout: HFSOLVER_REFERENCE_SRC, else a checkout named
+# "reference" beside this repository
+REF_SRC = os.environ.get("HFSOLVER_REFERENCE_SRC") or os.path.normpath(
+    os.path.join(HERE, "..", "..", "reference", "src"))
 CFLAGS = ["-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
 
 

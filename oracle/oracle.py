@@ -81,6 +81,10 @@ def _bind(L, prefix="oracle_"):
         L.oracle_ijkl.restype = ctypes.c_int64
         L.oracle_formG_entries.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_int64, _ip, _dp]
         L.oracle_formG_entries.restype = None
+        L.oracle_formG_scatter.argtypes = [ctypes.c_int, _dp, _dp, _dp]
+        L.oracle_formG_scatter.restype = None
+        L.oracle_getInts_screened.argtypes = basis_args + [ctypes.c_double, _dp, _dp]
+        L.oracle_getInts_screened.restype = None
 
 
 def _d(a):
@@ -254,9 +258,16 @@ def one_electron(basis, which, L=None, prefix="oracle_"):
     return out.reshape(n, n, order="F")
 
 
-def getInts(basis, L=None, prefix="oracle_"):
+def getInts(basis, L=None, prefix="oracle_", screen=0.0):
+    """All unique (ij|kl), packed (qc.c:95-131).  screen > 0 leaves quartets
+    whose Schwarz bound sqrt((ij|ij)(kl|kl)) is below it at zero (not a
+    reference option; used only for oracle fixtures beyond 200 functions)."""
     L = L or lib()
     out = np.zeros(n_ints(basis.n))
+    if screen > 0:
+        Q = np.zeros(basis.n * (basis.n + 1) // 2)
+        lib().oracle_getInts_screened(*basis.cargs(), float(screen), _d(Q), _d(out))
+        return out
     getattr(L, prefix + "getInts")(*basis.cargs(), _d(out))
     return out
 
@@ -283,12 +294,13 @@ def formP(C, nocc):
     return 2 * Co @ Co.T
 
 
-def formG(P, int2):
-    """G = J - K/2 from the packed integrals (scf.f90:26-58)."""
+def formG(P, int2, scatter=False):
+    """G = J - K/2 from the packed integrals (scf.f90:26-58).  scatter=True
+    sums the same terms by reading each unique integral once (for n > 200)."""
     n = P.shape[0]
     Pf = np.asfortranarray(P)
     G = np.zeros((n, n), order="F")
-    lib().oracle_formG(n, _d(Pf), _d(int2), _d(G))
+    (lib().oracle_formG_scatter if scatter else lib().oracle_formG)(n, _d(Pf), _d(int2), _d(G))
     return np.array(G)
 
 
@@ -299,7 +311,7 @@ def eigh(F, S):
     return scipy.linalg.eigh(F, S, lower=True, driver="gvd")
 
 
-def doscf(H, int2, S, nocc, nscf, tolE, tolP, alpha, verbose=False, diis=0):
+def doscf(H, int2, S, nocc, nscf, tolE, tolP, alpha, verbose=False, diis=0, scatter=False):
     """Restates scf.f90:72-136 (P = 0 start, linear mixing, 4-energy window).
 
     diis > 0 replaces the linear mixing by Pulay DIIS with that many vectors
@@ -310,7 +322,7 @@ def doscf(H, int2, S, nocc, nscf, tolE, tolP, alpha, verbose=False, diis=0):
     Escf = []
     hist_F, hist_e = [], []
     for it in range(nscf):
-        G = formG(P, int2)
+        G = formG(P, int2, scatter)
         F = H + G
         E0 = 0.5 * np.sum(P * (H + F))
         Escf.append(E0)
@@ -357,15 +369,18 @@ def nuclear_energy(atno, xyz):
     return E
 
 
-def rhf_gauss(atno, xyz, nscf=40, alpha=1.0, tolE=1e-10, tolP=1e-8, verbose=False, diis=0):
-    """drivers.f90:12-51: integrals, H = T + V, SCF with Nocc = sum(atno)/2."""
+def rhf_gauss(atno, xyz, nscf=40, alpha=1.0, tolE=1e-10, tolP=1e-8, verbose=False, diis=0, screen=0.0,
+              scatter=False):
+    """drivers.f90:12-51: integrals, H = T + V, SCF with Nocc = sum(atno)/2.
+    screen and scatter (see getInts, formG) only speed up fixtures of 300-400
+    functions; the defaults follow the reference."""
     b = Basis(atno, xyz)
     S = one_electron(b, "S")
     T = one_electron(b, "T")
     V = one_electron(b, "V")
-    int2 = getInts(b)
+    int2 = getInts(b, screen=screen)
     H = T + V
-    r = doscf(H, int2, S, int(sum(atno)) // 2, nscf, tolE, tolP, alpha, verbose, diis)
+    r = doscf(H, int2, S, int(sum(atno)) // 2, nscf, tolE, tolP, alpha, verbose, diis, scatter)
     Enuc = nuclear_energy(b.atno, b.xyz)
     r.update(basis=b, S=S, T=T, V=V, H=H, int2=int2, Enuc=Enuc, Ekin=float(np.sum(r["P"] * T)),
              Etot=r["E0"] + Enuc)
@@ -455,10 +470,12 @@ def mbpt3(moint2, lam, nocc):
     return float(t1 + t2 + t3)
 
 
-def mp2_semidirect(int2, C, lam, nocc, block=8):
+def mp2_semidirect(int2, C, lam, nocc, block=None):
     """The same E2 as mbpt2(transform_int2(...)), built from (ia|jb) only, in
     blocks of mu so that no n^4 tensor is formed (for n beyond 120)."""
     n = C.shape[0]
+    if block is None:
+        block = max(1, min(8, int(1.0e8 // n ** 3)))
     Co, Cv = C[:, :nocc], C[:, nocc:]
     iajb = np.zeros((nocc, n - nocc, nocc, n - nocc))
     i = np.arange(n)

@@ -22,6 +22,7 @@
  */
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #ifndef M_PI
@@ -168,6 +169,39 @@ void oracle_getInts(int nbf, const int *nprim, const int *istart, const double *
                 for (int l = 0; l < k + 1; l++) {
                     int64_t kl = (int64_t)k * (k + 1) / 2 + l;
                     if (ij >= kl)
+                        Ints[oracle_ijkl(i, j, k, l)] = eri_contracted(
+                            nprim, istart, xc, yc, zc, lp, mp, np, coef, alpha, i, j, k, l);
+                }
+        }
+}
+
+/* oracle_getInts with quartets left at zero when their Schwarz bound
+ * sqrt((ij|ij)) sqrt((kl|kl)) is below thr.  Not a reference routine (the
+ * reference computes every quartet): it makes oracle fixtures of 300-400
+ * functions affordable.  With thr far below the GPU path's cut (1e-16 against
+ * 1e-12) the dropped integrals are below 1e-16 each; the fixture generator
+ * checks the screened oracle against the unscreened one at 200 functions.
+ * Ints must be zero on entry; Q (nbf(nbf+1)/2 doubles) receives the bounds. */
+void oracle_getInts_screened(int nbf, const int *nprim, const int *istart, const double *xc,
+                             const double *yc, const double *zc, const int *lp, const int *mp,
+                             const int *np, int n2, const double *coef, const double *alpha,
+                             double thr, double *Q, double *Ints)
+{
+    (void)n2;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int i = 0; i < nbf; i++)
+        for (int j = 0; j <= i; j++) {
+            double d = eri_contracted(nprim, istart, xc, yc, zc, lp, mp, np, coef, alpha, i, j, i, j);
+            Q[(int64_t)i * (i + 1) / 2 + j] = sqrt(fabs(d));
+        }
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = nbf - 1; i >= 0; i--)
+        for (int j = 0; j < i + 1; j++) {
+            int64_t ij = (int64_t)i * (i + 1) / 2 + j;
+            for (int k = 0; k < nbf; k++)
+                for (int l = 0; l < k + 1; l++) {
+                    int64_t kl = (int64_t)k * (k + 1) / 2 + l;
+                    if (ij >= kl && Q[ij] * Q[kl] >= thr)
                         Ints[oracle_ijkl(i, j, k, l)] = eri_contracted(
                             nprim, istart, xc, yc, zc, lp, mp, np, coef, alpha, i, j, k, l);
                 }
@@ -342,6 +376,62 @@ void oracle_formG(int n, const double *P, const double *int2, double *G)
                 }
             G[i + (int64_t)j * n] = acc;
         }
+}
+
+/* The same G as oracle_formG, summed in a different order: each unique packed
+ * integral (ij|kl) is read once and its eight permutations are scattered into
+ * G (J from the (ij) and (kl) pairs, K from the four cross pairs).  n^4/8 reads
+ * instead of formG2's 2 n^4 gathers, for oracle SCF runs beyond 200 functions.
+ * Per-thread G accumulators are summed at the end.  G is column-major n x n. */
+void oracle_formG_scatter(int n, const double *P, const double *int2, double *G)
+{
+    const int64_t m = (int64_t)n * (n + 1) / 2;
+    const int64_t nn = (int64_t)n * n;
+    for (int64_t e = 0; e < nn; e++) G[e] = 0.;
+#pragma omp parallel
+    {
+        double *Gt = (double *)calloc((size_t)nn, sizeof(double));
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t ij = 0; ij < m; ij++) {
+            int i = (int)((sqrt(8.0 * (double)ij + 1.0) - 1.0) / 2.0);
+            while ((int64_t)i * (i + 1) / 2 > ij) i--;
+            while ((int64_t)(i + 1) * (i + 2) / 2 <= ij) i++;
+            int j = (int)(ij - (int64_t)i * (i + 1) / 2);
+            const double *row = int2 + ij * (ij + 1) / 2;
+            int k = 0, l = 0;
+            for (int64_t kl = 0; kl <= ij; kl++) {
+                double v = row[kl];
+                if (v != 0.) {
+                    /* weight: each distinct member of the 8-fold orbit once */
+                    double w = v;
+                    if (i == j) w *= 0.5;
+                    if (k == l) w *= 0.5;
+                    if (ij == kl) w *= 0.5;
+                    /* J: member (x y|z w) adds v P(z,w) to G(x,y) */
+                    double pkl = P[k + (int64_t)l * n] + P[l + (int64_t)k * n];
+                    double pij = P[i + (int64_t)j * n] + P[j + (int64_t)i * n];
+                    Gt[i + (int64_t)j * n] += w * pkl;
+                    Gt[j + (int64_t)i * n] += w * pkl;
+                    Gt[k + (int64_t)l * n] += w * pij;
+                    Gt[l + (int64_t)k * n] += w * pij;
+                    /* K: member (x y|z w) adds -v/2 P(z,y) to G(x,w) */
+                    double hw = 0.5 * w;
+                    Gt[i + (int64_t)l * n] -= hw * P[k + (int64_t)j * n];
+                    Gt[j + (int64_t)l * n] -= hw * P[k + (int64_t)i * n];
+                    Gt[i + (int64_t)k * n] -= hw * P[l + (int64_t)j * n];
+                    Gt[j + (int64_t)k * n] -= hw * P[l + (int64_t)i * n];
+                    Gt[k + (int64_t)j * n] -= hw * P[i + (int64_t)l * n];
+                    Gt[l + (int64_t)j * n] -= hw * P[i + (int64_t)k * n];
+                    Gt[k + (int64_t)i * n] -= hw * P[j + (int64_t)l * n];
+                    Gt[l + (int64_t)i * n] -= hw * P[j + (int64_t)k * n];
+                }
+                if (++l > k) { k++; l = 0; }
+            }
+        }
+#pragma omp critical
+        for (int64_t e = 0; e < nn; e++) G[e] += Gt[e];
+        free(Gt);
+    }
 }
 
 /* G(i,j) of formG2 for a list of (i,j) entries only (bounded timing samples of

@@ -105,3 +105,18 @@ def test_eigh_rejects_bad_arguments_before_the_gpu(L):
     assert L.hfgpu_tridiag_eigen(0, buf, buf, buf, buf) == _lib.ERR_INVALID
     with pytest.raises(ValueError):
         hf.tridiag_eigen([1.0, 2.0], [])
+
+
+def test_boys_rejects_bad_arguments_before_the_gpu(L):
+    """hfgpu_boys checks its arguments on the host, as the reference's Fm stops
+    on them (src/special_functions.f90:218-221)."""
+    from hfsolver_gb300 import _lib
+
+    T = (ctypes.c_double * 2)(1.0, -1.0)
+    F = (ctypes.c_double * 40)()
+    assert L.hfgpu_boys(13, 1, T, F) == _lib.ERR_INVALID
+    assert L.hfgpu_boys(-1, 1, T, F) == _lib.ERR_INVALID
+    assert L.hfgpu_boys(4, 2, T, F) == _lib.ERR_INVALID
+    assert b"T must be" in L.hfgpu_last_error()
+    T[1] = float("nan")
+    assert L.hfgpu_boys(4, 2, T, F) == _lib.ERR_INVALID

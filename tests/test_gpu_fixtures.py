@@ -1,11 +1,19 @@
-"""Full-size parity on seeded water clusters (2, 4, 8 waters; up to 200
-functions) against oracle fixtures made by tests/golden/make_fixtures.py (THO
-integrals for every unique quartet, no screening, converged to dP < 1e-10).
+"""Full-size parity on seeded water clusters against oracle fixtures made by
+tests/golden/make_fixtures.py, converged to dP < 1e-10:
+
+* 2, 4, 8 waters (up to 200 functions): THO integrals for every unique
+  quartet, no screening, as the reference computes them;
+* 12 waters (300 functions) and the 16-water precision workload (400
+  functions, 11 A cube): THO integrals with quartets below a Schwarz bound of
+  1e-16 left out on the oracle side (pinned against the unscreened oracle at 8
+  waters: |dE_HF| 2.3e-13, |dE2| 8e-15);
+* a seeded subset of the batch workload (water_batch(256, seed=0): 1-12 waters
+  with 0.05 A jitter), run through one batched call.
 
 The GPU runs the production configuration (Schwarz cut 1e-12, DIIS) and must
 agree to |dE_HF| <= 1e-10 Ha and |dE_MP2| <= 1e-8 Ha, with both the FP64 and
-the tensor-core MBPT2; 400 packed integrals at fixed random positions must
-agree to 1e-12 + 1e-12 |v|."""
+the tensor-core MBPT2; up to 8 waters, 400 packed integrals at fixed random
+positions must agree to 1e-12 + 1e-12 |v|."""
 import json
 import os
 
@@ -13,54 +21,61 @@ import numpy as np
 import pytest
 
 import hfsolver_gb300 as hf
-from hfsolver_gb300.clusters import water_cluster
+from hfsolver_gb300.clusters import water_batch, water_cluster
 
 pytestmark = pytest.mark.gpu
 
 FIX = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "water_clusters.json")))
+SIZES = sorted((k for k in FIX if k.isdigit()), key=int)
+TOL_E, TOL_E2 = 1e-10, 1e-8
 
 
-@pytest.mark.parametrize("nw", sorted(FIX, key=int))
+def _molecule(f):
+    return water_cluster(f["n_waters"], box=f.get("box_ang"), seed=f["seed"])
+
+
+@pytest.mark.parametrize("nw", SIZES)
 @pytest.mark.parametrize("mp2", ["fp64", "split_bf16"])
 def test_cluster_energies(nw, mp2):
     f = FIX[nw]
-    atno, xyz = water_cluster(f["n_waters"], seed=f["seed"])
+    atno, xyz = _molecule(f)
     r = hf.rhf(atno, xyz, hf.RHFOptions(nscf=60, diis=True, schwarz=1e-12, tolP=1e-10, tolE=1e-12, mp2=mp2))
     assert r["nbf"] == f["nbf"]
-    assert abs(r["Etot"] - f["Etot"]) <= 1e-10
-    assert abs(r["E2"] - f["E2"]) <= 1e-8
+    assert abs(r["Etot"] - f["Etot"]) <= TOL_E, r["Etot"] - f["Etot"]
+    assert abs(r["E2"] - f["E2"]) <= TOL_E2, r["E2"] - f["E2"]
 
 
-@pytest.mark.parametrize("nw", sorted(FIX, key=int))
+@pytest.mark.parametrize("nw", SIZES)
 def test_cluster_energies_bench_configuration(nw):
-    """The bench's SCF: DIIS, SP2 purification and Fock builds from screened
-    density differences (full rebuild every 8 iterations and at convergence)."""
+    """The bench's SCF: DIIS, SP2 purification, Fock builds from screened
+    density differences (full rebuild every 8 iterations and at convergence),
+    atomic-density start, tensor-core MBPT2."""
     f = FIX[nw]
-    atno, xyz = water_cluster(f["n_waters"], seed=f["seed"])
+    atno, xyz = _molecule(f)
     r = hf.rhf(atno, xyz, hf.RHFOptions(nscf=60, diis=True, schwarz=1e-12, tolP=1e-10, tolE=1e-12,
-                                        mp2="split_bf16", purify=True, incremental=True))
-    assert abs(r["Etot"] - f["Etot"]) <= 1e-10
-    assert abs(r["E2"] - f["E2"]) <= 1e-8
+                                        mp2="split_bf16", purify=True, incremental=True, guess="sad"))
+    assert abs(r["Etot"] - f["Etot"]) <= TOL_E, r["Etot"] - f["Etot"]
+    assert abs(r["E2"] - f["E2"]) <= TOL_E2, r["E2"] - f["E2"]
 
 
-@pytest.mark.parametrize("nw", sorted(FIX, key=int))
+@pytest.mark.parametrize("nw", [k for k in SIZES if int(k) <= 8])
 def test_cluster_energies_atomic_guess(nw):
     """Starting from the superposition of atomic densities reaches the same SCF
     solution as the reference's P = 0 start, in fewer iterations."""
     f = FIX[nw]
-    atno, xyz = water_cluster(f["n_waters"], seed=f["seed"])
+    atno, xyz = _molecule(f)
     o = dict(nscf=60, diis=True, schwarz=1e-12, tolP=1e-10, tolE=1e-12, mp2="fp64")
     core = hf.rhf(atno, xyz, hf.RHFOptions(**o))
     sad = hf.rhf(atno, xyz, hf.RHFOptions(guess="sad", **o))
-    assert abs(sad["Etot"] - f["Etot"]) <= 1e-10
-    assert abs(sad["E2"] - f["E2"]) <= 1e-8
+    assert abs(sad["Etot"] - f["Etot"]) <= TOL_E
+    assert abs(sad["E2"] - f["E2"]) <= TOL_E2
     assert sad["niter"] < core["niter"]
 
 
-@pytest.mark.parametrize("nw", sorted(FIX, key=int))
+@pytest.mark.parametrize("nw", [k for k in SIZES if "ints_pos" in FIX[k]])
 def test_cluster_packed_integrals(oracle, nw):
     f = FIX[nw]
-    atno, xyz = water_cluster(f["n_waters"], seed=f["seed"])
+    atno, xyz = _molecule(f)
     b = oracle.Basis(atno, xyz)
     from tests.gpu_common import basis_args
 
@@ -68,3 +83,32 @@ def test_cluster_packed_integrals(oracle, nw):
     got = ints[np.array(f["ints_pos"], dtype=np.int64)]
     ref = np.array(f["ints_val"])
     assert np.all(np.abs(got - ref) <= 1e-12 + 1e-12 * np.abs(ref))
+
+
+@pytest.mark.skipif("batch" not in FIX, reason="batch fixture not generated")
+def test_batch_subset_energies():
+    """The fixture molecules of the batch workload, all in one batched call in
+    the bench's configuration, each against its oracle energies."""
+    fb = FIX["batch"]
+    mols = water_batch(fb["count"], seed=fb["seed"])
+    sel = [mols[m["index"]] for m in fb["molecules"]]
+    opt = hf.RHFOptions(nscf=60, diis=True, schwarz=1e-12, tolP=1e-10, tolE=1e-12, mp2="split_bf16", purify=True,
+                        incremental=True, guess="sad")
+    res = hf.rhf_batch(sel, opt)
+    for f, r in zip(fb["molecules"], res):
+        assert r["niter"] > 0, f
+        assert r["nbf"] == f["nbf"]
+        assert abs(r["Etot"] - f["Etot"]) <= TOL_E, (f["index"], r["Etot"] - f["Etot"])
+        assert abs(r["E2"] - f["E2"]) <= TOL_E2, (f["index"], r["E2"] - f["E2"])
+
+
+@pytest.mark.skipif("batch" not in FIX, reason="batch fixture not generated")
+def test_batch_subset_one_at_a_time_fp64():
+    """The same molecules one at a time through the plain FP64 path."""
+    fb = FIX["batch"]
+    mols = water_batch(fb["count"], seed=fb["seed"])
+    for f in fb["molecules"]:
+        atno, xyz = mols[f["index"]]
+        r = hf.rhf(atno, xyz, hf.RHFOptions(nscf=60, diis=True, schwarz=1e-12, tolP=1e-10, tolE=1e-12, mp2="fp64"))
+        assert abs(r["Etot"] - f["Etot"]) <= TOL_E, (f["index"], r["Etot"] - f["Etot"])
+        assert abs(r["E2"] - f["E2"]) <= TOL_E2, (f["index"], r["E2"] - f["E2"])

@@ -36,3 +36,17 @@ def test_scf_nonconvergence_is_reported(oracle):
     c = CASES["H2O"]
     with pytest.raises(oracle.SCFNotConverged):
         oracle.rhf_gauss(c["atno"], np.array(c["xyz"], float), nscf=3)
+
+
+def test_screened_oracle_reproduces_unscreened_fixture():
+    """The oracle fixtures beyond 200 functions leave out quartets whose Schwarz
+    bound is below 1e-16; at 8 waters that shortcut reproduced the unscreened
+    oracle (every quartet, as the reference computes them)."""
+    import json
+
+    fix = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "water_clusters.json")))
+    if "screen_check" not in fix:
+        pytest.skip("screen_check fixture not generated")
+    c = fix["screen_check"]
+    assert abs(c["dEtot_vs_unscreened"]) <= 1e-12
+    assert abs(c["dE2_vs_unscreened"]) <= 1e-12
