@@ -2,6 +2,8 @@
 assert for the GTO path (src/tests/test_gaussians_molecules.f90,
 src/tests/test_gaussians_atoms.f90), with the reference's tolerances.  The H2
 total energy is asserted at 1e-7 in the reference (eps, :16,42)."""
+import os
+
 import numpy as np
 import pytest
 
