@@ -19,8 +19,10 @@ library's stream; `e2e` repeats the measurement through the C ABI with host
 buffers (coordinates in, orbitals out).  Multi-GPU: independent replicas, one
 molecule per rank per step (the path has no exchange step).
 `--impl reference` times hfsolver's own CPU algorithm (the oracle port of
-src/cints.c THO integrals, formG, transform_int2, term1) on a bounded sample
-of the same workload on the host cores, extrapolated to one molecule.
+src/cints.c THO integrals for every unique quartet, doscf's dense TT built
+once, formG and dsygvd per SCF iteration, transform_int2, term1) on bounded
+samples of the same workload on all host cores, scaled to one molecule, with
+the serial (one-core) cost beside it.
 """
 import argparse
 import json
@@ -125,54 +127,43 @@ def options(mp2="split_bf16"):
 
 
 # ---------------------------------------------------------------- CPU baseline
-def cpu_sample(atno, xyz, niter, budget_s=8.0, seed=0):
-    """Time hfsolver's CPU algorithm (oracle port, all host threads) on bounded
-    samples and extrapolate to one molecule:
-      ERIs  : THO contracted quartets on a random sample of unique (ij|kl)
-              x all m(m+1)/2 unique quartets (the reference screens nothing);
-      Fock  : formG on a random sample of G(i,j) entries x n^2 entries x niter;
-      MP2   : transform_int2 cost 8 n^5 flops at the measured rate of a
-              numpy (BLAS) dense quarter transform on one mu slice, + term1.
-    Returns (seconds per molecule, description)."""
-    from oracle import oracle as O
+# The reference's SCF mixes densities linearly from P = 0; the iteration count
+# used to scale its per-iteration stages is the GPU DIIS run's (14 on this
+# molecule), fewer than linear mixing needs, so the CPU time is a lower bound.
+REF_NITER = 14
 
-    rng = np.random.default_rng(seed)
+
+def cpu_sample(atno, xyz, niter, ws=None, seed=0, serial=True, eri_budget_s=2.0):
+    """hfsolver's per-molecule algorithm on this host's cores (oracle/refcost.py:
+    THO ERIs for every unique quartet, the dense TT built once, formG and dsygvd
+    per iteration, transform_int2's four loops, term1), timed on bounded
+    samples and scaled to one molecule, on all host threads and, if serial, on
+    one thread as the reference runs.  Returns a dict for the JSON line."""
+    from oracle import oracle as O
+    from oracle import refcost
+
     b = O.Basis(atno, xyz)
-    n = b.n
-    nq_total = O.n_ints(n)
-    # ERIs
-    q = O.random_unique_quartets(n, 2000, rng)
+    nocc = int(sum(atno)) // 2
+    if ws is None:
+        ws = refcost.Workspace(b.n, nocc, seed=seed)
+    rng = np.random.default_rng(seed)
+    threads = os.cpu_count() or 1
     t0 = time.perf_counter()
-    O.eri_list(b, q)
-    dt = time.perf_counter() - t0
-    nq = max(2000, int(2000 * budget_s * 0.6 / max(dt, 1e-6)))
-    q = O.random_unique_quartets(n, nq, rng)
-    t0 = time.perf_counter()
-    O.eri_list(b, q)
-    t_eri = (time.perf_counter() - t0) * nq_total / nq
-    # formG entries on a synthetic packed array of the right size
-    int2 = rng.standard_normal(nq_total) * 1e-3
-    P = rng.standard_normal((n, n))
-    P = P + P.T
-    ne = 4
-    ents = np.stack([rng.integers(0, n, ne), rng.integers(0, n, ne)], axis=1)
-    t0 = time.perf_counter()
-    O.formG_entries(P, int2, ents)
-    t_fock = (time.perf_counter() - t0) * n * n / ne * niter
-    del int2
-    # one quarter-transform slice: (nu la si) x C for one mu, scaled to 4 quarters of n^5
-    X = rng.standard_normal((n, n, n))
-    C = rng.standard_normal((n, n))
-    t0 = time.perf_counter()
-    np.einsum("abc,ck->abk", X, C, optimize=True)
-    t_slice = time.perf_counter() - t0
-    t_mp2 = t_slice * n * 4
-    total = t_eri + t_fock + t_mp2
-    desc = (f"extrapolated: {nq} random unique quartets of {nq_total} (THO, oracle/tho.c), "
-            f"{ne} formG entries of {n * n} x {niter} iterations, one mu slice of the 4 quarter "
-            f"transforms (numpy BLAS); per molecule ERI {t_eri:.1f} s, Fock {t_fock:.1f} s, "
-            f"transform {t_mp2:.1f} s")
-    return total, desc
+    st, smp = refcost.molecule_cost(b, nocc, niter, threads, ws, rng, eri_budget_s=eri_budget_s)
+    out = {"value": 1.0 / st["total"], "unit": "molecules/s", "cores": threads, "kind": "port",
+           "seconds_per_molecule": st["total"],
+           "stages_s": {k: round(v, 3) for k, v in st.items() if k != "total"},
+           "sample": ("extrapolated from bounded samples of each stage of the reference's algorithm "
+                      "(oracle/refpath.c, oracle/tho.c): " + "; ".join(f"{k}: {v}" for k, v in smp.items())
+                      + f"; SCF iterations {niter}"),
+           "measured_s": None}
+    if serial:
+        st1, smp1 = refcost.molecule_cost(b, nocc, niter, 1, ws, rng, eri_budget_s=eri_budget_s)
+        out["serial"] = {"value": 1.0 / st1["total"], "unit": "molecules/s", "cores": 1,
+                         "seconds_per_molecule": st1["total"],
+                         "stages_s": {k: round(v, 3) for k, v in st1.items() if k != "total"}}
+    out["measured_s"] = round(time.perf_counter() - t0, 2)
+    return out, ws
 
 
 def run_reference(args):
@@ -180,20 +171,26 @@ def run_reference(args):
     if rank != 0:
         return 0
     atno, xyz = workload(0)
-    niter = 14  # iterations of the DIIS SCF on this molecule (GPU run); the reference's linear mixing needs more
-    per = []
+    ws = None
+    per, per1, last = [], [], None
     for it in range(args.warmup + args.steps):
-        t, desc = cpu_sample(atno, xyz, niter, budget_s=6.0, seed=it)
-        if it >= args.warmup:
-            per.append(t)
+        timed = it >= args.warmup
+        cb, ws = cpu_sample(atno, xyz, REF_NITER, ws=ws, seed=it, serial=timed, eri_budget_s=1.0)
+        if timed:
+            per.append(cb["seconds_per_molecule"])
+            per1.append(cb["serial"]["seconds_per_molecule"])
+            last = cb
     v = 1.0 / float(np.mean(per))
-    cores = os.cpu_count()
+    cpu = dict(last)
+    cpu["value"] = v
+    cpu["seconds_per_molecule"] = float(np.mean(per))
+    cpu["serial"]["value"] = 1.0 / float(np.mean(per1))
+    cpu["serial"]["seconds_per_molecule"] = float(np.mean(per1))
     line = {"metric": METRIC, "value": v, "unit": "molecules/s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(per)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": WORKLOAD, "nbf": 200, "nocc": 40},
-            "cpu_baseline": {"value": v, "unit": "molecules/s", "cores": cores, "kind": "port",
-                             "sample": desc},
+            "cpu_baseline": cpu,
             "e2e": {"value": v, "unit": "molecules/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -305,9 +302,9 @@ def run_gpu(args):
     top = max(roof, key=lambda k: roof[k]["ms"])
     dominant = dict(roof[top])
     dominant["traffic"] = None
-    cpu_t, cpu_desc = (None, None)
+    cpu = None
     if world == 1 and not args.no_cpu_baseline:
-        cpu_t, cpu_desc = cpu_sample(atno, xyz, r["niter"], budget_s=8.0)
+        cpu, _ = cpu_sample(atno, xyz, r["niter"], serial=True)
     ro = res_o[-1]
     mixed = r if main_mp2 == "split_bf16" else ro
     plain = ro if main_mp2 == "split_bf16" else r
@@ -344,9 +341,8 @@ def run_gpu(args):
         "gpu_launches": int(launches),
         "clocks": clk,
     }
-    if cpu_t is not None:
-        line["cpu_baseline"] = {"value": 1.0 / cpu_t, "unit": "molecules/s", "cores": os.cpu_count(),
-                                "kind": "port", "sample": cpu_desc}
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
     print(json.dumps(line))
     return 0
 

@@ -1,6 +1,7 @@
 """Build recipe for the oracle (test infrastructure only).
 
-* ``liboracle.so``  — the C restatement (fm.c, tho.c), built everywhere.
+* ``liboracle.so``  — the C restatement (fm.c, tho.c) and the reference's
+  per-molecule loops for CPU-baseline timing (refpath.c), built everywhere.
 * ``_ref/libref.so`` — hfsolver's own src/cints.c and src/qc.c compiled
   unmodified from the reference checkout, linked with fm.c for the c_Fm
   callback that src/qc.f90:90-95 provides in the reference.  Built only where the
@@ -28,7 +29,7 @@ def _run(cmd):
 
 def build_oracle():
     out = os.path.join(HERE, "liboracle.so")
-    srcs = [os.path.join(HERE, "fm.c"), os.path.join(HERE, "tho.c")]
+    srcs = [os.path.join(HERE, "fm.c"), os.path.join(HERE, "tho.c"), os.path.join(HERE, "refpath.c")]
     _run(["gcc", *CFLAGS, "-fopenmp", *srcs, "-o", out, "-lm"])
     return out
 
