@@ -1,15 +1,10 @@
-// AO -> MO transform and the MBPT2 energy, plain FP64.
+// The MBPT2 energy and the packed-MO drop-ins, plain FP64.
 //
-// ao2mo_fp64 builds (i a | j b) from the packed AO integrals as four quarter
-// transforms, the same contraction as transform_int2 (src/mbpt.f90:11-79):
-//   X[m nu la si]  = (mu nu|la si)            unpacked, a block of mu at a time
-//   X1[m nu la j]  = sum_si X C1[si, j]       cuBLAS DGEMM
-//   X2[m nu j b]   = sum_la X1 C2[la, b]      batched DGEMM over (m, nu)
-//   X3[i nu j b]  += sum_m C1[mu, i] X2       DGEMM, accumulated over mu blocks
-//   out[i a j b]   = sum_nu C2[nu, a] X3      batched DGEMM over i
-// With C1 = C_occ and C2 = C_vir it gives the (ia|jb) block MBPT2 needs; with
-// C1 = C2 = C it gives every (ij|kl) for the full-transform drop-in.
-// mp2_energy then evaluates term1 (src/mbpt2.f90:8-31) from (ia|jb).
+// ao2mo_fp64 (dgemm_rows.cu) builds (i a | j b) from the packed AO integrals,
+// the contraction of transform_int2 (src/mbpt.f90:11-79): with C1 = C_occ and
+// C2 = C_vir the (ia|jb) block MBPT2 needs, with C1 = C2 = C every (ij|kl) for
+// the full-transform drop-in.  mp2_energy then evaluates term1
+// (src/mbpt2.f90:8-31) from (ia|jb).
 #include <algorithm>
 #include <vector>
 
@@ -23,47 +18,6 @@ __device__ __forceinline__ int64_t pidx(int64_t i, int64_t j, int64_t k, int64_t
     int64_t a = i > j ? i : j, b = i > j ? j : i, c = k > l ? k : l, d = k > l ? l : k;
     int64_t ij = a * (a + 1) / 2 + b, kl = c * (c + 1) / 2 + d;
     return ij >= kl ? ij * (ij + 1) / 2 + kl : kl * (kl + 1) / 2 + ij;
-}
-
-__global__ void unpack_kernel(int n, int mu0, int bm, const double* __restrict__ ints, double* X)
-{
-    const int64_t n3 = (int64_t)n * n * n, total = (int64_t)bm * n3;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        int64_t r = e;
-        const int si = (int)(r % n); r /= n;
-        const int la = (int)(r % n); r /= n;
-        const int nu = (int)(r % n); r /= n;
-        const int mu = mu0 + (int)r;
-        X[e] = ints[pidx(mu, nu, la, si)];
-    }
-}
-
-void ao2mo_fp64(Context& ctx, int n, const double* d_int2, const double* C1, int n1, const double* C2, int n2,
-                double* out)
-{
-    cudaStream_t st = ctx.stream;
-    const double one = 1.0, zero = 0.0;
-    const int64_t n3 = (int64_t)n * n * n;
-    int bm = (int)std::max<int64_t>(1, std::min<int64_t>(n, (int64_t)500000000 / n3));
-    DBuf<double> X((size_t)bm * n3, st), X1((size_t)bm * n * n * n1, st), X2((size_t)bm * n * n1 * n2, st);
-    const int64_t r3 = (int64_t)n * n1 * n2;
-    DBuf<double> X3((size_t)r3 * n1, st);
-    for (int mu0 = 0; mu0 < n; mu0 += bm) {
-        const int b = std::min(bm, n - mu0);
-        unpack_kernel<<<std::max(1, ctx.num_sms * 8), 256, 0, st>>>(n, mu0, b, d_int2, X.p);
-        count_launch();
-        HF_CUDA(cudaGetLastError());
-        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_T, CUBLAS_OP_N, n1, b * n * n, n, &one, C1, n, X.p, n, &zero,
-                              X1.p, n1));
-        HF_CUBLAS(cublasDgemmStridedBatched(ctx.blas, CUBLAS_OP_T, CUBLAS_OP_T, n2, n1, n, &one, C2, n, 0, X1.p,
-                                            n1, (int64_t)n1 * n, &zero, X2.p, n2, (int64_t)n1 * n2, b * n));
-        const double beta = mu0 == 0 ? 0.0 : 1.0;
-        HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)r3, n1, b, &one, X2.p, (int)r3, C1 + mu0, n,
-                              &beta, X3.p, (int)r3));
-    }
-    HF_CUBLAS(cublasDgemmStridedBatched(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n1 * n2, n2, n, &one, X3.p, n1 * n2,
-                                        r3, C2, n, 0, &zero, out, n1 * n2, (int64_t)n2 * n1 * n2, n1));
 }
 
 // one block per (i, j): sum_ab (ia|jb) [2 (ia|jb) - (ib|ja)] / (e_i + e_j - e_a - e_b)

@@ -38,6 +38,14 @@ __global__ void transpose_kernel(const double* __restrict__ in, int64_t rows, in
     }
 }
 
+void transpose_device(Context& ctx, const double* in, int64_t rows, int64_t cols, double* out)
+{
+    const dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+    transpose_kernel<<<grid, dim3(32, 8), 0, ctx.stream>>>(in, rows, cols, out);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+}
+
 void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, int n1, const double* C2, int n2,
                   double* T)
 {
@@ -104,13 +112,8 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
     // Z^T: one contiguous row of pairs per q, so that the (q, mu) rows of step 3
     // gather from one L2-resident row instead of one cache line per element
     DBuf<double> Zt((size_t)npair * nq, st);
-    {
-        const dim3 grid((unsigned)((nq + 31) / 32), (unsigned)((npair + 31) / 32));
-        transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(Z.p, npair, nq, Zt.p);
-        count_launch();
-        HF_CUDA(cudaGetLastError());
-        Z.release();
-    }
+    transpose_device(ctx, Z.p, npair, nq, Zt.p);
+    Z.release();
     ctx.trace_mark("mp2 transpose");
     // steps 3-4 over blocks of q
     const int64_t qb = std::max<int64_t>(1, SLICE_BUDGET_ROWS / std::max(n, n1));

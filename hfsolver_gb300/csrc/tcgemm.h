@@ -52,5 +52,7 @@ void dense_row_max(Context& ctx, const double* A, int64_t rows, int K, int64_t l
 void sliced_gemm_dense_gather(Context& ctx, const double* A, int64_t rows, int K, int64_t ld, const unsigned* rmax,
                               const Sliced& B, double* out, OutMap om);
 void sympair_row_max(Context& ctx, const double* Zt, int64_t ldz, int64_t nq, int n, unsigned* out);
+// out[c][r] = in[r][c] for a rows x cols row-major FP64 matrix (mp2_mixed.cu)
+void transpose_device(Context& ctx, const double* in, int64_t rows, int64_t cols, double* out);
 
 }  // namespace hfgpu
