@@ -67,6 +67,8 @@ SIGNATURES = {
     "hfgpu_transform_int2": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
     "hfgpu_mbpt2": (ctypes.c_int, [ctypes.c_int, _dp, _dp, ctypes.c_int, _dp]),
     "hfgpu_mbpt3": (ctypes.c_int, [ctypes.c_int, _dp, _dp, ctypes.c_int, _dp]),
+    "hfgpu_find_pole_diag": (ctypes.c_int, [ctypes.c_int, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_double, _dp, _ip]),
     "hfgpu_dgemm_sliced": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]),
     "hfgpu_default_options": (None, [ctypes.POINTER(Options)]),
     "hfgpu_basis_size": (ctypes.c_int, [ctypes.c_int, _ip]),

@@ -237,6 +237,18 @@ def mbpt3(moint2, lam, Noccupied):
     return float(E3[0])
 
 
+def find_pole_diag(i, moint2, lam, Noccupied, Nscf=200, tolE=1e-10):
+    """gf.f90 find_pole_diag: the Green's-function pole of orbital i (1-based,
+    as the Fortran function takes it); raises SCFNotConverged after Nscf
+    iterations, where the reference stops."""
+    moint2, lam = _f64(moint2), _f64(lam)
+    E = np.zeros(1)
+    it = np.zeros(1, dtype=np.int32)
+    _check(_lib.lib().hfgpu_find_pole_diag(len(lam), _d(moint2), _d(lam), int(Noccupied), int(i), int(Nscf),
+                                           float(tolE), _d(E), _i(it)))
+    return float(E[0])
+
+
 @dataclass
 class RHFOptions:
     nscf: int = 40

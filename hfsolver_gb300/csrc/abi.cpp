@@ -495,6 +495,26 @@ int hfgpu_mbpt3(int n, const double* moint2, const double* lam, int nocc, double
     });
 }
 
+int hfgpu_find_pole_diag(int n, const double* moint2, const double* lam, int nocc, int i, int nscf, double tolE,
+                         double* E, int* niter)
+{
+    return guard([&] {
+        HF_CHECK(n >= 2 && nocc >= 1 && nocc < n, HFGPU_ERR_INVALID, "find_pole_diag: need 1 <= nocc < n");
+        HF_CHECK(i >= 1 && i <= n, HFGPU_ERR_INVALID, "find_pole_diag: i is a 1-based orbital index in [1, n]");
+        HF_CHECK(nscf >= 1 && tolE > 0, HFGPU_ERR_INVALID, "find_pole_diag: need nscf >= 1 and tolE > 0");
+        check_ptr(moint2, "moint2"); check_ptr(lam, "lam"); check_ptr(E, "E");
+        Context& ctx = context();
+        std::lock_guard<std::recursive_mutex> call_lock(ctx.call_mutex);
+        const int64_t np = packed_size(n);
+        DBuf<double> dM(np, ctx.stream), dL(n, ctx.stream);
+        dM.upload(moint2, np);
+        dL.upload(lam, n);
+        int it = 0;
+        *E = find_pole_diag(ctx, n, dM.p, dL.p, nocc, i - 1, nscf, tolE, &it);
+        if (niter) *niter = it;
+    });
+}
+
 int hfgpu_dgemm_sliced(int64_t M, int N, int K, const double* A, const double* Bt, double* C)
 {
     return guard([&] {

@@ -35,11 +35,14 @@ namespace {
 constexpr int DG_BM = 128, DG_BK = 16, DG_TM = 4, DG_THREADS = 256;
 }
 
+// B element (k, c) at B[k sk + c sc]: column-major B has sk = 1, row-major sc = 1.
+// out = alpha A B + beta out (beta = 0: out is not read).
 template <class Src, int TN>
 __global__ void __launch_bounds__(DG_THREADS) dgemm_rows_kernel(const Src src, const int64_t M, const int K,
-                                                                const double* __restrict__ B, const int ldb,
-                                                                const int N, double* __restrict__ out,
-                                                                const OutMap om)
+                                                                const double* __restrict__ B, const int64_t sk,
+                                                                const int64_t sc, const int N,
+                                                                double* __restrict__ out, const OutMap om,
+                                                                const double alpha, const double beta)
 {
     constexpr int BN = 8 * TN;
     __shared__ double As[DG_BK][DG_BM];
@@ -72,9 +75,10 @@ __global__ void __launch_bounds__(DG_THREADS) dgemm_rows_kernel(const Src src, c
 #pragma unroll
         for (int e = 0; e < 8; ++e) As[lk0 + e][lr] = areg[e];
         for (int idx = tid; idx < DG_BK * BN; idx += DG_THREADS) {
-            const int kk = idx % DG_BK, c = idx / DG_BK;  // consecutive k of one column: coalesced
+            // consecutive threads along B's unit-stride direction: coalesced
+            const int kk = sk == 1 ? idx % DG_BK : idx / BN, c = sk == 1 ? idx / DG_BK : idx % BN;
             const int k = k0 + kk, col = n0 + c;
-            Bs[kk][c] = (k < K && col < N) ? __ldg(B + k + (int64_t)col * ldb) : 0.0;
+            Bs[kk][c] = (k < K && col < N) ? __ldg(B + k * sk + col * sc) : 0.0;
         }
         __syncthreads();
         if (k0 + DG_BK < K) fetch(k0 + DG_BK);
@@ -101,7 +105,10 @@ __global__ void __launch_bounds__(DG_THREADS) dgemm_rows_kernel(const Src src, c
 #pragma unroll
         for (int j = 0; j < TN; ++j) {
             const int col = n0 + ty * TN + j;
-            if (col < N) out[base + col * cs] = acc[i][j];
+            if (col < N) {
+                double* o = out + base + col * cs;
+                *o = beta == 0.0 ? alpha * acc[i][j] : fma(alpha, acc[i][j], beta * *o);
+            }
         }
     }
 }
@@ -123,30 +130,38 @@ static int pick_tn(int N)
 }
 
 template <class Src, int TN>
-static void dgemm_rows_tn(Context& ctx, const Src& src, int64_t M, int K, const double* B, int ldb, int N,
-                          double* out, OutMap om)
+static void dgemm_rows_tn(Context& ctx, const Src& src, int64_t M, int K, const double* B, int64_t sk, int64_t sc,
+                          int N, double* out, OutMap om, double alpha, double beta)
 {
     const int64_t bx = (M + DG_BM - 1) / DG_BM;
     const int by = (N + 8 * TN - 1) / (8 * TN);
     HF_CHECK(bx <= 0x7fffffff && by <= 65535, HFGPU_ERR_UNSUPPORTED, "FP64 transform GEMM: grid too large");
-    dgemm_rows_kernel<Src, TN><<<dim3((unsigned)bx, (unsigned)by), DG_THREADS, 0, ctx.stream>>>(src, M, K, B, ldb, N,
-                                                                                               out, om);
+    dgemm_rows_kernel<Src, TN><<<dim3((unsigned)bx, (unsigned)by), DG_THREADS, 0, ctx.stream>>>(
+        src, M, K, B, sk, sc, N, out, om, alpha, beta);
     count_launch();
     HF_CUDA(cudaGetLastError());
 }
 
-// out (M x N, placed by om) = rows of src (M x K) times B (K x N, column-major, ldb)
+// out (M x N, placed by om) = alpha rows of src (M x K) times B (K x N, element
+// (k, c) at B[k sk + c sc]) + beta out
 template <class Src>
-static void dgemm_rows(Context& ctx, const Src& src, int64_t M, int K, const double* B, int ldb, int N, double* out,
-                       OutMap om)
+static void dgemm_rows(Context& ctx, const Src& src, int64_t M, int K, const double* B, int64_t sk, int64_t sc,
+                       int N, double* out, OutMap om, double alpha = 1.0, double beta = 0.0)
 {
     if (M <= 0 || N <= 0) return;
     switch (pick_tn(N)) {
-        case 10: dgemm_rows_tn<Src, 10>(ctx, src, M, K, B, ldb, N, out, om); break;
-        case 8: dgemm_rows_tn<Src, 8>(ctx, src, M, K, B, ldb, N, out, om); break;
-        case 5: dgemm_rows_tn<Src, 5>(ctx, src, M, K, B, ldb, N, out, om); break;
-        default: dgemm_rows_tn<Src, 4>(ctx, src, M, K, B, ldb, N, out, om); break;
+        case 10: dgemm_rows_tn<Src, 10>(ctx, src, M, K, B, sk, sc, N, out, om, alpha, beta); break;
+        case 8: dgemm_rows_tn<Src, 8>(ctx, src, M, K, B, sk, sc, N, out, om, alpha, beta); break;
+        case 5: dgemm_rows_tn<Src, 5>(ctx, src, M, K, B, sk, sc, N, out, om, alpha, beta); break;
+        default: dgemm_rows_tn<Src, 4>(ctx, src, M, K, B, sk, sc, N, out, om, alpha, beta); break;
     }
+}
+
+void dgemm_rowmajor(Context& ctx, int64_t m, int n, int k, double alpha, const double* A, int64_t lda,
+                    const double* B, int64_t ldb, double beta, double* C, int64_t ldc)
+{
+    const DenseRowsG rows{A, lda, nullptr};
+    dgemm_rows(ctx, rows, m, k, B, ldb, 1, n, C, OutMap{0, ldc}, alpha, beta);
 }
 
 // rows per operand block (Y and W), as in the mixed transform
@@ -171,10 +186,10 @@ void ao2mo_fp64(Context& ctx, int n, const double* d_int2, const double* C1, int
     for (int64_t p0 = 0; p0 < npair; p0 += pb) {
         const int64_t np = std::min(pb, npair - p0);
         const PackedRowsBlocked rows1{d_int2, pairs.p, p0, np, n, nlg, nullptr};
-        dgemm_rows(ctx, rows1, (np + 7) / 8 * nlg * 128, n, C1, n, n1, Y.p, OutMap{n, n1});
+        dgemm_rows(ctx, rows1, (np + 7) / 8 * nlg * 128, n, C1, 1, n, n1, Y.p, OutMap{n, n1});
         ctx.trace_mark("fp64 step 1");
         const DenseRowsG rows2{Y.p, n, nullptr};
-        dgemm_rows(ctx, rows2, np * n1, n, C2, n, n2, Z.p + p0 * nq, OutMap{0, n2});
+        dgemm_rows(ctx, rows2, np * n1, n, C2, 1, n, n2, Z.p + p0 * nq, OutMap{0, n2});
         ctx.trace_mark("fp64 step 2");
     }
     Y.release();
@@ -186,10 +201,10 @@ void ao2mo_fp64(Context& ctx, int n, const double* d_int2, const double* C1, int
     for (int64_t q0 = 0; q0 < nq; q0 += qb) {
         const int64_t nqb = std::min(qb, nq - q0);
         SymPairRows rows3{Zt.p + q0 * npair, npair, n};
-        dgemm_rows(ctx, rows3, nqb * n, n, C1, n, n1, W.p, OutMap{n, n1});
+        dgemm_rows(ctx, rows3, nqb * n, n, C1, 1, n, n1, W.p, OutMap{n, n1});
         ctx.trace_mark("fp64 step 3");
         const DenseRowsG rows4{W.p, n, nullptr};
-        dgemm_rows(ctx, rows4, nqb * n1, n, C2, n, n2, T + q0 * n1 * n2, OutMap{0, n2});
+        dgemm_rows(ctx, rows4, nqb * n1, n, C2, 1, n, n2, T + q0 * n1 * n2, OutMap{0, n2});
         ctx.trace_mark("fp64 step 4");
     }
 }

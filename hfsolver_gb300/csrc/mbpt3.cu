@@ -16,7 +16,8 @@
 //       T1 = (2(ar|bs) - (br|as))/D_ab^rs, T2 = ((ar|bs) - 2(br|as))/D_ab^rs,
 //       M1[ar][ct] = (ar|ct), M2[ar][ct] = (ac|rt),
 //       P1[ct][bs] = (bs|ct)/D_bc^st, P2[ct][bs] = (bt|cs)/D_bc^st.
-// Matrices are row-major; cuBLAS sees them as their column-major transposes.
+// Matrices are row-major; the products run on the row-gathered FP64 GEMM of
+// dgemm_rows.cu.
 #include <algorithm>
 #include <vector>
 
@@ -98,8 +99,7 @@ __global__ void mp3_ring_kernel(int o, int v, const double* __restrict__ mo, con
 static void gemm_rm(Context& ctx, int m, int n, int k, double alpha, const double* A, int64_t lda, const double* B,
                     int64_t ldb, double beta, double* C, int64_t ldc)
 {
-    HF_CUBLAS(cublasDgemm(ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, k, &alpha, B, (int)ldb, A, (int)lda, &beta, C,
-                          (int)ldc));
+    dgemm_rowmajor(ctx, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 static void gemm_rm(Context& ctx, int m, int n, int k, double alpha, const double* A, const double* B, double beta,
                     double* C)

@@ -46,6 +46,10 @@ double device_dot(Context& ctx, int64_t nn, const double* A, const double* B);
 // packed AO integrals.  Output layout [i][a][j][b].
 void ao2mo_fp64(Context& ctx, int n, const double* d_int2, const double* dC1, int n1, const double* dC2, int n2,
                 double* d_out);
+// C[m][n] = alpha A[m][k] B[k][n] + beta C, row-major FP64 with leading
+// dimensions lda, ldb, ldc: the row-gathered FP64 GEMM of dgemm_rows.cu
+void dgemm_rowmajor(Context& ctx, int64_t m, int n, int k, double alpha, const double* A, int64_t lda,
+                    const double* B, int64_t ldb, double beta, double* C, int64_t ldc);
 // E2 from (ia|jb) in [i][a][j][b] layout and orbital energies (device)
 double mp2_energy(Context& ctx, int nocc, int nvir, const double* d_iajb, const double* d_eps);
 
@@ -56,6 +60,10 @@ namespace hfgpu {
 void transform_packed(Context& ctx, int n, const double* d_int2, const double* dC, double* d_mo);
 // MBPT2 energy with the tensor-core (exactly sliced bf16) transform (mp2_mixed.cu)
 double mp2_energy_mixed(Context& ctx, int n, const double* d_int2, const double* dC, int nocc, const double* d_eps);
+// Green's-function pole of orbital i (0-based) by find_pole_diag's fixed-point
+// iteration (gf.cu); HFGPU_ERR_NOT_CONVERGED after nscf iterations
+double find_pole_diag(Context& ctx, int n, const double* d_mo, const double* d_lam, int nocc, int i, int nscf,
+                      double tolE, int* niter);
 // term1 of src/mbpt2.f90 on packed MO integrals (mbpt2 drop-in)
 double mbpt2_packed(Context& ctx, int n, const double* d_mo, const double* d_lam, int nocc);
 // E3 of src/mbpt3.f90 on packed MO integrals (mbpt3 drop-in, mbpt3.cu)

@@ -173,8 +173,19 @@ int hfgpu_mbpt2(int n, const double *moint2, const double *lam, int nocc, double
 /* replaces mbpt3, src/mbpt.f90:161-169 (term1 + term2 + term3 of
  * src/mbpt3.f90:8-128): the third-order energy from the packed MO integrals,
  * all electrons correlated.  FP64; the terms run as dense GEMMs over compound
- * occupied-virtual indices instead of the reference's six nested loops. */
+ * occupied-virtual indices (the project's FP64 GEMM kernels) instead of the
+ * reference's six nested loops. */
 int hfgpu_mbpt3(int n, const double *moint2, const double *lam, int nocc, double *E3);
+
+/* replaces find_pole_diag, src/gf.f90:15-34: the Green's-function pole of
+ * orbital i (1-based, as the Fortran function takes it) by the fixed-point
+ * iteration E <- lam(i) + Sigma_ii(E) from E = lam(i), with the second-order
+ * self-energy of src/gf.f90:124-148 over nocc occupied orbitals, until
+ * |E - E_old| < tolE; E gets the pole, niter (may be NULL) the iterations.
+ * HFGPU_ERR_NOT_CONVERGED after nscf iterations (the reference stops there).
+ * FP64, from the packed MO integrals. */
+int hfgpu_find_pole_diag(int n, const double *moint2, const double *lam, int nocc, int i, int nscf, double tolE,
+                         double *E, int *niter);
 
 /* FP64-accurate C = A B on the tcgen05 tensor cores (the kernel behind the
  * mixed-precision transform): A row-major M x K, Bt = B^T row-major N x K

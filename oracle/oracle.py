@@ -11,6 +11,8 @@ calls it.  It is a CPU restatement of hfsolver's molecular GTO path:
 * nuclear repulsion, rhf_gauss           src/scf.f90:138-150, src/drivers.f90:12-51
 * AO->MO transform                       src/mbpt.f90:11-79
 * MBPT2 energy                           src/mbpt2.f90:8-31, src/mbpt.f90:154-159
+* MBPT3 energy                           src/mbpt3.f90:8-128
+* Green's-function pole (diagonal)       src/gf.f90:15-34, 124-148
 
 Parity is pinned against the reference's own known answers
 (src/tests/test_gaussians_molecules.f90, test_gaussians_atoms.f90, test_fm.f90,
@@ -468,6 +470,36 @@ def mbpt3(moint2, lam, nocc):
     t3 = (2 * np.einsum("abrs,rstu,abtu->", arbs / D, rt_su, ta_ub / D, optimize=True)
           - 1 * np.einsum("abrs,rstu,abtu->", arbs / D, rt_su, ua_tb / D, optimize=True))
     return float(t1 + t2 + t3)
+
+
+def self_energy(i, j, E, moint2, lam, nocc):
+    """Second-order self-energy Sigma_ij(E), gf.f90:124-148 (0-based i, j)."""
+    n = len(lam)
+    a = np.arange(nocc)
+    r = np.arange(nocc, n)
+    A, R, S = np.meshgrid(a, r, r, indexing="ij")
+    iras = moint2[ijkl(i, R, A, S)]
+    jras = moint2[ijkl(j, R, A, S)]
+    jsar = moint2[ijkl(j, S, A, R)]
+    E1 = np.sum(iras * (2 * jras - jsar) / (E + lam[A] - lam[R] - lam[S]))
+    A, B, R = np.meshgrid(a, a, r, indexing="ij")
+    iabr = moint2[ijkl(i, A, B, R)]
+    jabr = moint2[ijkl(j, A, B, R)]
+    jbar = moint2[ijkl(j, B, A, R)]
+    E2 = np.sum(iabr * (2 * jabr - jbar) / (E + lam[R] - lam[A] - lam[B]))
+    return float(E1 + E2)
+
+
+def find_pole_diag(i, moint2, lam, nocc, nscf, tolE):
+    """gf.f90:15-34: E <- lam(i) + Sigma_ii(E) from E = lam(i) until |dE| < tolE
+    (i is 1-based, as in the reference)."""
+    E = lam[i - 1]
+    for _ in range(nscf):
+        Eold = E
+        E = lam[i - 1] + self_energy(i - 1, i - 1, E, moint2, lam, nocc)
+        if abs(E - Eold) < tolE:
+            return float(E)
+    raise SCFNotConverged(f"Green's function SCF did not converge in {nscf} iterations.")
 
 
 def mp2_semidirect(int2, C, lam, nocc, block=None):

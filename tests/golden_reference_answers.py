@@ -2,7 +2,8 @@
 
 Each entry: atomic numbers, geometry (bohr), SCF mixing alpha, the occupied count
 the test passes to mbpt2, and the asserted values with their tolerances, each
-with its source line in src/tests/.  Nscf = 40, tolE = 1e-10, tolP = 1e-8
+with its source line in src/tests/.  gf = (1-based orbital, pole, tolerance,
+line) of find_pole_diag with Nelec/2 occupied, Nscf = 200, tolE = 1e-10.  Nscf = 40, tolE = 1e-10, tolP = 1e-8
 throughout (test_gaussians_molecules.f90:20-23, test_gaussians_atoms.f90:20-23).
 """
 ANG2BOHR = 1 / 0.529177249
@@ -12,7 +13,8 @@ CASES = {
     # test_gaussians_molecules.f90
     "H2": dict(atno=[1, 1], xyz=[[0, 0, 0], [0, 0, 1.4]], alpha=1.0, nocc_mp2=1,
                etot=(-1.13128434, 1e-7, ":42"), e2=(-0.0263, 6e-5, ":48"),
-               e3=(-0.00551598, 1e-8, ":52"), lam=[(0, -0.595, 6e-4, ":44")]),
+               e3=(-0.00551598, 1e-8, ":52"), lam=[(0, -0.595, 6e-4, ":44")],
+               gf=(1, -0.59832340, 1e-8, ":55")),
     "N2": dict(atno=[7, 7], xyz=[[0, 0, 0], [0, 0, 2.074]], alpha=1.0, nocc_mp2=None,
                etot=(-108.94268654, 1e-8, ":66"),
                lam=[(4, -0.630, 6e-4, ":68"), (5, -0.612, 6e-4, ":69"), (6, -0.612, 6e-4, ":70")]),
@@ -24,7 +26,8 @@ CASES = {
                        [-0.683292, -0.966387, -1.673831], [-0.683292, -0.966387, 1.673831]],
                   alpha=1.0, nocc_mp2=5, etot=(-40.20170036, 1e-8, ":106"),
                   e2=(-0.16815509, 1e-7, ":114"), e3=(-0.01819243, 1e-7, ":116"),
-                  lam=[(4, -0.545, 6e-4, ":109"), (4, -0.54451008, 1e-8, ":110")]),
+                  lam=[(4, -0.545, 6e-4, ":109"), (4, -0.54451008, 1e-8, ":110")],
+                  gf=(5, -0.51384473, 1e-8, ":119")),
     "CH4_2": dict(atno=[6, 1, 1, 1, 1],
                   xyz=[[0, 0, 0], [_a, -_a, _a], [-_a, _a, _a], [_a, _a, -_a], [-_a, -_a, -_a]],
                   alpha=1.0, nocc_mp2=5, etot=(-40.20170480, 1e-8, ":137"),
@@ -33,14 +36,15 @@ CASES = {
                 xyz=[[0, 0, 0], [1.913, 0, 0], [-0.548761, 1.832602, 0],
                      [-0.548761, -0.916301, -1.587080]],
                 alpha=1.0, nocc_mp2=None, etot=(-56.19457246, 1e-8, ":156"),
-                lam=[(4, -0.41491598, 1e-8, ":158")]),
+                lam=[(4, -0.41491598, 1e-8, ":158")], gf=(5, -0.35357570, 1e-8, ":161")),
     "H2O": dict(atno=[8, 1, 1], xyz=[[0, 0, 0], [1.809, 0, 0], [-0.453549, 1.751221, 0]],
                 alpha=1.0, nocc_mp2=5, etot=(-76.02315869, 1e-8, ":183"),
                 e2=(-0.19925995, 1e-6, ":189"), e3=(-0.00611895, 1e-6, ":191"),
-                lam=[(4, -0.497, 6e-4, ":186")]),
+                lam=[(4, -0.497, 6e-4, ":186")], gf=(5, -0.40499448, 1e-8, ":194")),
     "FH": dict(atno=[9, 1], xyz=[[0, 0, 0], [1.733, 0, 0]], alpha=1.0, nocc_mp2=None,
                etot=(-100.01134814, 1e-8, ":209"),
-               lam=[(3, -0.627, 6e-4, ":211"), (4, -0.627, 6e-4, ":212")]),
+               lam=[(3, -0.627, 6e-4, ":211"), (4, -0.627, 6e-4, ":212")],
+               gf=(5, -0.51894290, 2e-8, ":215")),
     # test_gaussians_atoms.f90
     "He": dict(atno=[2], xyz=[[0, 0, 0]], alpha=1.0, nocc_mp2=1,
                etot=(-2.8551604262, 1e-10, ":41"), e2=(-0.02547703, 1e-6, ":46"), lam=[]),

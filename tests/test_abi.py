@@ -120,3 +120,14 @@ def test_boys_rejects_bad_arguments_before_the_gpu(L):
     assert b"T must be" in L.hfgpu_last_error()
     T[1] = float("nan")
     assert L.hfgpu_boys(4, 2, T, F) == _lib.ERR_INVALID
+
+
+def test_find_pole_diag_rejects_bad_arguments_before_the_gpu(L):
+    from hfsolver_gb300 import _lib
+
+    buf = (ctypes.c_double * 64)()
+    it = ctypes.c_int(0)
+    assert L.hfgpu_find_pole_diag(4, buf, buf, 2, 0, 10, 1e-10, buf, ctypes.byref(it)) == _lib.ERR_INVALID
+    assert L.hfgpu_find_pole_diag(4, buf, buf, 2, 5, 10, 1e-10, buf, ctypes.byref(it)) == _lib.ERR_INVALID
+    assert L.hfgpu_find_pole_diag(4, buf, buf, 4, 1, 10, 1e-10, buf, ctypes.byref(it)) == _lib.ERR_INVALID
+    assert L.hfgpu_find_pole_diag(4, buf, buf, 2, 1, 0, 1e-10, buf, ctypes.byref(it)) == _lib.ERR_INVALID

@@ -199,3 +199,27 @@ def test_mbpt3_reference_known_answers(oracle, name):
     val, tol, _ = c["e3"]
     assert abs(e3 - val) < tol
     assert abs(e3 - oracle.mbpt3(mo, ref["lam"], c["nocc_mp2"])) < 1e-12
+
+
+@pytest.mark.parametrize("name", [k for k in CASES if "gf" in CASES[k]])
+def test_find_pole_diag_reference_known_answers(oracle, name):
+    """find_pole_diag drop-in (src/gf.f90:15-34) on the reference's own H2, CH4,
+    NH3, H2O and FH cases: the asserted poles (test_gaussians_molecules.f90:55,
+    :119, :161, :194, :215) from the GPU's own transform_int2, and the oracle's
+    pole from the same MO integrals."""
+    c = CASES[name]
+    ref = oracle.rhf_gauss(c["atno"], np.array(c["xyz"], float), nscf=40, alpha=c["alpha"], tolE=1e-10, tolP=1e-8)
+    mo = hf.transform_int2(ref["int2"], ref["C"])
+    nocc = int(sum(c["atno"])) // 2
+    i, val, tol, _ = c["gf"]
+    Eg = hf.find_pole_diag(i, mo, ref["lam"], nocc, 200, 1e-10)
+    assert abs(Eg - val) < tol, (Eg, val)
+    assert abs(Eg - oracle.find_pole_diag(i, mo, ref["lam"], nocc, 200, 1e-10)) < 1e-11
+
+
+def test_find_pole_diag_reports_nonconvergence(oracle):
+    c = CASES["H2O"]
+    ref = oracle.rhf_gauss(c["atno"], np.array(c["xyz"], float))
+    mo = hf.transform_int2(ref["int2"], ref["C"])
+    with pytest.raises(hf.SCFNotConverged):
+        hf.find_pole_diag(5, mo, ref["lam"], 5, 1, 1e-10)

@@ -32,6 +32,11 @@ def test_reference_known_answers(oracle, name):
             assert abs(E3 - val) < tol
             if c["atno"] == [1, 1]:
                 assert abs(E2 + E3 - (-0.0319)) < 6e-5  # test_gaussians_molecules.f90:49
+    if "gf" in c:
+        mo = oracle.transform_int2(r["int2"], r["C"])
+        i, val, tol, _ = c["gf"]
+        Eg = oracle.find_pole_diag(i, mo, r["lam"], int(sum(c["atno"])) // 2, 200, 1e-10)
+        assert abs(Eg - val) < tol, (name, Eg, val)
 
 
 def test_scf_nonconvergence_is_reported(oracle):
