@@ -124,6 +124,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         ctx.settle_timers();  // drop timers a failed earlier call may have left
         ctx.trace_begin();
         ctx.stat_fock_ms = ctx.stat_tc_ms = ctx.stat_tc_flops = 0;
+        ctx.stat_tc_step1_ms = ctx.stat_tc_step1_n = 0;
         ctx.stat_fock_full_ms = ctx.stat_fock_full_n = 0;
         ctx.tune = opt.autotune != 0 || tune_env_enabled();
         Timer total(st);
@@ -236,6 +237,8 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         res->block_elems = (double)es.n_block_elems;
         res->ms_tcgemm = ctx.stat_tc_ms;
         res->tc_flops = ctx.stat_tc_flops;
+        res->ms_tc_step1 = ctx.stat_tc_step1_ms;
+        res->n_tc_step1 = ctx.stat_tc_step1_n;
 }
 
 extern "C" {

@@ -134,6 +134,8 @@ struct Context {
     double stat_fock_full_ms = 0, stat_fock_full_n = 0;
     // kernel-time counters, reset by the pipeline entry points
     double stat_fock_ms = 0, stat_tc_ms = 0, stat_tc_flops = 0;
+    // the gather-fed GEMM over the packed integrals (transform step 1) alone
+    double stat_tc_step1_ms = 0, stat_tc_step1_n = 0;
     bool tune = false;  // time candidate kernel shapes on first use (autotune.cpp)
     // phase trace (HFGPU_TRACE=1 in the environment): an event on `stream` and a
     // host clock reading at each named point of a pipeline call; trace_report()

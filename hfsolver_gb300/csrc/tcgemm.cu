@@ -30,9 +30,11 @@
 
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 
 #include "internal.h"
 #include "gather_rows.cuh"
+#include "slice_bits.cuh"
 #include "tcgemm.h"
 
 namespace hfgpu {
@@ -148,6 +150,28 @@ __device__ __forceinline__ double pow2(int e)
     if (e < -1022) return 0.0;
     if (e > 1023) e = 1023;
     return __longlong_as_double((int64_t)(e + 1023) << 52);
+}
+
+static_assert(NSL == SLICE_NSL && SL_BITS == SLICE_BITS, "slice layout shared with slice_bits.cuh");
+
+// RN((double) S) 2^E, from integer fields where the result is a normal double
+// (slice_bits.cuh), else on the FP64 unit; identical results either way
+__device__ __forceinline__ double scaled_sum_to_double(long long S, int E)
+{
+    if (E >= -1022 && E <= 1023) {
+        bool ok;
+        const uint64_t b = scaled_int_to_double_bits(S, E, ok);
+        if (ok) return __longlong_as_double((long long)b);
+    }
+    return (double)S * pow2(E);
+}
+
+// two bf16 lanes minus 128 (exact): 0x4300 | d -> d (slice_bits.cuh)
+__device__ __forceinline__ uint32_t bf16x2_minus_128(uint32_t w)
+{
+    uint32_t r;
+    asm("sub.rn.bf16x2 %0, %1, %2;" : "=r"(r) : "r"(w), "r"(0x43004300u));
+    return r;
 }
 
 // ------------------------------------------------------------------ GEMM kernel
@@ -286,7 +310,7 @@ __global__ void __launch_bounds__(128, 1)
                     for (int i = 0; i < 16; ++i) {
                         const int c = n0 + c0 + i;
                         if (c < N) {
-                            const double x = (double)S[i] * pow2(er + eb[c] - SL_BITS * (NSL + 1));
+                            const double x = scaled_sum_to_double(S[i], er + eb[c] - SL_BITS * (NSL + 1));
                             const int64_t o = out_index(om, r, c);
                             out[o] = accumulate ? out[o] + x : x;
                         }
@@ -511,14 +535,16 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
                 for (int t = 0; t < NSL; ++t) tma_load_2d(sB(s, t), &tmB, ks * BK, t * b_rows_pad + n0, &full[s]);
                 pend_b = g;
             }
+            // two elements per 32-bit word and plane: digit patterns 0x4300 | d, one
+            // packed bf16 subtraction of 128, then the signs (slice_bits.cuh)
             uint32_t w[NSL][PK / 2];
 #pragma unroll
             for (int j = 0; j < PK; j += 2) {
-                uint16_t d0[NSL], d1[NSL];
-                digits_bf16(x[j], e, d0);
-                digits_bf16(x[j + 1], e, d1);
+                const uint64_t b0 = (uint64_t)__double_as_longlong(x[j]), b1 = (uint64_t)__double_as_longlong(x[j + 1]);
+                const uint64_t Y0 = scaled_magnitude(b0, e), Y1 = scaled_magnitude(b1, e);
+                const uint32_t sw = sign_word(b0, b1);
 #pragma unroll
-                for (int t = 0; t < NSL; ++t) w[t][j / 2] = (uint32_t)d0[t] | ((uint32_t)d1[t] << 16);
+                for (int t = 0; t < NSL; ++t) w[t][j / 2] = bf16x2_minus_128(digit_word(Y0, Y1, t)) ^ sw;
             }
             // the next step's elements are in flight while this one is stored and multiplied
             if (ks + 1 < ksteps) {
@@ -584,7 +610,7 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
 #pragma unroll
                     for (int i = 0; i < 16; ++i) {
                         const int c = n0 + c0 + i;
-                        if (c < N) out[out_index(om, ro, c)] = (double)S[i] * pow2(er + eb[c] - SL_BITS * (NSL + 1));
+                        if (c < N) out[out_index(om, ro, c)] = scaled_sum_to_double(S[i], er + eb[c] - SL_BITS * (NSL + 1));
                     }
                 }
             }
@@ -765,6 +791,10 @@ static void gather_gemm_cfg(Context& ctx, const Src& src, int64_t M, int64_t M_r
     cudaEventDestroy(e1);
     ctx.stat_tc_ms += ms;
     ctx.stat_tc_flops += 2.0 * (NSL * (NSL + 1) / 2) * (double)M_rows * (double)B.rows * (double)K;
+    if constexpr (std::is_same_v<Src, PackedRowsBlocked>) {
+        ctx.stat_tc_step1_ms += ms;
+        ctx.stat_tc_step1_n += 1;
+    }
     HF_CHECK(h == 0, HFGPU_ERR_CUDA, "gather GEMM: an mbarrier wait timed out");
 }
 

@@ -255,6 +255,8 @@ typedef struct {
     double ms_fock_full;     /* the part of ms_fock spent in full (not incremental) Fock builds */
     double n_fock_full;      /* number of those full builds */
     double block_elems;      /* component quartets a full Fock build digests (12 flops each) */
+    double ms_tc_step1;      /* the tensor-core GEMMs over the packed integrals (transform step 1) */
+    double n_tc_step1;       /* their launches */
 } hfgpu_result;
 
 void hfgpu_default_options(hfgpu_options *opt);
