@@ -200,7 +200,11 @@ def run_reference(args):
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the roofline
 # kernel for one molecule, from the ncu capture summarised under profiles/
 # (keyed by roofline entry and basis size).
-KERNEL_TRAFFIC = {}
+KERNEL_TRAFFIC = {
+    ("step1", 200): {"bytes_per_molecule": 4.3775e9, "bytes_per_launch": 1.0944e9,
+                     "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the 4 step-1 launches of one "
+                               "8-water molecule (profiles/gather_gemm_traffic_water8.md)"},
+}
 
 def measured_peaks():
     """Peaks measured on this GPU pool (generated file), else the stated fallback."""
@@ -330,6 +334,8 @@ def run_gpu(args):
     tr = KERNEL_TRAFFIC.get((top, n))
     dominant["traffic"] = tr["bytes_per_molecule"] if tr else None
     if tr:
+        dominant["traffic_unit"] = "bytes per molecule (all launches of the kernel, as achieved)"
+        dominant["traffic_per_launch"] = tr["bytes_per_launch"]
         dominant["traffic_source"] = tr["source"]
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
@@ -378,9 +384,12 @@ def run_gpu(args):
 
 def run_batch(args):
     """Batched molecules/s: args.batch seeded water clusters of 1-12 waters with
-    Gaussian atom jitter (0.05 A), all through hfgpu_rhf_batch (mixed MBPT2,
-    several molecules in flight on their own streams), against the same
-    molecules one at a time through the plain FP64 path (every 8th molecule)."""
+    Gaussian atom jitter (0.05 A) through hfgpu_rhf_batch with mixed MBPT2, in
+    waves whose molecules share one ERI launch and, every SCF iteration, one
+    Fock-build launch per quartet class (a replayed CUDA graph).  Beside it, on a
+    fixed subset (every 8th molecule): the same molecules one at a time through
+    the mixed path and through the plain FP64 path, and for the molecules the
+    oracle fixtures hold, |dE| against the oracle."""
     import torch
 
     import hfsolver_gb300 as hf
@@ -395,6 +404,7 @@ def run_batch(args):
     mols = water_batch(args.batch, seed=rank)
     opt = options("split_bf16")
     opt.batch_streams = args.streams
+    opt.batch_fused = not args.batch_streams_mode
     opt.autotune = True  # quartet-tile shapes timed on the first molecules of each size, then reused
     for w in range(args.warmup):
         hf.rhf_batch(mols[w * 4:(w + 1) * 4], opt)
@@ -410,34 +420,60 @@ def run_batch(args):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
-    # the same molecules one at a time, plain FP64 MBPT2, on a fixed subset
+    # the same molecules one at a time on a fixed subset: mixed, then plain FP64
     sub = list(range(0, len(mols), 8))
+    single = options("split_bf16")
     plain = options("fp64")
+    hf.rhf(mols[sub[0]][0], mols[sub[0]][1], single)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    ref = [hf.rhf(mols[i][0], mols[i][1], plain) for i in sub]
+    one_mixed = [hf.rhf(mols[i][0], mols[i][1], single) for i in sub]
     torch.cuda.synchronize()
-    wall_plain = time.perf_counter() - t1
+    wall_mixed = time.perf_counter() - t1
+    t2 = time.perf_counter()
+    one_plain = [hf.rhf(mols[i][0], mols[i][1], plain) for i in sub]
+    torch.cuda.synchronize()
+    wall_plain = time.perf_counter() - t2
     if world > 1:
-        wall, wall_plain = max_over_ranks([wall, wall_plain])
+        wall, wall_mixed, wall_plain = max_over_ranks([wall, wall_mixed, wall_plain])
     if rank != 0:
         return 0
     failed = sum(1 for r in res if r["niter"] <= 0)
-    dE2 = max(abs(res[i]["E2"] - r["E2"]) for i, r in zip(sub, ref))
-    dEt = max(abs(res[i]["Etot"] - r["Etot"]) for i, r in zip(sub, ref))
+    dE2 = max(abs(res[i]["E2"] - r["E2"]) for i, r in zip(sub, one_plain))
+    dEt = max(abs(res[i]["Etot"] - r["Etot"]) for i, r in zip(sub, one_plain))
+    # against the oracle fixtures of the batch workload (rank 0's molecules)
+    oracle = {}
+    try:
+        fx = json.load(open(os.path.join(ROOT, "tests", "golden", "water_clusters.json"))).get("batch")
+    except (OSError, ValueError):
+        fx = None
+    if fx and fx["count"] == len(mols) and fx["seed"] == rank:
+        d_hf = [abs(res[m["index"]]["Etot"] - m["Etot"]) for m in fx["molecules"]]
+        d_e2 = [abs(res[m["index"]]["E2"] - m["E2"]) for m in fx["molecules"]]
+        oracle = {"molecules": [m["index"] for m in fx["molecules"]], "max_dEtot": max(d_hf), "max_dE2": max(d_e2)}
     nbf = [r["nbf"] for r in res]
+    value = world * args.steps * len(mols) / wall
     line = {
-        "metric": METRIC + " (batched)", "value": world * args.steps * len(mols) / wall, "unit": "molecules/s",
+        "metric": METRIC + " (batched)", "value": value, "unit": "molecules/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"water_batch{len(mols)}_1to12_jitter0.05A_631gss_rhf_diis_schwarz1e-12_mp2",
                    "molecules": len(mols), "nbf_min": min(nbf), "nbf_max": max(nbf), "nbf_mean": float(np.mean(nbf)),
-                   "mp2": "split_bf16", "batch_streams": args.streams,
+                   "mp2": "split_bf16",
+                   "batch": ("molecules of a wave share one ERI launch and one Fock-build launch per quartet class "
+                             "per SCF iteration (replayed CUDA graph)" if opt.batch_fused else
+                             "each molecule on its own streams"),
+                   "molecules_per_wave" if opt.batch_fused else "molecules_in_flight": args.streams,
                    "autotuned_shapes": len(hf.autotune_table()),
-                   "timing": "host wall clock between device-wide synchronizes (molecules run on several streams)",
+                   "timing": "host wall clock between device-wide synchronizes",
                    "parallelism": f"replicas x{world}"},
-        "plain_fp64_one_at_a_time": {"molecules_per_s": len(sub) / wall_plain, "sample": f"every 8th molecule ({len(sub)})",
-                                     "max_dE2": dE2, "max_dEtot": dEt},
+        "batch": {"mixed_batched_molecules_per_s": value,
+                  "mixed_one_at_a_time_molecules_per_s": len(sub) / wall_mixed,
+                  "plain_fp64_one_at_a_time_molecules_per_s": len(sub) / wall_plain,
+                  "one_at_a_time_sample": f"every 8th molecule ({len(sub)})",
+                  "one_at_a_time_mean_nbf": float(np.mean([nbf[i] for i in sub])),
+                  "vs_gpu_fp64": {"max_dE2": dE2, "max_dEtot": dEt},
+                  "vs_oracle_fixtures": oracle or None},
         "failed": failed,
         "clocks": clk,
     }
@@ -492,7 +528,10 @@ def main():
                     help="skip the CPU-baseline sample (profiling runs)")
     ap.add_argument("--batch", type=int, default=0,
                     help="batched mode: this many water clusters of 1-12 waters per step")
-    ap.add_argument("--streams", type=int, default=8, help="batched mode: molecules in flight at once")
+    ap.add_argument("--streams", type=int, default=32,
+                    help="batched mode: molecules per wave (or in flight at once with --batch-streams-mode)")
+    ap.add_argument("--batch-streams-mode", action="store_true",
+                    help="batched mode: each molecule on its own streams instead of shared launches")
     ap.add_argument("--grad", action="store_true", help="time the analytic gradient (2-12 waters)")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -24,7 +24,7 @@ class Options(ctypes.Structure):
                 ("schwarz", ctypes.c_double), ("mp2", ctypes.c_int), ("mp2_nocc", ctypes.c_int),
                 ("purify", ctypes.c_int), ("batch_streams", ctypes.c_int), ("incremental", ctypes.c_int),
                 ("autotune", ctypes.c_int), ("guess", ctypes.c_int), ("eigensolver", ctypes.c_int),
-                ("reserved", ctypes.c_int * 2)]
+                ("batch_mode", ctypes.c_int), ("reserved", ctypes.c_int * 1)]
 
 
 class Result(ctypes.Structure):

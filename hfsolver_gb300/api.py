@@ -261,7 +261,8 @@ class RHFOptions:
     mp2: str = "fp64"          # "none" | "fp64" | "split_bf16"
     mp2_nocc: int = 0          # <= 0: sum(Z)/2
     purify: bool = False       # SP2 density purification instead of an eigensolve per iteration
-    batch_streams: int = 0     # rhf_batch: molecules in flight at once (<= 0: 8)
+    batch_streams: int = 0     # rhf_batch: molecules per wave (<= 0: 32), or in flight at once with batch_fused=False (<= 0: 8)
+    batch_fused: bool = True   # rhf_batch: waves sharing one ERI and one Fock-build launch per quartet class
     incremental: bool = False  # Fock builds from screened density differences
     autotune: bool = False     # time candidate kernel shapes on first use, keep the fastest
     guess: str = "core"        # starting density: "core" (P = 0, the reference) | "sad" (atomic densities)
@@ -282,6 +283,7 @@ class RHFOptions:
         o.autotune = 1 if self.autotune else 0
         o.guess = {"core": 0, "sad": 1}[self.guess]
         o.eigensolver = {"own": 0, "cusolver": 1}[self.eigensolver]
+        o.batch_mode = 0 if self.batch_fused else 1
         return o
 
 
@@ -347,7 +349,8 @@ def autotune_clear():
 
 def rhf_batch(molecules, options=None):
     """hfgpu_rhf over a list of (atno, xyz) molecules in one call; returns a list
-    of result dicts (a failed molecule has niter = -status)."""
+    of result dicts.  A molecule that failed has niter = -status and does not
+    stop the others; errors of the call itself (no device, bad arguments) raise."""
     opt = (options or RHFOptions()).to_c()
     natoms = _i32([len(a) for a, _ in molecules])
     atno = _i32(np.concatenate([np.asarray(a) for a, _ in molecules]))
@@ -355,7 +358,7 @@ def rhf_batch(molecules, options=None):
     res = (_lib.Result * len(molecules))()
     code = _lib.lib().hfgpu_rhf_batch(len(molecules), _i(natoms), _i(atno), _d(xyz), opt, res)
     out = [{k: getattr(r, k) for k, _ in _lib.Result._fields_ if k != "reserved"} for r in res]
-    if code not in (_lib.OK, _lib.ERR_NOT_CONVERGED):
+    if code != _lib.OK and not any(r["niter"] < 0 for r in out):
         _check(code)
     return out
 

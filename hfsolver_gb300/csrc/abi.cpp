@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "autotune.h"
+#include "batch.h"
 #include "eigh.h"
 #include "internal.h"
 #include "scf.h"
@@ -105,10 +106,22 @@ void ints_dropin(const Basis& b, double* Ints, double schwarz, EriStats* st)
 
 }  // namespace
 
+// a molecule's place in a wave of hfgpu_rhf_batch's fused mode (batch.h)
+struct BatchMember {
+    BatchWave* wave;
+    int mol;
+};
+
 static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu_options* opt_in, hfgpu_result* res,
                      double* C, double* lam, int& conv, int& nscf, double* grad = nullptr,
-                     Context* ctx_in = nullptr)
+                     Context* ctx_in = nullptr, BatchMember* bm = nullptr)
 {
+        // a wave's member leaves it however this call ends (its builds go on without it)
+        struct WaveExit {
+            BatchMember* b;
+            void now() { if (b) b->wave->leave(b->mol); b = nullptr; }
+            ~WaveExit() { now(); }
+        } wave_exit{bm};
         check_ptr(atno, "atno"); check_ptr(xyz, "xyz"); check_ptr(res, "res");
         hfgpu_options opt;
         if (opt_in) opt = *opt_in; else hfgpu_default_options(&opt);
@@ -143,9 +156,13 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         // host work (pair lists, quartet classes); joined before H is formed
         ctx.fork();
         onee_compute(ctx, b, natoms, atno, x.data(), y.data(), z.data(), dS.p, dT.p, dV.p, ctx.aux[0]);
-        // integrals, resident in HBM for the whole SCF
-        DBuf<double> dI(packed_size(n), st);
-        dI.zero();
+        // integrals, resident in HBM for the whole SCF (in a wave: the wave's arrays)
+        DBuf<double> dI;
+        if (!bm) {
+            dI.alloc(packed_size(n), st);
+            dI.zero();
+        }
+        const double* d_int2 = dI.p;
         EriStats es;
         std::unique_ptr<EriPlan, void (*)(EriPlan*)> plan(eri_plan_create(ctx, b, opt.schwarz), eri_plan_destroy);
         ctx.join();
@@ -156,7 +173,14 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         res->ms_setup = total.ms();
         ctx.trace_mark("one-electron + plan");
         // the packed array feeds MBPT2; the screened quartet blocks feed every Fock build
-        eri_compute(ctx, plan.get(), dI.p, true, &es);
+        if (bm) {
+            d_int2 = bm->wave->eri_rendezvous(bm->mol, ctx, plan.get(), &es.ms);
+            const double ms = es.ms;
+            es = eri_plan_stats(plan.get());
+            es.ms = ms;
+        } else {
+            eri_compute(ctx, plan.get(), dI.p, true, &es);
+        }
         res->ms_eri = es.ms;
         res->n_quartets = es.n_quartets;
         res->n_bf_quartets = es.n_bf_quartets;
@@ -167,7 +191,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         Timer ts(st);
         DBuf<double> dC(nn, st), dP(nn, st), dL(n, st);
         ScfIn in;
-        in.n = n; in.nocc = nocc; in.nscf = opt.nscf; in.dH = dH.p; in.dS = dS.p; in.d_int2 = dI.p;
+        in.n = n; in.nocc = nocc; in.nscf = opt.nscf; in.dH = dH.p; in.dS = dS.p; in.d_int2 = d_int2;
         in.tolE = opt.tolE; in.tolP = opt.tolP; in.alpha = opt.mix_alpha;
         in.accel = opt.scf_accel; in.diis_size = opt.diis_size > 0 ? opt.diis_size : 8;
         in.purify = opt.purify != 0;
@@ -180,6 +204,13 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         // iterations remove what they left out before convergence is accepted
         if (opt.incremental) in.inc_screen = std::max(opt.schwarz, 1e-10);
         in.direct_ctx = plan.get();
+        if (bm) {  // Fock builds shared with the rest of the wave
+            in.direct_jk = [](Context& c, void* user, const double* P, double* G, double screen) {
+                auto* m = (BatchMember*)user;
+                m->wave->digest(m->mol, c, P, G, screen);
+            };
+            in.direct_ctx = bm;
+        }
         DBuf<double> dP0;
         if (opt.guess == 1) {  // superposition of atomic densities instead of P = 0
             dP0.alloc(nn, st);
@@ -188,6 +219,8 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
             ctx.trace_mark("guess");
         }
         ScfOut so = run_scf(ctx, in, dC.p, dP.p, dL.p);
+        if (bm) res->ms_fock = bm->wave->fock_ms();
+        wave_exit.now();
         res->ms_scf = ts.ms();
         conv = so.converged;
         double Enuc = 0;
@@ -210,10 +243,10 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
             HF_CHECK(mo <= n, HFGPU_ERR_INVALID, "mp2_nocc larger than the basis");
             const int mv = n - mo;
             if (mo > 0 && mv > 0 && opt.mp2 == HFGPU_MP2_SPLIT_BF16) {
-                res->E2 = mp2_energy_mixed(ctx, n, dI.p, dC.p, mo, dL.p);
+                res->E2 = mp2_energy_mixed(ctx, n, d_int2, dC.p, mo, dL.p);
             } else if (mo > 0 && mv > 0) {
                 DBuf<double> iajb((size_t)mo * mv * mo * mv, st);
-                ao2mo_fp64(ctx, n, dI.p, dC.p, mo, dC.p + (size_t)n * mo, mv, iajb.p);
+                ao2mo_fp64(ctx, n, d_int2, dC.p, mo, dC.p + (size_t)n * mo, mv, iajb.p);
                 res->E2 = mp2_energy(ctx, mo, mv, iajb.p, dL.p);
             }
             res->ms_mp2 = tm.ms();
@@ -231,7 +264,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         ctx.trace_mark("download");
         ctx.trace_report();
         ctx.settle_timers();
-        res->ms_fock = ctx.stat_fock_ms;
+        if (!bm) res->ms_fock = ctx.stat_fock_ms;
         res->ms_fock_full = ctx.stat_fock_full_ms;
         res->n_fock_full = ctx.stat_fock_full_n;
         res->block_elems = (double)es.n_block_elems;
@@ -240,6 +273,13 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         res->ms_tc_step1 = ctx.stat_tc_step1_ms;
         res->n_tc_step1 = ctx.stat_tc_step1_n;
 }
+
+static void streams_batch(int nmol, const int* natoms, const int* atno, const double* xyz,
+                          const std::vector<int64_t>& a0, const hfgpu_options* opt, hfgpu_result* res,
+                          std::vector<int>& rc, std::vector<std::string>& err, int dev);
+static void fused_batch(int nmol, const int* natoms, const int* atno, const double* xyz,
+                        const std::vector<int64_t>& a0, const hfgpu_options* opt, hfgpu_result* res,
+                        std::vector<int>& rc, std::vector<std::string>& err, int dev);
 
 extern "C" {
 
@@ -635,8 +675,32 @@ int hfgpu_rhf_batch(int nmol, const int* natoms, const int* atno, const double* 
         set_last_error("hfgpu_rhf_batch: no CUDA device");
         return HFGPU_ERR_NO_DEVICE;
     }
-    // molecules in flight at once, each on its own context (streams, handles):
-    // while one waits on a host-side convergence check the others fill the GPU
+    if (!opt || opt->batch_mode == 0) {
+        fused_batch(nmol, natoms, atno, xyz, a0, opt, res, rc, err, dev);
+    } else {
+        streams_batch(nmol, natoms, atno, xyz, a0, opt, res, rc, err, dev);
+    }
+    int first = HFGPU_OK;
+    for (int m = 0; m < nmol; ++m)
+        if (rc[m] != HFGPU_OK) {
+            res[m].niter = -rc[m];
+            if (first == HFGPU_OK) {
+                first = rc[m];
+                set_last_error("molecule " + std::to_string(m) + ": " + err[m]);
+            }
+        }
+    return first;
+}
+
+}  // extern "C"
+
+// hfgpu_rhf_batch, batch_mode 1: each molecule on its own context (streams, handles),
+// batch_streams at once; while one waits on a host-side convergence check the
+// others fill the GPU
+static void streams_batch(int nmol, const int* natoms, const int* atno, const double* xyz,
+                          const std::vector<int64_t>& a0, const hfgpu_options* opt, hfgpu_result* res,
+                          std::vector<int>& rc, std::vector<std::string>& err, int dev)
+{
     int nw = opt && opt->batch_streams > 0 ? opt->batch_streams : 8;
     nw = std::max(1, std::min(nw, std::min(nmol, 64)));
     std::atomic<int> next{0};
@@ -671,16 +735,82 @@ int hfgpu_rhf_batch(int nmol, const int* natoms, const int* atno, const double* 
         for (int w = 0; w < nw; ++w) th.emplace_back(work);
         for (auto& t : th) t.join();
     }
-    int first = HFGPU_OK;
-    for (int m = 0; m < nmol; ++m)
-        if (rc[m] != HFGPU_OK) {
-            res[m].niter = -rc[m];
-            if (first == HFGPU_OK) {
-                first = rc[m];
-                set_last_error("molecule " + std::to_string(m) + ": " + err[m]);
-            }
-        }
-    return first;
 }
 
-}  // extern "C"
+// hfgpu_rhf_batch, batch_mode 0: waves of molecules, largest first, each wave at
+// most batch_streams molecules (32 by default) whose packed integrals and MBPT2
+// work arrays fit a device-memory budget.  One thread per molecule runs its
+// pipeline; the wave's BatchWave joins their ERI launches and Fock builds.
+static void fused_batch(int nmol, const int* natoms, const int* atno, const double* xyz,
+                        const std::vector<int64_t>& a0, const hfgpu_options* opt, hfgpu_result* res,
+                        std::vector<int>& rc, std::vector<std::string>& err, int dev)
+{
+    const int cap = opt && opt->batch_streams > 0 ? std::min(opt->batch_streams, 256) : 32;
+    // sizes (molecules with bad input get 0 and fail on their own thread)
+    std::vector<int> nbf(nmol, 0), order(nmol);
+    for (int m = 0; m < nmol; ++m) {
+        nbf[m] = natoms[m] > 0 ? hfgpu_basis_size(natoms[m], atno + a0[m]) : 0;
+        order[m] = m;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return nbf[x] > nbf[y]; });
+    // device bytes a molecule holds in a wave: its packed integrals and quartet
+    // blocks, and at its MBPT2 stage two pair x occupied x virtual arrays
+    auto bytes = [&](int m) {
+        const double n = nbf[m], o = 0.2 * n, v = n - o;
+        return 8.0 * (1.2 * (double)packed_size(nbf[m]) + 2.0 * n * (n + 1) / 2 * o * v + 8.0 * n * n);
+    };
+    size_t freeb = 0, totb = 0;
+    if (cudaSetDevice(dev) != cudaSuccess || cudaMemGetInfo(&freeb, &totb) != cudaSuccess) freeb = 0;
+    const double budget = std::max(8e9, 0.6 * (double)freeb);
+    size_t i = 0;
+    while (i < order.size()) {
+        std::vector<int> wave;
+        double used = 0;
+        while (i < order.size() && (int)wave.size() < cap && (wave.empty() || used + bytes(order[i]) <= budget)) {
+            used += bytes(order[i]);
+            wave.push_back(order[i++]);
+        }
+        Context* wctx = nullptr;
+        const int r0 = guard([&] {
+            HF_CUDA(cudaSetDevice(dev));
+            wctx = context_acquire();
+        });
+        if (r0 != HFGPU_OK) {
+            for (int m : wave) {
+                rc[m] = r0;
+                err[m] = hfgpu_last_error();
+            }
+            continue;
+        }
+        wctx->tune = (opt && opt->autotune != 0) || tune_env_enabled();
+        {
+            BatchWave bw((int)wave.size(), wctx);
+            auto work = [&](int k) {
+                const int m = wave[k];
+                BatchMember mem{&bw, k};
+                Context* c = nullptr;
+                int r = guard([&] {
+                    HF_CUDA(cudaSetDevice(dev));
+                    c = context_acquire();
+                });
+                int conv = 1, nscf = 0;
+                if (r == HFGPU_OK)
+                    r = guard([&] { rhf_impl(natoms[m], atno + a0[m], xyz + 3 * a0[m], opt, &res[m], nullptr, nullptr,
+                                             conv, nscf, nullptr, c, &mem); });
+                else
+                    bw.leave(k);
+                if (r == HFGPU_OK && !conv) {
+                    r = HFGPU_ERR_NOT_CONVERGED;
+                    set_last_error("SCF did not converge in " + std::to_string(nscf) + " iterations.");
+                }
+                rc[m] = r;
+                if (r != HFGPU_OK) err[m] = hfgpu_last_error();
+                context_release(c);
+            };
+            std::vector<std::thread> th;
+            for (size_t k = 0; k < wave.size(); ++k) th.emplace_back(work, (int)k);
+            for (auto& t : th) t.join();
+        }
+        context_release(wctx);
+    }
+}

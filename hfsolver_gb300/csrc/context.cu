@@ -18,6 +18,7 @@ void set_last_error(const std::string& m) { g_last_error = m; }
 
 static std::atomic<int64_t> g_launches{0};
 void count_launch(int n) { g_launches += n; }
+int64_t launches_counted() { return g_launches.load(); }
 
 static std::mutex g_ctx_mutex;
 static std::vector<Context*> g_ctx;

@@ -202,6 +202,7 @@ static void launch_class(Context& ctx, EriPlan* P, ClassPlan& c, int mode, doubl
     EriArgs a;
     a.blocks = blocks;
     a.nq_class = c.nq;
+    a.mol_out = mode == MODE_PACKED ? P->mol_out.p : nullptr;
     a.sh = P->shdev();
     a.pr = P->prdev();
     a.boys = ctx.boys;
@@ -360,6 +361,7 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
             groups.push_back(std::move(gg));
         }
         P->gpairs = to_device(gp, st);
+        P->h_gpairs = gp;
         P->dQ = to_device(P->Q, st);
 
         // segments per class
@@ -431,6 +433,7 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
                 }
             }
         P->prefix = to_device(prefix, st);
+        P->h_prefix = prefix;
         P->stats = stt;
         HF_CUDA(cudaStreamSynchronize(st));
         ctx.trace_mark("plan classes");
@@ -571,6 +574,13 @@ void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG, double s
         a.Q = P->dQ.p;
         a.Dm = Dm.p;
         a.ns = ns;
+        a.mol_n = nullptr;
+        a.mol_P = nullptr;
+        a.mol_Gh = nullptr;
+        a.mol_screen = nullptr;
+        a.mol_Dm = nullptr;
+        a.mol_ns = nullptr;
+        a.mol_sh0 = nullptr;
         a.split = digest_split_tuned(ctx, c, a, nn);
         cudaStream_t s = ctx.aux[slot++ % Context::NAUX];
         launch_digest(c, a, s);
@@ -674,6 +684,296 @@ void eri_compute(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks, EriS
         *st = P->stats;
         st->ms = ms;
     }
+}
+
+
+
+// ------------------------------------------------------------------ batches of molecules
+// Several molecules' plans as one: shells, pairs, primitive-pair records, groups
+// and prefix sums concatenated with their indices offset, and every class's
+// segments from all molecules in one list (each segment tagged with its
+// molecule), so that one launch per class computes or digests the quartets of
+// every molecule.  Function indices stay local to each molecule.
+EriPlan* eri_plan_merge(Context& ctx, const std::vector<EriPlan*>& plans)
+{
+    cudaStream_t st = ctx.stream;
+    auto M = new EriPlan();
+    try {
+        M->nmol = (int)plans.size();
+        std::vector<int> L, np, p0, c0, f0, cfn;
+        std::vector<double> xyz, alpha, coef;
+        std::vector<int64_t> pref_base(plans.size()), gp_base(plans.size()), pd_base(plans.size());
+        int64_t off = 0;
+        int pair0 = 0, shell0 = 0;
+        for (size_t m = 0; m < plans.size(); ++m) {
+            const EriPlan& P = *plans[m];
+            const Basis& b = P.basis;
+            const int a0 = (int)alpha.size(), cc0 = (int)coef.size(), ff0 = (int)cfn.size();
+            M->mol_nbf.push_back(b.nbf);
+            M->mol_ns.push_back((int)b.shells.size());
+            M->mol_sh0.push_back(shell0);
+            for (const Shell& s : b.shells) {
+                L.push_back(s.L);
+                np.push_back(s.nprim);
+                p0.push_back(s.prim0 + a0);
+                c0.push_back(s.coef0 + cc0);
+                f0.push_back(s.cfn0 + ff0);
+                xyz.push_back(s.x);
+                xyz.push_back(s.y);
+                xyz.push_back(s.z);
+            }
+            alpha.insert(alpha.end(), b.alpha.begin(), b.alpha.end());
+            coef.insert(coef.end(), b.coef.begin(), b.coef.end());
+            cfn.insert(cfn.end(), b.comp_fn.begin(), b.comp_fn.end());
+            for (int id = 0; id < P.npair; ++id) {
+                M->pA.push_back(P.pA[id] + shell0);
+                M->pB.push_back(P.pB[id] + shell0);
+                M->pK.push_back(P.pK[id]);
+                M->pT.push_back(P.pT[id]);
+                M->poff.push_back(P.poff[id] + off);
+                M->Q.push_back(P.Q[id]);
+            }
+            gp_base[m] = (int64_t)M->h_gpairs.size();
+            for (int g : P.h_gpairs) M->h_gpairs.push_back(g + pair0);
+            pref_base[m] = (int64_t)M->h_prefix.size();
+            M->h_prefix.insert(M->h_prefix.end(), P.h_prefix.begin(), P.h_prefix.end());
+            pd_base[m] = off;
+            off += (int64_t)P.pdata.n;
+            pair0 += P.npair;
+            shell0 += (int)b.shells.size();
+            M->stats.n_quartets += P.stats.n_quartets;
+            M->stats.n_bf_quartets += P.stats.n_bf_quartets;
+            M->stats.n_prim_quartets += P.stats.n_prim_quartets;
+            M->stats.flops += P.stats.flops;
+        }
+        HF_CHECK(M->h_gpairs.size() < (1u << 31) && pair0 < (1 << 30), HFGPU_ERR_UNSUPPORTED,
+                 "batch too large for 32-bit pair indexing");
+        M->npair = pair0;
+        M->sL = to_device(L, st); M->snp = to_device(np, st); M->sp0 = to_device(p0, st);
+        M->sc0 = to_device(c0, st); M->scf = to_device(f0, st); M->cfn = to_device(cfn, st);
+        M->sxyz = to_device(xyz, st); M->alpha = to_device(alpha, st); M->coef = to_device(coef, st);
+        M->dA = to_device(M->pA, st); M->dB = to_device(M->pB, st); M->dK = to_device(M->pK, st);
+        M->doff = to_device(M->poff, st);
+        M->dQ = to_device(M->Q, st);
+        M->gpairs = to_device(M->h_gpairs, st);
+        M->prefix = to_device(M->h_prefix, st);
+        M->pdata.alloc(std::max<int64_t>(off, 1), st);
+        for (size_t m = 0; m < plans.size(); ++m)
+            if (plans[m]->pdata.n)
+                HF_CUDA(cudaMemcpyAsync(M->pdata.p + pd_base[m], plans[m]->pdata.p, plans[m]->pdata.n * sizeof(double),
+                                        cudaMemcpyDeviceToDevice, st));
+        for (int tb = 0; tb < NPTYPE; tb++)
+            for (int tk = tb; tk < NPTYPE; tk++) {
+                ClassPlan c;
+                c.tb = tb;
+                c.tk = tk;
+                for (size_t m = 0; m < plans.size(); ++m)
+                    for (const ClassPlan& pc : plans[m]->classes) {
+                        if (pc.tb != tb || pc.tk != tk) continue;
+                        for (size_t i = 0; i < pc.segs.size(); ++i) {
+                            Seg s = pc.segs[i];
+                            s.pref0 += pref_base[m];
+                            s.bra0 += (int)gp_base[m];
+                            s.ket0 += (int)gp_base[m];
+                            s.mol = (int)m;
+                            s.qoff = c.nq;
+                            c.nq += s.nq;
+                            c.segs.push_back(s);
+                            c.kprod.push_back(pc.kprod[i]);
+                        }
+                    }
+                if (c.segs.empty()) continue;
+                HF_CHECK(c.nq < (1ll << 31), HFGPU_ERR_UNSUPPORTED, "quartet class too large for 32-bit indexing");
+                c.dsegs = to_device(c.segs, st);
+                layout_class(ctx, c, 16);
+                M->classes.push_back(std::move(c));
+            }
+        HF_CUDA(cudaStreamSynchronize(st));
+        return M;
+    } catch (...) {
+        delete M;
+        throw;
+    }
+}
+
+// largest |P| of every shell pair of every molecule with a screened build
+__global__ void batch_dmax_kernel(int nmol, const int64_t* __restrict__ dm_prefix, const int* __restrict__ L,
+                                  const int* __restrict__ cfn0, const int* __restrict__ comp_fn,
+                                  const int* __restrict__ mol_n, const int* __restrict__ mol_ns,
+                                  const int* __restrict__ mol_sh0, const double* const* __restrict__ mol_P,
+                                  const double* __restrict__ mol_screen, double* __restrict__ Dm)
+{
+    const int64_t total = dm_prefix[nmol];
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nmol - 1;  // last molecule with dm_prefix <= idx
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (dm_prefix[mid] <= idx) lo = mid; else hi = mid - 1;
+        }
+        if (mol_screen[lo] <= 0.0) continue;
+        const int ns = mol_ns[lo], n = mol_n[lo];
+        const int64_t e = idx - dm_prefix[lo];
+        const int s1 = mol_sh0[lo] + (int)(e / ns), s2 = mol_sh0[lo] + (int)(e % ns);
+        const double* P = mol_P[lo];
+        double m = 0.0;
+        for (int i = 0; i < ncart(L[s1]); ++i) {
+            const int f = comp_fn[cfn0[s1] + i];
+            if (f < 0) continue;
+            for (int j = 0; j < ncart(L[s2]); ++j) {
+                const int g = comp_fn[cfn0[s2] + j];
+                if (g >= 0) m = fmax(m, fabs(P[f + (int64_t)g * n]));
+            }
+        }
+        Dm[idx] = m;
+    }
+}
+
+// G_m = Gh_m + Gh_m^T for every molecule of the build
+__global__ void batch_sym_kernel(int nmol, const int64_t* __restrict__ nn_prefix, const int* __restrict__ mol_n,
+                                 const double* __restrict__ Gh, double* const* __restrict__ mol_G,
+                                 const double* __restrict__ mol_screen)
+{
+    const int64_t total = nn_prefix[nmol];
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nmol - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (nn_prefix[mid] <= idx) lo = mid; else hi = mid - 1;
+        }
+        if (mol_screen[lo] < 0.0) continue;
+        const int n = mol_n[lo];
+        const int64_t e = idx - nn_prefix[lo];
+        const int i = (int)(e % n), j = (int)(e / n);
+        const double* gh = Gh + nn_prefix[lo];
+        mol_G[lo][e] = gh[e] + gh[j + (int64_t)i * n];
+    }
+}
+
+void BatchDigest::setup(Context& ctx, const EriPlan* P, cudaStream_t s)
+{
+    nmol = P->nmol;
+    std::vector<int64_t> nnp(nmol + 1, 0), dmp(nmol + 1, 0);
+    for (int m = 0; m < nmol; ++m) {
+        nnp[m + 1] = nnp[m] + (int64_t)P->mol_nbf[m] * P->mol_nbf[m];
+        dmp[m + 1] = dmp[m] + (int64_t)P->mol_ns[m] * P->mol_ns[m];
+    }
+    nn_prefix = to_device(nnp, s);
+    dm_prefix = to_device(dmp, s);
+    mol_n = to_device(P->mol_nbf, s);
+    mol_ns = to_device(P->mol_ns, s);
+    mol_sh0 = to_device(P->mol_sh0, s);
+    Gh.alloc(std::max<int64_t>(nnp[nmol], 1), s);
+    Dm.alloc(std::max<int64_t>(dmp[nmol], 1), s);
+    std::vector<double*> gh(nmol);
+    std::vector<const double*> dm(nmol);
+    for (int m = 0; m < nmol; ++m) {
+        gh[m] = Gh.p + nnp[m];
+        dm[m] = Dm.p + dmp[m];
+    }
+    mol_Gh = to_device(gh, s);
+    mol_Dm = to_device(dm, s);
+    mol_P.alloc(nmol, s);
+    mol_G.alloc(nmol, s);
+    mol_screen.alloc(nmol, s);
+    HF_CUDA(cudaMallocHost((void**)&h_P, nmol * sizeof(const double*)));
+    HF_CUDA(cudaMallocHost((void**)&h_G, nmol * sizeof(double*)));
+    HF_CUDA(cudaMallocHost((void**)&h_screen, nmol * sizeof(double)));
+    for (int m = 0; m < nmol; ++m) {
+        h_P[m] = nullptr;
+        h_G[m] = nullptr;
+        h_screen[m] = -1.0;
+    }
+}
+
+BatchDigest::~BatchDigest()
+{
+    if (exec) cudaGraphExecDestroy(exec);
+    if (h_P) cudaFreeHost((void*)h_P);
+    if (h_G) cudaFreeHost(h_G);
+    if (h_screen) cudaFreeHost(h_screen);
+}
+
+// One Fock build for every molecule whose h_screen >= 0: Gh zeroed, shell-pair
+// maxima for the screened ones, one digest launch per quartet class over all
+// molecules' quartets, and the symmetrisation into each molecule's G.
+static void batch_digest_launches(Context& ctx, EriPlan* P, BatchDigest& t, cudaStream_t s)
+{
+    HF_CUDA(cudaMemsetAsync(t.Gh.p, 0, t.Gh.n * sizeof(double), s));
+    const int64_t dm_total = t.Dm.n, nn_total = t.Gh.n;
+    const unsigned gd = (unsigned)std::max<int64_t>(1, std::min<int64_t>((dm_total + 255) / 256, ctx.num_sms * 8));
+    batch_dmax_kernel<<<gd, 256, 0, s>>>(t.nmol, t.dm_prefix.p, P->sL.p, P->scf.p, P->cfn.p, t.mol_n.p, t.mol_ns.p,
+                                        t.mol_sh0.p, t.mol_P.p, t.mol_screen.p, t.Dm.p);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+    for (int ci = (int)P->classes.size() - 1; ci >= 0; --ci) {
+        auto& c = P->classes[ci];
+        if (c.nq == 0) continue;
+        DigestArgs a;
+        a.sh = P->shdev();
+        a.pr = P->prdev();
+        a.gpairs = P->gpairs.p;
+        a.prefix = P->prefix.p;
+        a.list = nullptr;
+        a.segs = c.dsegs.p;
+        a.nseg = (int)c.segs.size();
+        a.nq = c.nq;
+        a.blocks = P->blocks.p + c.boff;
+        a.P = nullptr;
+        a.n = 0;
+        a.Gh = nullptr;
+        a.screen = 0.0;
+        a.Q = P->dQ.p;
+        a.Dm = nullptr;
+        a.ns = 0;
+        a.mol_n = t.mol_n.p;
+        a.mol_P = t.mol_P.p;
+        a.mol_Gh = t.mol_Gh.p;
+        a.mol_screen = t.mol_screen.p;
+        a.mol_Dm = t.mol_Dm.p;
+        a.mol_ns = t.mol_ns.p;
+        a.mol_sh0 = t.mol_sh0.p;
+        int split = digest_split(c);
+        if (ctx.tune) tune_get(TUNE_DIGEST, c.tb, c.tk, tune_bucket(c.nq), &split);
+        a.split = split;
+        launch_digest(c, a, s);
+    }
+    const unsigned gs = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nn_total + 255) / 256, ctx.num_sms * 8));
+    batch_sym_kernel<<<gs, 256, 0, s>>>(t.nmol, t.nn_prefix.p, t.mol_n.p, t.Gh.p, t.mol_G.p, t.mol_screen.p);
+    count_launch();
+    HF_CUDA(cudaGetLastError());
+}
+
+void eri_digest_batch(Context& ctx, EriPlan* P, BatchDigest& t, cudaStream_t s)
+{
+    HF_CHECK(P->blocks.p != nullptr && P->nmol == t.nmol, HFGPU_ERR_INVALID, "eri_digest_batch: plan and tables differ");
+    // this build's densities, outputs and screens
+    HF_CUDA(cudaMemcpyAsync(t.mol_P.p, t.h_P, t.nmol * sizeof(const double*), cudaMemcpyHostToDevice, s));
+    HF_CUDA(cudaMemcpyAsync(t.mol_G.p, t.h_G, t.nmol * sizeof(double*), cudaMemcpyHostToDevice, s));
+    HF_CUDA(cudaMemcpyAsync(t.mol_screen.p, t.h_screen, t.nmol * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (!t.exec) {
+        // the launches of a build are the same every iteration: captured once into a
+        // CUDA graph and replayed (the tables above are read from device memory)
+        const int64_t before = launches_counted();
+        cudaGraph_t g = nullptr;
+        HF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        try {
+            batch_digest_launches(ctx, P, t, s);
+        } catch (...) {
+            cudaStreamEndCapture(s, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        HF_CUDA(cudaStreamEndCapture(s, &g));
+        t.graph_kernels = launches_counted() - before;
+        count_launch(-(int)t.graph_kernels);  // captured, not yet run
+        const cudaError_t e = cudaGraphInstantiate(&t.exec, g, 0);
+        cudaGraphDestroy(g);
+        HF_CUDA(e);
+    }
+    HF_CUDA(cudaGraphLaunch(t.exec, s));
+    count_launch((int)t.graph_kernels);
 }
 
 }  // namespace hfgpu

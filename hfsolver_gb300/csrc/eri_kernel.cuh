@@ -40,6 +40,7 @@ struct Seg {
     int nbra;
     int list;        // 1: explicit (bra, ket) list
     int split;       // lanes per quartet (power of two): they share its primitive pairs
+    int mol;         // molecule of the segment in a batched plan (0 for one molecule)
 };
 
 enum { MODE_PACKED = 0, MODE_DIAG = 1 };
@@ -57,6 +58,7 @@ struct EriArgs {
     double* out;     // packed integrals (may be null), or diagonal buffer [pair][36]
     double* blocks;  // class-wise quartet blocks [element][quartet] (may be null)
     int64_t nq_class;
+    const int64_t* mol_out;  // batched plans: offset of each molecule's packed array in out (else null)
 };
 
 using KernelFn = void (*)(EriArgs);
@@ -84,8 +86,8 @@ template <int TB, int TK, int CH>
 struct EriBody;  // generated
 
 template <int TB, int TK, int MODE, int CH>
-__device__ __forceinline__ void run_chunk(const EriArgs& a, int bra, int ket, bool active, int64_t qg, int sub,
-                                          int split)
+__device__ __forceinline__ void run_chunk(const EriArgs& a, double* out, int bra, int ket, bool active, int64_t qg,
+                                          int sub, int split)
 {
     using CI = ClassInfo<TB, TK>;
     double acc[CI::NAB * CI::NCD];
@@ -120,7 +122,7 @@ __device__ __forceinline__ void run_chunk(const EriArgs& a, int bra, int ket, bo
 #pragma unroll
         for (int s = 0; s < CI::NCD; ++s) {
             const int icd = CH * CI::NCD + s;
-            a.out[(int64_t)ket * 36 + icd] = acc[icd * CI::NCD + s];
+            out[(int64_t)ket * 36 + icd] = acc[icd * CI::NCD + s];
         }
     } else {
         if (a.blocks) {  // the whole block, one element plane per component quartet (coalesced in q)
@@ -130,7 +132,7 @@ __device__ __forceinline__ void run_chunk(const EriArgs& a, int bra, int ket, bo
                 for (int ab = 0; ab < CI::NAB; ++ab)
                     a.blocks[(int64_t)(ab * CI::NCDT + CH * CI::NCD + s) * a.nq_class + qg] = acc[ab * CI::NCD + s];
         }
-        if (!a.out) return;
+        if (!out) return;
         const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
         const int* fa = a.sh.comp_fn + a.sh.cfn0[A];
         const int* fb = a.sh.comp_fn + a.sh.cfn0[B];
@@ -151,21 +153,21 @@ __device__ __forceinline__ void run_chunk(const EriArgs& a, int bra, int ket, bo
                 if (sameBK && ij < kl) continue;
                 // pair indices fit 32 bits (n <= 512); only the packed position needs 64
                 const int64_t idx = ij >= kl ? (((int64_t)ij * (ij + 1)) >> 1) + kl : (((int64_t)kl * (kl + 1)) >> 1) + ij;
-                a.out[idx] = acc[ab * CI::NCD + s];
+                out[idx] = acc[ab * CI::NCD + s];
             }
         }
     }
 }
 
 template <int TB, int TK, int MODE, int G, int CH>
-__device__ __forceinline__ void dispatch_chunk(const EriArgs& a, int chunk, int bra, int ket, bool active, int64_t qg,
-                                               int sub, int split)
+__device__ __forceinline__ void dispatch_chunk(const EriArgs& a, double* out, int chunk, int bra, int ket, bool active,
+                                               int64_t qg, int sub, int split)
 {
     if constexpr (CH < G) {
         if (chunk == CH)
-            run_chunk<TB, TK, MODE, CH>(a, bra, ket, active, qg, sub, split);
+            run_chunk<TB, TK, MODE, CH>(a, out, bra, ket, active, qg, sub, split);
         else
-            dispatch_chunk<TB, TK, MODE, G, CH + 1>(a, chunk, bra, ket, active, qg, sub, split);
+            dispatch_chunk<TB, TK, MODE, G, CH + 1>(a, out, chunk, bra, ket, active, qg, sub, split);
     }
 }
 
@@ -209,7 +211,9 @@ __global__ void __launch_bounds__(ERI_BLOCK) eri_class_kernel(EriArgs a)
         bra = a.gpairs[sg.bra0 + l2];
         ket = a.gpairs[sg.ket0 + (q - (int)pf[l2])];
     }
-    dispatch_chunk<TB, TK, MODE, CI::G, 0>(a, chunk, bra, ket, active, sg.qoff + q, sub, split);
+    double* out = a.out;
+    if (out && a.mol_out) out += a.mol_out[sg.mol];  // the segment's molecule's packed array
+    dispatch_chunk<TB, TK, MODE, CI::G, 0>(a, out, chunk, bra, ket, active, sg.qoff + q, sub, split);
 }
 
 template <int TB, int TK>

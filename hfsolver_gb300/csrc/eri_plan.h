@@ -40,6 +40,15 @@ struct EriPlan {
     std::vector<ClassPlan> classes;
     DBuf<double> blocks;  // class-wise quartet blocks, kept for the SCF's Fock builds
     EriStats stats;
+    // host copies of the grouped pair ids and prefix sums (for merging plans)
+    std::vector<int> h_gpairs;
+    std::vector<int64_t> h_prefix;
+    // batched plans (eri_plan_merge): the molecules' basis sizes, shell counts and
+    // first shells, and each molecule's packed-array offset in the output of
+    // eri_compute (device; null for one molecule)
+    int nmol = 1;
+    std::vector<int> mol_nbf, mol_ns, mol_sh0;
+    DBuf<int64_t> mol_out;
     ShellDev shdev() const
     {
         return ShellDev{sL.p, snp.p, sxyz.p, sp0.p, sc0.p, scf.p, alpha.p, coef.p, cfn.p};

@@ -245,6 +245,34 @@ void rhf_gradient(Context& ctx, EriPlan* plan, int natoms, const int* atno, cons
 // probe.cu: measured FP64 FMA rate (TFLOP/s)
 double probe_fp64_tflops(Context& ctx);
 
+// ---------------------------------------------------------------- batches of molecules
+// eri.cu: several molecules' plans merged into one (segments tagged by
+// molecule), so one launch per quartet class computes or digests all of them
+EriPlan* eri_plan_merge(Context& ctx, const std::vector<EriPlan*>& plans);
+// device tables of a batched Fock build over a merged plan: per molecule its
+// density and output pointers and its screen (< 0: not in this build), set in
+// the pinned host copies h_P, h_G, h_screen before each eri_digest_batch
+struct BatchDigest {
+    int nmol = 0;
+    DBuf<int64_t> nn_prefix, dm_prefix;  // element offsets of the molecules' n x n and ns x ns blocks
+    DBuf<int> mol_n, mol_ns, mol_sh0;
+    DBuf<double> Gh, Dm;                 // half matrices and shell-pair maxima of all molecules
+    DBuf<double*> mol_Gh, mol_G;
+    DBuf<const double*> mol_Dm, mol_P;
+    DBuf<double> mol_screen;
+    const double** h_P = nullptr;
+    double** h_G = nullptr;
+    double* h_screen = nullptr;
+    cudaGraphExec_t exec = nullptr;      // the build's launches, captured on first use
+    int64_t graph_kernels = 0;
+    void setup(Context& ctx, const EriPlan* P, cudaStream_t s);
+    ~BatchDigest();
+};
+// one Fock build (G = J - K/2) for every molecule with h_screen >= 0, on stream s
+void eri_digest_batch(Context& ctx, EriPlan* P, BatchDigest& t, cudaStream_t s);
+// kernels counted so far (context.cu)
+int64_t launches_counted();
+
 // noalloc.cu: load the module that holds the allocation-free Fock build's fixed
 // scratch array on device dev (the current device) and cache its device
 // address; called when a device context is created, so that the array's device

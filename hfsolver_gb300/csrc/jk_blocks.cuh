@@ -39,19 +39,57 @@ struct DigestArgs {
     const double* Q;
     const double* Dm;
     int ns;
+    // batched plans (mol_n != null): per molecule its basis size, density,
+    // half-matrix output, screen (< 0: not part of this build), shell-pair
+    // maximum table, shell count and first shell; the scalars above are unused
+    const int* mol_n;
+    const double* const* mol_P;
+    double* const* mol_Gh;
+    const double* mol_screen;
+    const double* const* mol_Dm;
+    const int* mol_ns;
+    const int* mol_sh0;
 };
+
+// the per-molecule view of a batched build (the arguments themselves for one molecule)
+struct DigestMol {
+    int n, ns, sh0;
+    const double* P;
+    double* Gh;
+    double screen;
+    const double* Dm;
+};
+
+__device__ __forceinline__ bool digest_mol(const DigestArgs& a, int mol, DigestMol& m)
+{
+    if (!a.mol_n) {
+        m = DigestMol{a.n, a.ns, 0, a.P, a.Gh, a.screen, a.Dm};
+        return true;
+    }
+    m.screen = a.mol_screen[mol];
+    if (m.screen < 0.0) return false;
+    m.n = a.mol_n[mol];
+    m.ns = a.mol_ns[mol];
+    m.sh0 = a.mol_sh0[mol];
+    m.P = a.mol_P[mol];
+    m.Gh = a.mol_Gh[mol];
+    m.Dm = a.mol_Dm ? a.mol_Dm[mol] : nullptr;
+    return true;
+}
 
 // true if the quartet's whole contribution is below the screening threshold:
 // |(ab|cd)| <= Q_bra Q_ket, and the largest density factor it meets is
 // 2|P_ab|, 2|P_cd| (Coulomb) or |P_ac|/2 ... (exchange)
-__device__ __forceinline__ bool digest_skip(const DigestArgs& a, int bra, int ket, int A, int B, int C, int D)
+__device__ __forceinline__ bool digest_skip(const DigestArgs& a, const DigestMol& m, int bra, int ket, int A, int B,
+                                            int C, int D)
 {
-    if (a.screen <= 0.0) return false;
-    const double* Dm = a.Dm;
-    const int ns = a.ns;
+    if (m.screen <= 0.0) return false;
+    const double* Dm = m.Dm;
+    const int ns = m.ns;
+    A -= m.sh0; B -= m.sh0; C -= m.sh0; D -= m.sh0;
     const double dj = fmax(Dm[A * ns + B], Dm[C * ns + D]);
     const double dk = fmax(fmax(Dm[A * ns + C], Dm[B * ns + D]), fmax(Dm[A * ns + D], Dm[B * ns + C]));
-    return a.Q[bra] * a.Q[ket] * fmax(2.0 * dj, 0.5 * dk) < a.screen;
+    return a.Q[bra] * a.Q[ket] * fmax(2.0 * dj, 0.5 * dk) < m.screen;
 }
 
 template <int TB, int TK>
@@ -84,8 +122,10 @@ __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
         bra = a.gpairs[sg.bra0 + l2];
         ket = a.gpairs[sg.ket0 + (q - (int)pf[l2])];
     }
+    DigestMol mm;
+    if (!digest_mol(a, sg.mol, mm)) return;
     const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
-    if (digest_skip(a, bra, ket, A, B, C, D)) return;
+    if (digest_skip(a, mm, bra, ket, A, B, C, D)) return;
     int fa[NA], fb[NB], fc[NC], fd[ND];
 #pragma unroll
     for (int i = 0; i < NA; ++i) fa[i] = a.sh.comp_fn[a.sh.cfn0[A] + i];
@@ -95,8 +135,9 @@ __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
     for (int i = 0; i < NC; ++i) fc[i] = a.sh.comp_fn[a.sh.cfn0[C] + i];
 #pragma unroll
     for (int i = 0; i < ND; ++i) fd[i] = a.sh.comp_fn[a.sh.cfn0[D] + i];
-    const int n = a.n;
-    auto Pv = [&](int x, int y) { return (x < 0 || y < 0) ? 0.0 : __ldg(a.P + x + (int64_t)y * n); };
+    const int n = mm.n;
+    const double* Pm = mm.P;
+    auto Pv = [&](int x, int y) { return (x < 0 || y < 0) ? 0.0 : __ldg(Pm + x + (int64_t)y * n); };
     const double f = (A == B ? 0.5 : 1.0) * (C == D ? 0.5 : 1.0) * (bra == ket ? 0.5 : 1.0);
     // accumulators indexed by the rolled (a, b) loop live in local memory and are
     // touched once per (a, b); everything indexed by (c, d) stays in registers
@@ -162,7 +203,7 @@ __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
                 kbd[ib * ND + id] += s_bd[id];
             }
         }
-    double* Gh = a.Gh;
+    double* Gh = mm.Gh;
     auto add = [&](int x, int y, double v) {
         if (x >= 0 && y >= 0 && v != 0.0) atomicAdd(Gh + x + (int64_t)y * n, v);
     };
@@ -222,8 +263,10 @@ __global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
         bra = a.gpairs[sg.bra0 + l2];
         ket = a.gpairs[sg.ket0 + (q - (int)pf[l2])];
     }
+    DigestMol mm;
+    if (!digest_mol(a, sg.mol, mm)) return;  // same answer for all lanes of the quartet
     const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
-    if (digest_skip(a, bra, ket, A, B, C, D)) return;  // same answer for all lanes of the quartet
+    if (digest_skip(a, mm, bra, ket, A, B, C, D)) return;  // same answer for all lanes of the quartet
     int fc[NC], fd[ND];
 #pragma unroll
     for (int i = 0; i < NC; ++i) fc[i] = a.sh.comp_fn[a.sh.cfn0[C] + i];
@@ -231,9 +274,10 @@ __global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
     for (int i = 0; i < ND; ++i) fd[i] = a.sh.comp_fn[a.sh.cfn0[D] + i];
     const int* fa = a.sh.comp_fn + a.sh.cfn0[A];
     const int* fb = a.sh.comp_fn + a.sh.cfn0[B];
-    const int n = a.n;
-    auto Pv = [&](int x, int y) { return (x < 0 || y < 0) ? 0.0 : __ldg(a.P + x + (int64_t)y * n); };
-    double* Gh = a.Gh;
+    const int n = mm.n;
+    const double* Pm = mm.P;
+    auto Pv = [&](int x, int y) { return (x < 0 || y < 0) ? 0.0 : __ldg(Pm + x + (int64_t)y * n); };
+    double* Gh = mm.Gh;
     auto add = [&](int x, int y, double v) {
         if (x >= 0 && y >= 0 && v != 0.0) atomicAdd(Gh + x + (int64_t)y * n, v);
     };

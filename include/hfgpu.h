@@ -233,7 +233,12 @@ typedef struct {
                             of free-atom densities (closer start, fewer iterations) */
     int eigensolver;     /* 0: own generalized eigensolver (as hfgpu_eigh) for 3 <= n <= 1024,
                             else cuSOLVER dsygvd; 1: cuSOLVER dsygvd always */
-    int reserved[2];
+    int batch_mode;      /* hfgpu_rhf_batch: 0 = waves of molecules share one ERI launch and,
+                            every SCF iteration, one Fock-build launch per quartet class (a
+                            replayed CUDA graph), batch_streams molecules per wave at most
+                            (<= 0: 32, fewer if their integrals would not fit); 1 = each molecule
+                            runs the whole pipeline on its own streams, batch_streams at once */
+    int reserved[1];
 } hfgpu_options;
 
 typedef struct {
@@ -282,9 +287,13 @@ int hfgpu_rhf_gradient(int natoms, const int *atno, const double *xyz, const hfg
 
 /* hfgpu_rhf for nmol molecules in one call: molecule m has natoms[m] atoms, its
  * charges and coordinates follow those of molecule m-1 in atno and xyz; res[m]
- * gets its results (res[m].niter = -status if it failed).  opt->batch_streams
- * molecules run at once, each on its own CUDA streams and library handles, so
- * small molecules share the GPU.  Returns the first failure's status (in
+ * gets its results (res[m].niter = -status if it failed).  The molecules run in
+ * waves (opt->batch_mode 0, by decreasing size): the integrals of a wave are one
+ * launch per quartet class, and every SCF iteration one batched Fock build
+ * serves every molecule of the wave still iterating, while each molecule's own
+ * SCF steps (DIIS, density, convergence test) run on its own streams.  With
+ * batch_mode 1, opt->batch_streams molecules run at once, each on its own CUDA
+ * streams and library handles.  Returns the first failure's status (in
  * molecule order), or HFGPU_OK. */
 int hfgpu_rhf_batch(int nmol, const int *natoms, const int *atno, const double *xyz,
                     const hfgpu_options *opt, hfgpu_result *res);
