@@ -739,8 +739,9 @@ static void streams_batch(int nmol, const int* natoms, const int* atno, const do
 
 // hfgpu_rhf_batch, batch_mode 0: waves of molecules, largest first, each wave at
 // most batch_streams molecules (32 by default) whose packed integrals and MBPT2
-// work arrays fit a device-memory budget.  One thread per molecule runs its
-// pipeline; the wave's BatchWave joins their ERI launches and Fock builds.
+// work arrays fit a device-memory budget; two waves in flight at a time.  One
+// thread per molecule runs its pipeline; the wave's BatchWave joins their ERI
+// launches and Fock builds.
 static void fused_batch(int nmol, const int* natoms, const int* atno, const double* xyz,
                         const std::vector<int64_t>& a0, const hfgpu_options* opt, hfgpu_result* res,
                         std::vector<int>& rc, std::vector<std::string>& err, int dev)
@@ -761,15 +762,21 @@ static void fused_batch(int nmol, const int* natoms, const int* atno, const doub
     };
     size_t freeb = 0, totb = 0;
     if (cudaSetDevice(dev) != cudaSuccess || cudaMemGetInfo(&freeb, &totb) != cudaSuccess) freeb = 0;
-    const double budget = std::max(8e9, 0.6 * (double)freeb);
-    size_t i = 0;
-    while (i < order.size()) {
+    // two waves run at once, so that one wave's Fock builds overlap the other
+    // wave's per-molecule SCF steps; each gets half of the memory budget
+    constexpr int WAVES_IN_FLIGHT = 2;
+    const double budget = std::max(4e9, 0.6 * (double)freeb / WAVES_IN_FLIGHT);
+    std::vector<std::vector<int>> waves;
+    for (size_t i = 0; i < order.size();) {
         std::vector<int> wave;
         double used = 0;
         while (i < order.size() && (int)wave.size() < cap && (wave.empty() || used + bytes(order[i]) <= budget)) {
             used += bytes(order[i]);
             wave.push_back(order[i++]);
         }
+        waves.push_back(std::move(wave));
+    }
+    auto run_wave = [&](const std::vector<int>& wave) {
         Context* wctx = nullptr;
         const int r0 = guard([&] {
             HF_CUDA(cudaSetDevice(dev));
@@ -780,7 +787,7 @@ static void fused_batch(int nmol, const int* natoms, const int* atno, const doub
                 rc[m] = r0;
                 err[m] = hfgpu_last_error();
             }
-            continue;
+            return;
         }
         wctx->tune = (opt && opt->autotune != 0) || tune_env_enabled();
         {
@@ -812,5 +819,17 @@ static void fused_batch(int nmol, const int* natoms, const int* atno, const doub
             for (auto& t : th) t.join();
         }
         context_release(wctx);
+    };
+    std::atomic<size_t> next{0};
+    auto wave_worker = [&]() {
+        for (size_t w; (w = next.fetch_add(1)) < waves.size();) run_wave(waves[w]);
+    };
+    const int nthreads = (int)std::min<size_t>(WAVES_IN_FLIGHT, waves.size());
+    if (nthreads <= 1) {
+        wave_worker();
+    } else {
+        std::vector<std::thread> wt;
+        for (int t = 0; t < nthreads; ++t) wt.emplace_back(wave_worker);
+        for (auto& t : wt) t.join();
     }
 }
