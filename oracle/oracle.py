@@ -87,6 +87,8 @@ def _bind(L, prefix="oracle_"):
         L.oracle_formG_scatter.restype = None
         L.oracle_getInts_screened.argtypes = basis_args + [ctypes.c_double, _dp, _dp]
         L.oracle_getInts_screened.restype = None
+        L.oracle_unpack_mu.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _dp]
+        L.oracle_unpack_mu.restype = None
 
 
 def _d(a):
@@ -503,20 +505,20 @@ def find_pole_diag(i, moint2, lam, nocc, nscf, tolE):
 
 
 def mp2_semidirect(int2, C, lam, nocc, block=None):
-    """The same E2 as mbpt2(transform_int2(...)), built from (ia|jb) only, in
-    blocks of mu so that no n^4 tensor is formed (for n beyond 120)."""
+    """The same E2 as mbpt2(transform_int2(...)), built from (ia|jb) only, one mu
+    at a time (unpacked in C), so that no n^4 tensor is formed (for n beyond
+    120).  block is accepted for compatibility and ignored."""
     n = C.shape[0]
-    if block is None:
-        block = max(1, min(8, int(1.0e8 // n ** 3)))
-    Co, Cv = C[:, :nocc], C[:, nocc:]
+    Co, Cv = np.ascontiguousarray(C[:, :nocc]), np.ascontiguousarray(C[:, nocc:])
     iajb = np.zeros((nocc, n - nocc, nocc, n - nocc))
-    i = np.arange(n)
-    for m0 in range(0, n, block):
-        mu = np.arange(m0, min(n, m0 + block))
-        X = int2[ijkl(mu[:, None, None, None], i[None, :, None, None], i[None, None, :, None],
-                      i[None, None, None, :])]
-        X = np.einsum("mnls,lj,sb->mnjb", X, Co, Cv, optimize=True)
-        iajb += np.einsum("mnjb,mi,na->iajb", X, Co[mu], Cv, optimize=True)
+    X = np.empty((n, n, n))
+    L = lib()
+    for mu in range(n):
+        L.oracle_unpack_mu(n, _d(int2), mu, _d(X))
+        # (mu nu | j b) then (mu a | j b), accumulated into (i a | j b)
+        Y = np.tensordot(np.tensordot(X, Co, axes=([1], [0])), Cv, axes=([1], [0]))  # [nu][j][b]
+        Z = np.tensordot(Cv, Y, axes=([0], [0]))  # [a][j][b]
+        iajb += Co[mu][:, None, None, None] * Z[None]
     e_o, e_v = lam[:nocc], lam[nocc:]
     den = e_o[:, None, None, None] - e_v[None, :, None, None] + e_o[None, None, :, None] \
         - e_v[None, None, None, :]

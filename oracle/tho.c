@@ -208,6 +208,18 @@ void oracle_getInts_screened(int nbf, const int *nprim, const int *istart, const
         }
 }
 
+/* out[(nu * n + la) * n + si] = (mu nu|la si) for one mu, from the packed
+ * integrals (the semi-direct MP2 of the oracle fixtures unpacks one mu at a
+ * time). */
+void oracle_unpack_mu(int n, const double *int2, int mu, double *out)
+{
+#pragma omp parallel for schedule(static)
+    for (int nu = 0; nu < n; nu++)
+        for (int la = 0; la < n; la++)
+            for (int si = 0; si < n; si++)
+                out[((int64_t)nu * n + la) * n + si] = int2[oracle_ijkl(mu, nu, la, si)];
+}
+
 /* contracted ERIs for an explicit list of function quartets q[4*t..4*t+3] */
 void oracle_eri_list(int nbf, const int *nprim, const int *istart, const double *xc,
                      const double *yc, const double *zc, const int *lp, const int *mp,
