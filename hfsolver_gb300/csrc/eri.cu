@@ -201,6 +201,7 @@ static void launch_class(Context& ctx, EriPlan* P, ClassPlan& c, int mode, doubl
     if (c.nwarps == 0) return;
     EriArgs a;
     a.blocks = blocks;
+    a.qlist = (blocks && mode == MODE_PACKED && P->qlist.p) ? P->qlist.p + c.qbase : nullptr;
     a.nq_class = c.nq;
     a.mol_out = mode == MODE_PACKED ? P->mol_out.p : nullptr;
     a.sh = P->shdev();
@@ -581,6 +582,8 @@ void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG, double s
         a.mol_Dm = nullptr;
         a.mol_ns = nullptr;
         a.mol_sh0 = nullptr;
+        a.qlist = P->qlist.p ? P->qlist.p + c.qbase : nullptr;
+        a.pair_mol = nullptr;
         a.split = digest_split_tuned(ctx, c, a, nn);
         cudaStream_t s = ctx.aux[slot++ % Context::NAUX];
         launch_digest(c, a, s);
@@ -660,12 +663,15 @@ void eri_compute(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks, EriS
     P->stats.n_block_elems = 0;
     for (auto& c : P->classes) P->stats.n_block_elems += c.nq * block_size(c.tb, c.tk);
     if (keep_blocks) {
-        int64_t total = 0;
+        int64_t total = 0, nqt = 0;
         for (auto& c : P->classes) {
             c.boff = total;
             total += c.nq * block_size(c.tb, c.tk);
+            c.qbase = nqt;
+            nqt += c.nq;
         }
         P->blocks.alloc(std::max<int64_t>(total, 1), ctx.stream);
+        P->qlist.alloc(std::max<int64_t>(nqt, 1), ctx.stream);
     }
     cudaEvent_t e0, e1;
     HF_CUDA(cudaEventCreate(&e0));
@@ -755,6 +761,12 @@ EriPlan* eri_plan_merge(Context& ctx, const std::vector<EriPlan*>& plans)
         M->dA = to_device(M->pA, st); M->dB = to_device(M->pB, st); M->dK = to_device(M->pK, st);
         M->doff = to_device(M->poff, st);
         M->dQ = to_device(M->Q, st);
+        {
+            std::vector<int> pm;
+            pm.reserve(pair0);
+            for (size_t m = 0; m < plans.size(); ++m) pm.insert(pm.end(), plans[m]->npair, (int)m);
+            M->pair_mol = to_device(pm, st);
+        }
         M->gpairs = to_device(M->h_gpairs, st);
         M->prefix = to_device(M->h_prefix, st);
         M->pdata.alloc(std::max<int64_t>(off, 1), st);
@@ -934,6 +946,8 @@ static void batch_digest_launches(Context& ctx, EriPlan* P, BatchDigest& t, cuda
         a.mol_Dm = t.mol_Dm.p;
         a.mol_ns = t.mol_ns.p;
         a.mol_sh0 = t.mol_sh0.p;
+        a.qlist = P->qlist.p ? P->qlist.p + c.qbase : nullptr;
+        a.pair_mol = P->pair_mol.p;
         int split = digest_split(c);
         if (ctx.tune) tune_get(TUNE_DIGEST, c.tb, c.tk, tune_bucket(c.nq), &split);
         a.split = split;

@@ -59,6 +59,7 @@ struct EriArgs {
     double* blocks;  // class-wise quartet blocks [element][quartet] (may be null)
     int64_t nq_class;
     const int64_t* mol_out;  // batched plans: offset of each molecule's packed array in out (else null)
+    int2* qlist;             // with blocks: the (bra, ket) pair ids of each quartet of the class (else null)
 };
 
 using KernelFn = void (*)(EriArgs);
@@ -125,6 +126,7 @@ __device__ __forceinline__ void run_chunk(const EriArgs& a, double* out, int bra
             out[(int64_t)ket * 36 + icd] = acc[icd * CI::NCD + s];
         }
     } else {
+        if (a.qlist && CH == 0) a.qlist[qg] = make_int2(bra, ket);
         if (a.blocks) {  // the whole block, one element plane per component quartet (coalesced in q)
 #pragma unroll
             for (int s = 0; s < CI::NCD; ++s)

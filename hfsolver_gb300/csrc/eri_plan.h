@@ -17,6 +17,7 @@ struct ClassPlan {
     int64_t nwarps = 0;
     int64_t nq = 0;     // quartets of the class
     int64_t boff = 0;   // offset of the class's blocks in EriPlan::blocks
+    int64_t qbase = 0;  // offset of the class's quartets in EriPlan::qlist
     DBuf<Seg> dsegs;
 };
 
@@ -39,6 +40,8 @@ struct EriPlan {
     DBuf<int64_t> prefix;
     std::vector<ClassPlan> classes;
     DBuf<double> blocks;  // class-wise quartet blocks, kept for the SCF's Fock builds
+    DBuf<int2> qlist;     // (bra, ket) pair ids of every kept quartet, class by class
+    DBuf<int> pair_mol;   // batched plans: the molecule of every pair
     EriStats stats;
     // host copies of the grouped pair ids and prefix sums (for merging plans)
     std::vector<int> h_gpairs;

@@ -49,6 +49,11 @@ struct DigestArgs {
     const double* const* mol_Dm;
     const int* mol_ns;
     const int* mol_sh0;
+    // the (bra, ket) pair ids of every quartet of the class, written by the ERI
+    // pass (null: found by searching the segments), and in batched plans the
+    // molecule of every pair
+    const int2* qlist;
+    const int* pair_mol;
 };
 
 // the per-molecule view of a batched build (the arguments themselves for one molecule)
@@ -77,6 +82,42 @@ __device__ __forceinline__ bool digest_mol(const DigestArgs& a, int mol, DigestM
     return true;
 }
 
+// quartet qg of the class: its bra and ket pair ids and its molecule, from the
+// list the ERI pass wrote, else by searching the segments and prefix sums
+__device__ __forceinline__ void digest_quartet(const DigestArgs& a, int64_t qg, int& bra, int& ket, int& mol)
+{
+    if (a.qlist) {
+        const int2 e = __ldg(a.qlist + qg);
+        bra = e.x;
+        ket = e.y;
+        mol = a.pair_mol ? __ldg(a.pair_mol + bra) : 0;
+        return;
+    }
+    const int qg32 = (int)qg;
+    int lo = 0, hi = a.nseg - 1;  // last segment with qoff <= qg
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((int)(a.segs[mid].qoff) <= qg32) lo = mid; else hi = mid - 1;
+    }
+    const Seg sg = a.segs[lo];
+    const int q = qg32 - (int)sg.qoff;  // class quartet counts stay below 2^31 (plan check)
+    mol = sg.mol;
+    if (sg.list) {
+        const int2 e = a.list[sg.pref0 + q];
+        bra = e.x;
+        ket = e.y;
+        return;
+    }
+    const int64_t* pf = a.prefix + sg.pref0;
+    int l2 = 0, h2 = sg.nbra - 1;
+    while (l2 < h2) {
+        const int mid = (l2 + h2 + 1) >> 1;
+        if ((int)pf[mid] <= q) l2 = mid; else h2 = mid - 1;
+    }
+    bra = a.gpairs[sg.bra0 + l2];
+    ket = a.gpairs[sg.ket0 + (q - (int)pf[l2])];
+}
+
 // true if the quartet's whole contribution is below the screening threshold:
 // |(ab|cd)| <= Q_bra Q_ket, and the largest density factor it meets is
 // 2|P_ab|, 2|P_cd| (Coulomb) or |P_ac|/2 ... (exchange)
@@ -99,31 +140,10 @@ __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
     constexpr int NA = ncart(CI::LA), NB = ncart(CI::LB), NC = ncart(CI::LC), ND = ncart(CI::LD);
     const int64_t qg = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (qg >= a.nq) return;
-    const int qg32 = (int)qg;
-    int lo = 0, hi = a.nseg - 1;  // last segment with qoff <= qg
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if ((int)(a.segs[mid].qoff) <= qg32) lo = mid; else hi = mid - 1;
-    }
-    const Seg sg = a.segs[lo];
-    const int q = qg32 - (int)sg.qoff;  // class quartet counts stay below 2^31 (plan check)
-    int bra, ket;
-    if (sg.list) {
-        const int2 e = a.list[sg.pref0 + q];
-        bra = e.x;
-        ket = e.y;
-    } else {
-        const int64_t* pf = a.prefix + sg.pref0;
-        int l2 = 0, h2 = sg.nbra - 1;
-        while (l2 < h2) {
-            const int mid = (l2 + h2 + 1) >> 1;
-            if ((int)pf[mid] <= q) l2 = mid; else h2 = mid - 1;
-        }
-        bra = a.gpairs[sg.bra0 + l2];
-        ket = a.gpairs[sg.ket0 + (q - (int)pf[l2])];
-    }
+    int bra, ket, mol;
+    digest_quartet(a, qg, bra, ket, mol);
     DigestMol mm;
-    if (!digest_mol(a, sg.mol, mm)) return;
+    if (!digest_mol(a, mol, mm)) return;
     const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
     if (digest_skip(a, mm, bra, ket, A, B, C, D)) return;
     int fa[NA], fb[NB], fc[NC], fd[ND];
@@ -244,27 +264,10 @@ __global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
     const unsigned mask = split == 32 ? 0xffffffffu : (((1u << split) - 1u) << (lane & ~(unsigned)(split - 1)));
     const int64_t qg = tid / split;
     if (qg >= a.nq) return;  // all lanes of a quartet leave together
-    const int qg32 = (int)qg;
-    int lo = 0, hi = a.nseg - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if ((int)(a.segs[mid].qoff) <= qg32) lo = mid; else hi = mid - 1;
-    }
-    const Seg sg = a.segs[lo];
-    const int q = qg32 - (int)sg.qoff;  // class quartet counts stay below 2^31 (plan check)
-    int bra, ket;
-    {
-        const int64_t* pf = a.prefix + sg.pref0;
-        int l2 = 0, h2 = sg.nbra - 1;
-        while (l2 < h2) {
-            const int mid = (l2 + h2 + 1) >> 1;
-            if ((int)pf[mid] <= q) l2 = mid; else h2 = mid - 1;
-        }
-        bra = a.gpairs[sg.bra0 + l2];
-        ket = a.gpairs[sg.ket0 + (q - (int)pf[l2])];
-    }
+    int bra, ket, mol;
+    digest_quartet(a, qg, bra, ket, mol);
     DigestMol mm;
-    if (!digest_mol(a, sg.mol, mm)) return;  // same answer for all lanes of the quartet
+    if (!digest_mol(a, mol, mm)) return;  // same answer for all lanes of the quartet
     const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
     if (digest_skip(a, mm, bra, ket, A, B, C, D)) return;  // same answer for all lanes of the quartet
     int fc[NC], fd[ND];
