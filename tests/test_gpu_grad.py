@@ -58,14 +58,19 @@ def test_water_gradient_energy_matches_rhf():
     assert r["ms_grad"] > 0
 
 
-@pytest.mark.parametrize("nw,ncoord", [(2, 18), (4, 6), (8, 4), (12, 2)])
+@pytest.mark.parametrize("nw,ncoord", [(2, 18), (4, 9), (8, 12), (12, 9)])
 def test_cluster_gradient_vs_fd(nw, ncoord):
+    """Every coordinate of one water of the cluster (its three atoms), plus
+    randomly chosen coordinates of the others up to ncoord."""
     atno, xyz = water_cluster(nw, seed=1)
     opt = hf.RHFOptions(schwarz=1e-12, **OPT)
     _, g = hf.rhf_gradient(atno, xyz, opt)
     rng = np.random.default_rng(nw)
-    cand = [(a, k) for a in range(len(atno)) for k in range(3)]
-    coords = [cand[i] for i in rng.choice(len(cand), size=min(ncoord, len(cand)), replace=False)]
+    w = nw // 2
+    coords = [(3 * w + a, k) for a in range(3) for k in range(3)]
+    rest = [(a, k) for a in range(len(atno)) for k in range(3) if (a, k) not in coords]
+    extra = max(0, min(ncoord, len(atno) * 3) - len(coords))
+    coords += [rest[i] for i in rng.choice(len(rest), size=extra, replace=False)]
 
     def e_gpu(x):
         return hf.rhf(atno, x, opt)["Etot"]
