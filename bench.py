@@ -340,6 +340,17 @@ def run_gpu(args):
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         cpu, _ = cpu_sample(atno, xyz, r["niter"], serial=True)
+    batch = None
+    if world == 1 and not args.no_batch and not args.no_cpu_baseline:
+        # the batch workload beside the headline: 256 seeded clusters of 1-12 waters,
+        # fused waves against the same molecules one at a time (mixed: all; plain
+        # FP64: every 8th)
+        from hfsolver_gb300.clusters import water_batch
+
+        bopt = options("split_bf16")
+        bopt.batch_streams = 32
+        batch, _, _ = measure_batch(water_batch(256, seed=0), bopt, 1, 1, 8)
+        batch["workload"] = "water_batch256_1to12_jitter0.05A_631gss_rhf_diis_schwarz1e-12_mp2, fused waves of 32"
     ro = res_o[-1]
     mixed = r if main_mp2 == "split_bf16" else ro
     plain = ro if main_mp2 == "split_bf16" else r
@@ -378,8 +389,73 @@ def run_gpu(args):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if batch is not None:
+        line["batch"] = batch
     print(json.dumps(line))
     return 0
+
+
+def measure_batch(mols, opt, steps, warmup, plain_every=4, clocks=None, barrier=None):
+    """The batch workload's three throughputs on the same molecules: batched
+    through hfgpu_rhf_batch (opt), all of them one at a time through the mixed
+    path, every plain_every-th one at a time through plain FP64; energies
+    compared with each other and with the oracle fixtures of this batch."""
+    import torch
+
+    import hfsolver_gb300 as hf
+
+    # warm-up passes over the whole batch: the autotuner meets every (class, size)
+    # it will see, so no tuning runs inside the timed region
+    for _ in range(warmup):
+        hf.rhf_batch(mols, opt)
+    if clocks:
+        clocks.start()
+    if barrier:
+        barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = []
+    for _ in range(steps):
+        res = hf.rhf_batch(mols, opt)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop() if clocks else None
+    sub = list(range(0, len(mols), plain_every))
+    single = options("split_bf16")
+    plain = options("fp64")
+    hf.rhf(mols[0][0], mols[0][1], single)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    one_mixed = [hf.rhf(a, x, single) for a, x in mols]
+    torch.cuda.synchronize()
+    wall_mixed = time.perf_counter() - t1
+    t2 = time.perf_counter()
+    one_plain = [hf.rhf(mols[i][0], mols[i][1], plain) for i in sub]
+    torch.cuda.synchronize()
+    wall_plain = time.perf_counter() - t2
+    nbf = [r["nbf"] for r in res]
+    oracle = None
+    try:
+        fx = json.load(open(os.path.join(ROOT, "tests", "golden", "water_clusters.json"))).get("batch")
+    except (OSError, ValueError):
+        fx = None
+    if fx and fx["count"] == len(mols) and all(len(mols[m["index"]][0]) == 3 * m["n_waters"] for m in fx["molecules"]):
+        oracle = {"molecules": [m["index"] for m in fx["molecules"]],
+                  "max_dEtot": max(abs(res[m["index"]]["Etot"] - m["Etot"]) for m in fx["molecules"]),
+                  "max_dE2": max(abs(res[m["index"]]["E2"] - m["E2"]) for m in fx["molecules"])}
+    rec = {"molecules": len(mols), "nbf_min": min(nbf), "nbf_max": max(nbf), "nbf_mean": float(np.mean(nbf)),
+           "mixed_batched_molecules_per_s": steps * len(mols) / wall,
+           "mixed_one_at_a_time_molecules_per_s": len(mols) / wall_mixed,
+           "plain_fp64_one_at_a_time_molecules_per_s": len(sub) / wall_plain,
+           "plain_fp64_sample": f"every {plain_every}th molecule ({len(sub)}, mean "
+                                f"{np.mean([nbf[i] for i in sub]):.1f} functions against {np.mean(nbf):.1f} for all)",
+           "max_dE2_batched_vs_one_at_a_time_mixed": max(abs(a["E2"] - b["E2"]) for a, b in zip(res, one_mixed)),
+           "vs_gpu_fp64": {"max_dE2": max(abs(res[i]["E2"] - r["E2"]) for i, r in zip(sub, one_plain)),
+                           "max_dEtot": max(abs(res[i]["Etot"] - r["Etot"]) for i, r in zip(sub, one_plain))},
+           "vs_oracle_fixtures": oracle,
+           "failed": sum(1 for r in res if r["niter"] <= 0),
+           "timing": "host wall clock between device-wide synchronizes"}
+    return rec, (wall, wall_mixed, wall_plain), clk
 
 
 def run_batch(args):
@@ -405,80 +481,29 @@ def run_batch(args):
     opt = options("split_bf16")
     opt.batch_streams = args.streams
     opt.batch_fused = not args.batch_streams_mode
-    opt.autotune = True  # quartet-tile shapes timed on the first molecules of each size, then reused
-    # warm-up passes over the whole batch: the autotuner meets every (class, size)
-    # it will see, so no tuning runs inside the timed region
-    for _ in range(args.warmup):
-        hf.rhf_batch(mols, opt)
-    clocks = ClockSampler(local)
-    clocks.start()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    res = []
-    for _ in range(args.steps):
-        res = hf.rhf_batch(mols, opt)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    clk = clocks.stop()
-    # the same molecules one at a time: all of them through the mixed path, every
-    # 4th through the plain FP64 path
-    sub = list(range(0, len(mols), 4))
-    single = options("split_bf16")
-    plain = options("fp64")
-    hf.rhf(mols[0][0], mols[0][1], single)
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    one_mixed = [hf.rhf(a, x, single) for a, x in mols]
-    torch.cuda.synchronize()
-    wall_mixed = time.perf_counter() - t1
-    t2 = time.perf_counter()
-    one_plain = [hf.rhf(mols[i][0], mols[i][1], plain) for i in sub]
-    torch.cuda.synchronize()
-    wall_plain = time.perf_counter() - t2
+    barrier = (lambda: torch.distributed.barrier()) if world > 1 else None
+    rec, walls, clk = measure_batch(mols, opt, args.steps, args.warmup, 4, ClockSampler(local), barrier)
+    wall, wall_mixed, wall_plain = walls
     if world > 1:
         wall, wall_mixed, wall_plain = max_over_ranks([wall, wall_mixed, wall_plain])
     if rank != 0:
         return 0
-    failed = sum(1 for r in res if r["niter"] <= 0)
-    dE2 = max(abs(res[i]["E2"] - r["E2"]) for i, r in zip(sub, one_plain))
-    dEt = max(abs(res[i]["Etot"] - r["Etot"]) for i, r in zip(sub, one_plain))
-    # against the oracle fixtures of the batch workload (rank 0's molecules)
-    oracle = {}
-    try:
-        fx = json.load(open(os.path.join(ROOT, "tests", "golden", "water_clusters.json"))).get("batch")
-    except (OSError, ValueError):
-        fx = None
-    if fx and fx["count"] == len(mols) and fx["seed"] == rank:
-        d_hf = [abs(res[m["index"]]["Etot"] - m["Etot"]) for m in fx["molecules"]]
-        d_e2 = [abs(res[m["index"]]["E2"] - m["E2"]) for m in fx["molecules"]]
-        oracle = {"molecules": [m["index"] for m in fx["molecules"]], "max_dEtot": max(d_hf), "max_dE2": max(d_e2)}
-    nbf = [r["nbf"] for r in res]
     value = world * args.steps * len(mols) / wall
+    rec["mixed_batched_molecules_per_s"] = value
     line = {
         "metric": METRIC + " (batched)", "value": value, "unit": "molecules/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"water_batch{len(mols)}_1to12_jitter0.05A_631gss_rhf_diis_schwarz1e-12_mp2",
-                   "molecules": len(mols), "nbf_min": min(nbf), "nbf_max": max(nbf), "nbf_mean": float(np.mean(nbf)),
                    "mp2": "split_bf16",
                    "batch": ("molecules of a wave share one ERI launch and one Fock-build launch per quartet class "
                              "per SCF iteration (replayed CUDA graph)" if opt.batch_fused else
                              "each molecule on its own streams"),
                    "molecules_per_wave" if opt.batch_fused else "molecules_in_flight": args.streams,
                    "autotuned_shapes": len(hf.autotune_table()),
-                   "timing": "host wall clock between device-wide synchronizes",
                    "parallelism": f"replicas x{world}"},
-        "batch": {"mixed_batched_molecules_per_s": value,
-                  "mixed_one_at_a_time_molecules_per_s": len(mols) / wall_mixed,
-                  "plain_fp64_one_at_a_time_molecules_per_s": len(sub) / wall_plain,
-                  "plain_fp64_sample": f"every 4th molecule ({len(sub)}, mean {np.mean([nbf[i] for i in sub]):.1f} "
-                                       f"functions against {np.mean(nbf):.1f} for all)",
-                  "max_dE2_batched_vs_one_at_a_time_mixed": max(abs(a["E2"] - b["E2"]) for a, b in zip(res, one_mixed)),
-                  "vs_gpu_fp64": {"max_dE2": dE2, "max_dEtot": dEt},
-                  "vs_oracle_fixtures": oracle or None},
-        "failed": failed,
+        "batch": rec,
+        "failed": rec["failed"],
         "clocks": clk,
     }
     print(json.dumps(line))
@@ -530,6 +555,9 @@ def main():
                     help="cluster size (8: 200 functions, the headline workload; 16: 400 functions)")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the CPU-baseline sample (profiling runs)")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batch-workload record of the default run (256 molecules; "
+                         "--no-cpu-baseline skips it too)")
     ap.add_argument("--batch", type=int, default=0,
                     help="batched mode: this many water clusters of 1-12 waters per step")
     ap.add_argument("--streams", type=int, default=32,
