@@ -105,6 +105,7 @@ void BatchWave::run_digest_locked()
         cudaStream_t st = ctx_->stream;
         // the tables of the previous build must have been copied before they change
         HF_CUDA(cudaEventSynchronize(done_));
+        tables_.wait_tables();
         for (int m = 0; m < nmol_; ++m) {
             const int s = slot_[m];
             if (s < 0) continue;

@@ -435,6 +435,10 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
             }
         P->prefix = to_device(prefix, st);
         P->h_prefix = prefix;
+        P->nmol = 1;
+        P->mol_nbf = {b.nbf};
+        P->mol_ns = {ns};
+        P->mol_sh0 = {0};
         P->stats = stt;
         HF_CUDA(cudaStreamSynchronize(st));
         ctx.trace_mark("plan classes");
@@ -889,6 +893,7 @@ void BatchDigest::setup(Context& ctx, const EriPlan* P, cudaStream_t s)
     mol_P.alloc(nmol, s);
     mol_G.alloc(nmol, s);
     mol_screen.alloc(nmol, s);
+    HF_CUDA(cudaEventCreateWithFlags(&copied, cudaEventDisableTiming));
     HF_CUDA(cudaMallocHost((void**)&h_P, nmol * sizeof(const double*)));
     HF_CUDA(cudaMallocHost((void**)&h_G, nmol * sizeof(double*)));
     HF_CUDA(cudaMallocHost((void**)&h_screen, nmol * sizeof(double)));
@@ -899,8 +904,14 @@ void BatchDigest::setup(Context& ctx, const EriPlan* P, cudaStream_t s)
     }
 }
 
+void BatchDigest::wait_tables()
+{
+    if (copied) HF_CUDA(cudaEventSynchronize(copied));
+}
+
 BatchDigest::~BatchDigest()
 {
+    if (copied) cudaEventDestroy(copied);
     if (exec) cudaGraphExecDestroy(exec);
     if (h_P) cudaFreeHost((void*)h_P);
     if (h_G) cudaFreeHost(h_G);
@@ -919,6 +930,11 @@ static void batch_digest_launches(Context& ctx, EriPlan* P, BatchDigest& t, cuda
                                         t.mol_sh0.p, t.mol_P.p, t.mol_screen.p, t.Dm.p);
     count_launch();
     HF_CUDA(cudaGetLastError());
+    // the classes are independent until the symmetrisation: spread over the side
+    // streams (inside a capture these become parallel branches of the graph)
+    HF_CUDA(cudaEventRecord(ctx.fork_ev, s));
+    for (int i = 0; i < Context::NAUX; ++i) HF_CUDA(cudaStreamWaitEvent(ctx.aux[i], ctx.fork_ev, 0));
+    int slot = 0;
     for (int ci = (int)P->classes.size() - 1; ci >= 0; --ci) {
         auto& c = P->classes[ci];
         if (c.nq == 0) continue;
@@ -951,7 +967,11 @@ static void batch_digest_launches(Context& ctx, EriPlan* P, BatchDigest& t, cuda
         int split = digest_split(c);
         if (ctx.tune) tune_get(TUNE_DIGEST, c.tb, c.tk, tune_bucket(c.nq), &split);
         a.split = split;
-        launch_digest(c, a, s);
+        launch_digest(c, a, ctx.aux[slot++ % Context::NAUX]);
+    }
+    for (int i = 0; i < Context::NAUX; ++i) {
+        HF_CUDA(cudaEventRecord(ctx.join_ev[i], ctx.aux[i]));
+        HF_CUDA(cudaStreamWaitEvent(s, ctx.join_ev[i], 0));
     }
     const unsigned gs = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nn_total + 255) / 256, ctx.num_sms * 8));
     batch_sym_kernel<<<gs, 256, 0, s>>>(t.nmol, t.nn_prefix.p, t.mol_n.p, t.Gh.p, t.mol_G.p, t.mol_screen.p);
@@ -966,6 +986,7 @@ void eri_digest_batch(Context& ctx, EriPlan* P, BatchDigest& t, cudaStream_t s)
     HF_CUDA(cudaMemcpyAsync(t.mol_P.p, t.h_P, t.nmol * sizeof(const double*), cudaMemcpyHostToDevice, s));
     HF_CUDA(cudaMemcpyAsync(t.mol_G.p, t.h_G, t.nmol * sizeof(double*), cudaMemcpyHostToDevice, s));
     HF_CUDA(cudaMemcpyAsync(t.mol_screen.p, t.h_screen, t.nmol * sizeof(double), cudaMemcpyHostToDevice, s));
+    HF_CUDA(cudaEventRecord(t.copied, s));
     if (!t.exec) {
         // the launches of a build are the same every iteration: captured once into a
         // CUDA graph and replayed (the tables above are read from device memory)
@@ -988,6 +1009,36 @@ void eri_digest_batch(Context& ctx, EriPlan* P, BatchDigest& t, cudaStream_t s)
     }
     HF_CUDA(cudaGraphLaunch(t.exec, s));
     count_launch((int)t.graph_kernels);
+}
+
+// One molecule's Fock build through the same captured launches as a batch of one
+// (eri_digest_batch): the graph replaces the build's ~23 launches per SCF iteration.
+void eri_digest_graph(Context& ctx, EriPlan* P, const double* dP, double* dG, double screen)
+{
+    HF_CHECK(P->blocks.p != nullptr && P->nmol == 1, HFGPU_ERR_INVALID, "eri_digest_graph: integrals were not kept");
+    if (!P->solo && ctx.tune) {
+        // the first build runs the launches themselves, so that the autotuner can time
+        // its candidate shapes; the graph is captured at the next build
+        P->solo.reset(new BatchDigest());
+        eri_digest(ctx, P, dP, dG, screen);
+        return;
+    }
+    if (!P->solo || P->solo->nmol == 0) {
+        if (!P->solo) P->solo.reset(new BatchDigest());
+        P->solo->setup(ctx, P, ctx.stream);
+    }
+    BatchDigest& t = *P->solo;
+    t.wait_tables();  // the previous build's table copies have left the host buffers
+    t.h_P[0] = dP;
+    t.h_G[0] = dG;
+    t.h_screen[0] = screen > 0 ? screen : 0.0;
+    cudaEvent_t e0, e1;
+    HF_CUDA(cudaEventCreate(&e0));
+    HF_CUDA(cudaEventCreate(&e1));
+    HF_CUDA(cudaEventRecord(e0, ctx.stream));
+    eri_digest_batch(ctx, P, t, ctx.stream);
+    HF_CUDA(cudaEventRecord(e1, ctx.stream));
+    ctx.fock_events.push_back({e0, e1, screen <= 0});  // timed later, without a host wait here
 }
 
 }  // namespace hfgpu

@@ -2,6 +2,7 @@
 // primitive-pair records, Schwarz bounds and the screened quartet segments of
 // every class.  Shared by the ERI, Fock-digest and gradient translation units.
 #pragma once
+#include <memory>
 #include <vector>
 
 #include "eri_kernel.cuh"
@@ -52,6 +53,8 @@ struct EriPlan {
     int nmol = 1;
     std::vector<int> mol_nbf, mol_ns, mol_sh0;
     DBuf<int64_t> mol_out;
+    // the one-molecule Fock build's tables and captured graph (eri_digest_graph)
+    std::unique_ptr<BatchDigest> solo;
     ShellDev shdev() const
     {
         return ShellDev{sL.p, snp.p, sxyz.p, sp0.p, sc0.p, scf.p, alpha.p, coef.p, cfn.p};

@@ -25,7 +25,7 @@
 // with R, H and the six density blocks of the quartet in shared memory.  The
 // quartets are those the energy path evaluated (same Schwarz screening).
 //
-// One-electron part: one thread per basis-function pair; dS/dA and dT/dA from
+// One-electron part: one thread per basis-function pair and pair of nuclei; dS/dA and dT/dA from
 // shifted 1-D overlaps (dB = -dA for two-centre integrals), dV from the shifted
 // Hermite sums with the Hellmann-Feynman term of each nucleus C obtained by
 // translational invariance, dV/dC = -(dV/dA + dV/dB).
@@ -507,6 +507,11 @@ __device__ static void e1d_oe(double* E, int imax, int jmax, double xpa, double 
             }
 }
 
+// nuclei per block row: the grid's second dimension splits the nuclear-attraction
+// loop, so that a function pair's nuclei run in parallel (row 0 also does the
+// overlap and kinetic terms)
+constexpr int ONEE_GRAD_NUCLEI = 2;
+
 __global__ void onee_grad_kernel(OneArgs o)
 {
     const double PI = 3.14159265358979323846;
@@ -556,7 +561,7 @@ __global__ void onee_grad_kernel(OneArgs o)
                                 lb[2] * (lb[2] - 1) * sx * sy * s1(2, q[2], lb[2] - 2);
                     t = t0 + t1 - 0.5 * t2;
                 };
-                for (int k = 0; k < 3; ++k) {
+                for (int k = 0; k < 3 && blockIdx.y == 0; ++k) {
                     int up[3] = {la[0], la[1], la[2]}, dn[3] = {la[0], la[1], la[2]};
                     up[k] += 1;
                     dn[k] -= 1;
@@ -572,7 +577,8 @@ __global__ void onee_grad_kernel(OneArgs o)
                 // nuclear attraction
                 const int L = la[0] + la[1] + la[2] + lb[0] + lb[1] + lb[2] + 1;
                 const double vpre = wP * cc * K * 2 * PI * ip;
-                for (int c = 0; c < o.nat; ++c) {
+                const int c_end = min(o.nat, (int)(blockIdx.y + 1) * ONEE_GRAD_NUCLEI);
+                for (int c = blockIdx.y * ONEE_GRAD_NUCLEI; c < c_end; ++c) {
                     const double X = Pc[0] - o.C[3 * c], Y = Pc[1] - o.C[3 * c + 1], Zc = Pc[2] - o.C[3 * c + 2];
                     double F[OG_L + 1];
                     boys_rt(L, p * (X * X + Y * Y + Zc * Zc), 1.0, -2.0 * p, o.boys, F);
@@ -800,7 +806,8 @@ void onee_gradient(Context& ctx, const Basis& b, int nat, const int* atno, const
     const int64_t npair = (int64_t)n * (n + 1) / 2;
     const size_t smem = (size_t)3 * nat * sizeof(double);
     HF_CHECK(smem <= 48 * 1024, HFGPU_ERR_UNSUPPORTED, "too many atoms for the one-electron gradient kernel");
-    onee_grad_kernel<<<(unsigned)((npair + 127) / 128), 128, smem, st>>>(o);
+    const dim3 grid((unsigned)((npair + 127) / 128), (unsigned)((nat + ONEE_GRAD_NUCLEI - 1) / ONEE_GRAD_NUCLEI));
+    onee_grad_kernel<<<grid, 128, smem, st>>>(o);
     count_launch();
     HF_CUDA(cudaGetLastError());
     HF_CUDA(cudaStreamSynchronize(st));

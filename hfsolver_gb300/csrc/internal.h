@@ -265,9 +265,14 @@ struct BatchDigest {
     double* h_screen = nullptr;
     cudaGraphExec_t exec = nullptr;      // the build's launches, captured on first use
     int64_t graph_kernels = 0;
+    cudaEvent_t copied = nullptr;        // recorded after each build's table copies
     void setup(Context& ctx, const EriPlan* P, cudaStream_t s);
+    void wait_tables();                  // host tables free to be rewritten
     ~BatchDigest();
 };
+// one molecule's Fock build (G = J - K/2 of dP into dG) as the replayed graph of a
+// batch of one; screen > 0 screens a density difference
+void eri_digest_graph(Context& ctx, EriPlan* P, const double* dP, double* dG, double screen);
 // one Fock build (G = J - K/2) for every molecule with h_screen >= 0, on stream s
 void eri_digest_batch(Context& ctx, EriPlan* P, BatchDigest& t, cudaStream_t s);
 // kernels counted so far (context.cu)
