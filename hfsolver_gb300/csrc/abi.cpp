@@ -197,7 +197,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         in.purify = opt.purify != 0;
         in.eigensolver = opt.eigensolver;
         in.direct_jk = [](Context& c, void* user, const double* P, double* G, double screen) {
-            eri_digest_graph(c, (EriPlan*)user, P, G, screen);
+            eri_digest(c, (EriPlan*)user, P, G, screen);
         };
         // density-difference builds skip quartets whose bounded contribution is below
         // 1e-10 (or the Schwarz threshold, if larger); the full builds of the last

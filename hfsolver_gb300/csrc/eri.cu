@@ -1011,34 +1011,4 @@ void eri_digest_batch(Context& ctx, EriPlan* P, BatchDigest& t, cudaStream_t s)
     count_launch((int)t.graph_kernels);
 }
 
-// One molecule's Fock build through the same captured launches as a batch of one
-// (eri_digest_batch): the graph replaces the build's ~23 launches per SCF iteration.
-void eri_digest_graph(Context& ctx, EriPlan* P, const double* dP, double* dG, double screen)
-{
-    HF_CHECK(P->blocks.p != nullptr && P->nmol == 1, HFGPU_ERR_INVALID, "eri_digest_graph: integrals were not kept");
-    if (!P->solo && ctx.tune) {
-        // the first build runs the launches themselves, so that the autotuner can time
-        // its candidate shapes; the graph is captured at the next build
-        P->solo.reset(new BatchDigest());
-        eri_digest(ctx, P, dP, dG, screen);
-        return;
-    }
-    if (!P->solo || P->solo->nmol == 0) {
-        if (!P->solo) P->solo.reset(new BatchDigest());
-        P->solo->setup(ctx, P, ctx.stream);
-    }
-    BatchDigest& t = *P->solo;
-    t.wait_tables();  // the previous build's table copies have left the host buffers
-    t.h_P[0] = dP;
-    t.h_G[0] = dG;
-    t.h_screen[0] = screen > 0 ? screen : 0.0;
-    cudaEvent_t e0, e1;
-    HF_CUDA(cudaEventCreate(&e0));
-    HF_CUDA(cudaEventCreate(&e1));
-    HF_CUDA(cudaEventRecord(e0, ctx.stream));
-    eri_digest_batch(ctx, P, t, ctx.stream);
-    HF_CUDA(cudaEventRecord(e1, ctx.stream));
-    ctx.fock_events.push_back({e0, e1, screen <= 0});  // timed later, without a host wait here
-}
-
 }  // namespace hfgpu

@@ -53,8 +53,7 @@ struct EriPlan {
     int nmol = 1;
     std::vector<int> mol_nbf, mol_ns, mol_sh0;
     DBuf<int64_t> mol_out;
-    // the one-molecule Fock build's tables and captured graph (eri_digest_graph)
-    std::unique_ptr<BatchDigest> solo;
+
     ShellDev shdev() const
     {
         return ShellDev{sL.p, snp.p, sxyz.p, sp0.p, sc0.p, scf.p, alpha.p, coef.p, cfn.p};

@@ -270,9 +270,7 @@ struct BatchDigest {
     void wait_tables();                  // host tables free to be rewritten
     ~BatchDigest();
 };
-// one molecule's Fock build (G = J - K/2 of dP into dG) as the replayed graph of a
-// batch of one; screen > 0 screens a density difference
-void eri_digest_graph(Context& ctx, EriPlan* P, const double* dP, double* dG, double screen);
+
 // one Fock build (G = J - K/2) for every molecule with h_screen >= 0, on stream s
 void eri_digest_batch(Context& ctx, EriPlan* P, BatchDigest& t, cudaStream_t s);
 // kernels counted so far (context.cu)
