@@ -434,10 +434,12 @@ __global__ void slice_kernel(Src src, int64_t rows, int K, int64_t rows_pad, int
 // largest magnitude of each row, from the same gathers).
 // 512 threads: thread t produces row t % 128, K quarter t / 128 (8 elements, one
 // 16-byte chunk per plane) of every stage, fetching the next stage's elements
-// before it stores this one; thread 0 also issues the B loads and the products;
-// the 16 warps share the epilogue (warp w: TMEM lanes 32 (w % 4), columns
-// 16 (w / 4) .. +15).
-constexpr int GATHER_THREADS = 512;
+// before it stores this one; the 16 producer warps share the epilogue (warp w:
+// TMEM lanes 32 (w % 4), columns 16 (w / 4) .. +15).  A 17th warp issues the
+// B loads (ahead, into every stage already free) and the products, so that no
+// producer waits for a stage's other producers.
+constexpr int GATHER_PRODUCERS = 512;
+constexpr int GATHER_THREADS = GATHER_PRODUCERS + 32;
 
 // Output-tile width and pipeline depth of the gather-fed GEMM: 64 columns with
 // three stages, or 80 columns (16 waters: 80 occupied orbitals in one tile, so
@@ -472,7 +474,7 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
     uint64_t* empty = full + C::GST;
     uint32_t* tslot = (uint32_t*)(empty + C::GST);
     __shared__ int s_ok;
-    constexpr int PARTS = GATHER_THREADS / BM;  // K parts of a stage per row
+    constexpr int PARTS = GATHER_PRODUCERS / BM;  // K parts of a stage per row
     __shared__ int s_exp[BM];  // row exponents of the current tile (for the epilogue)
     auto sA = [&](int s, int t) { return smem + s * C::STAGE + t * A_TILE; };
     auto sB = [&](int s, int t) { return smem + s * C::STAGE + NSL * A_TILE + t * C::B_T; };
@@ -481,9 +483,10 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
     constexpr int PK = BK / PARTS;              // elements per thread and stage (8: one 16-byte chunk)
     static_assert(PK == 8, "one 16-byte chunk per thread and plane");
     const int prow = tid & (BM - 1), part = tid / BM;
+    const bool producer = tid < GATHER_PRODUCERS, issuer = tid == GATHER_PRODUCERS;
     if (tid == 0) {
         for (int s = 0; s < C::GST; ++s) {
-            mbar_init(&full[s], GATHER_THREADS + 1);  // every producer + the B expect_tx
+            mbar_init(&full[s], GATHER_PRODUCERS + 1);  // every producer + the B expect_tx
             mbar_init(&empty[s], 1);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -501,20 +504,20 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
 
     bool ok = true;
     int64_t g0 = 0;
-    int64_t last_commit = -1;  // thread 0
-    int64_t pend_b = -1;       // thread 0: last step whose B load was issued
+    int64_t last_commit = -1;  // issuer
+    int64_t pend_b = -1;       // issuer: last step whose B load was issued
     for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const int64_t m0 = (tile / ntn) * BM;
         const int n0 = (int)(tile % ntn) * C::GBN;
         const int64_t R = m0 + prow;
-        const bool live = R < M && src.live(R);
+        const bool live = producer && R < M && src.live(R);
         const typename Src::Row row = src.row(live ? R : 0);
         // the row's exponent from the precomputed row maximum (row_max kernels);
         // the barrier keeps this tile's s_exp writes behind the last epilogue's reads
         const unsigned long long amax = live ? src.row_max(R) : 0ull;
         __syncthreads();
         const int e = row_exponent(amax);
-        if (part == 0) s_exp[prow] = e;
+        if (producer && part == 0) s_exp[prow] = e;
         // this thread's 8 elements of step 0, fetched ahead
         double x[PK];
 #pragma unroll
@@ -522,18 +525,62 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
             const int k = part * PK + j;
             x[j] = (live && k < K) ? src.at(row, k) : 0.0;
         }
-        for (int ks = 0; ks < ksteps && ok; ++ks) {
+        if (issuer) {
+            // B loads for every step up to g + GST - 1 whose stage is free (step g's own
+            // is waited for), then step g's products once its stage is full
+            int64_t next_b = g0;
+            const int64_t gend = g0 + ksteps;
+            for (int ks = 0; ks < ksteps && ok; ++ks) {
+                const int64_t g = g0 + ks;
+                while (next_b < gend && next_b < g + C::GST) {
+                    const int sl = (int)(next_b % C::GST);
+                    if (next_b >= C::GST) {
+                        const uint32_t ph = (uint32_t)(((next_b - C::GST) / C::GST) & 1);
+                        if (next_b == g) {
+                            if (!mbar_wait(&empty[sl], ph)) {
+                                ok = false;
+                                break;
+                            }
+                        } else if (!mbar_try_wait(&empty[sl], ph)) {
+                            break;
+                        }
+                    }
+                    mbar_expect_tx(&full[sl], NSL * C::B_T);
+#pragma unroll
+                    for (int t = 0; t < NSL; ++t)
+                        tma_load_2d(sB(sl, t), &tmB, (int)(next_b - g0) * BK, t * b_rows_pad + n0, &full[sl]);
+                    pend_b = next_b;
+                    ++next_b;
+                }
+                if (!ok) break;
+                const int s = (int)(g % C::GST);
+                if (!mbar_wait(&full[s], (uint32_t)((g / C::GST) & 1))) {
+                    ok = false;
+                    break;
+                }
+                fence_after();
+#pragma unroll
+                for (int i = 0; i < NSL; ++i)
+#pragma unroll
+                    for (int jj = 0; jj < NSL - i; ++jj) {
+                        const uint32_t dt = tmem + (uint32_t)((i + jj) * C::GBN);
+#pragma unroll
+                        for (int kk = 0; kk < BK / 16; ++kk) {
+                            const uint64_t ad = sdesc(su32(sA(s, i)) + kk * 32);
+                            const uint64_t bd = sdesc(su32(sB(s, jj)) + kk * 32);
+                            umma_d(dt, ad, bd, C::IDESC, (ks == 0 && i == 0 && kk == 0) ? 0u : 1u);
+                        }
+                    }
+                umma_commit(&empty[s]);
+                last_commit = g;
+            }
+        }
+        for (int ks = 0; ks < ksteps && ok && producer; ++ks) {
             const int64_t g = g0 + ks;
             const int s = (int)(g % C::GST);
             if (g >= C::GST && !mbar_wait(&empty[s], (uint32_t)(((g - C::GST) / C::GST) & 1))) {
                 ok = false;
                 break;
-            }
-            if (tid == 0) {
-                mbar_expect_tx(&full[s], NSL * C::B_T);
-#pragma unroll
-                for (int t = 0; t < NSL; ++t) tma_load_2d(sB(s, t), &tmB, ks * BK, t * b_rows_pad + n0, &full[s]);
-                pend_b = g;
             }
             // two elements per 32-bit word and plane: digit patterns 0x4300 | d, one
             // packed bf16 subtraction of 128, then the signs (slice_bits.cuh)
@@ -561,27 +608,6 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
             // the tensor core reads shared memory through the async proxy
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(&full[s]);
-            if (tid == 0) {
-                if (!mbar_wait(&full[s], (uint32_t)((g / C::GST) & 1))) {
-                    ok = false;
-                    break;
-                }
-                fence_after();
-#pragma unroll
-                for (int i = 0; i < NSL; ++i)
-#pragma unroll
-                    for (int jj = 0; jj < NSL - i; ++jj) {
-                        const uint32_t dt = tmem + (uint32_t)((i + jj) * C::GBN);
-#pragma unroll
-                        for (int kk = 0; kk < BK / 16; ++kk) {
-                            const uint64_t ad = sdesc(su32(sA(s, i)) + kk * 32);
-                            const uint64_t bd = sdesc(su32(sB(s, jj)) + kk * 32);
-                            umma_d(dt, ad, bd, C::IDESC, (ks == 0 && i == 0 && kk == 0) ? 0u : 1u);
-                        }
-                    }
-                umma_commit(&empty[s]);
-                last_commit = g;
-            }
         }
         if (!ok) atomicExch(&s_ok, 0);
         __syncthreads();
@@ -589,7 +615,7 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
         const int64_t glast = g0 + ksteps - 1;
         if (ok) ok = mbar_wait(&empty[glast % C::GST], (uint32_t)((glast / C::GST) & 1));
         ok = __syncthreads_and(ok);
-        if (ok) {
+        if (ok && producer) {
             fence_after();
             // warp w: TMEM lanes 32 (w % 4), 16 columns starting at 16 (w / 4)
             const int64_t r = m0 + (warp & 3) * 32 + lane;
@@ -622,7 +648,7 @@ __global__ void __launch_bounds__(GATHER_THREADS, 1)
     }
     if (!ok) {
         if (lane == 0) atomicExch(err, 1);
-        if (tid == 0) {
+        if (issuer) {
             // B copies and products still in flight land before shared memory and TMEM go (bounded)
             if (pend_b >= 0) mbar_wait(&full[pend_b % C::GST], (uint32_t)((pend_b / C::GST) & 1));
             if (last_commit >= 0) mbar_wait(&empty[last_commit % C::GST], (uint32_t)((last_commit / C::GST) & 1));
