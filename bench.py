@@ -532,6 +532,8 @@ def run_grad(args):
         wall = (time.perf_counter() - t0) / args.steps
         out[f"water{nw}"] = {"nbf": rs[-1]["nbf"], "ms_per_call": 1e3 * wall,
                              "ms_gradient_kernels": float(np.mean([r["ms_grad"] for r in rs])),
+                             "ms_gradient_eri_kernels": float(np.mean([r["ms_grad_eri"] for r in rs])),
+                             "ms_energy_eri_kernels": float(np.mean([r["ms_eri"] for r in rs])),
                              "ms_scf": float(np.mean([r["ms_scf"] for r in rs])),
                              "shell_quartets": rs[-1]["n_quartets"]}
     print(json.dumps({"metric": "RHF gradient calls/s", "value": 1e3 / out["water12"]["ms_per_call"],

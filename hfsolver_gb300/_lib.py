@@ -37,7 +37,8 @@ class Result(ctypes.Structure):
                 ("ms_mp2", ctypes.c_double), ("ms_total", ctypes.c_double), ("ms_setup", ctypes.c_double),
                 ("ms_fock", ctypes.c_double), ("ms_tcgemm", ctypes.c_double), ("tc_flops", ctypes.c_double),
                 ("ms_grad", ctypes.c_double), ("ms_fock_full", ctypes.c_double), ("n_fock_full", ctypes.c_double),
-                ("block_elems", ctypes.c_double), ("ms_tc_step1", ctypes.c_double), ("n_tc_step1", ctypes.c_double)]
+                ("block_elems", ctypes.c_double), ("ms_tc_step1", ctypes.c_double), ("n_tc_step1", ctypes.c_double),
+                ("ms_grad_eri", ctypes.c_double)]
 
 
 # name -> (restype, argtypes); the list every test of the ABI checks against

@@ -1,6 +1,7 @@
 """Build libhfgpu.so in-tree for sm_103a.
 
-Generates the ERI class bodies (csrc/gen_eri.py), compiles every translation
+Generates the ERI and ERI-gradient class bodies (csrc/gen_eri.py,
+csrc/gen_grad.py), compiles every translation
 unit with nvcc in parallel (objects cached in csrc/_build by content hash of
 the source and the local headers), and links hfsolver_gb300/libhfgpu.so
 against cudart, cuBLAS and cuSOLVER.
@@ -28,7 +29,8 @@ def _nvcc():
 
 
 def _sources():
-    subprocess.run([sys.executable, os.path.join(CSRC, "gen_eri.py")], check=True, capture_output=True)
+    for gen in ("gen_eri.py", "gen_grad.py"):
+        subprocess.run([sys.executable, os.path.join(CSRC, gen)], check=True, capture_output=True)
     srcs = [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cu", ".cpp"))]
     gen = os.path.join(CSRC, "gen")
     srcs += [os.path.join(gen, f) for f in sorted(os.listdir(gen)) if f.endswith(".cu")]

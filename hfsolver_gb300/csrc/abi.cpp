@@ -254,7 +254,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         }
         // analytic nuclear gradient at the converged orbitals
         if (conv && grad) {
-            rhf_gradient(ctx, plan.get(), natoms, atno, xyz, dC.p, dL.p, nocc, grad, &res->ms_grad);
+            rhf_gradient(ctx, plan.get(), natoms, atno, xyz, dC.p, dL.p, nocc, grad, &res->ms_grad, &res->ms_grad_eri);
             ctx.trace_mark("gradient");
         }
         if (C) dC.download(C, nn);

@@ -14,16 +14,17 @@
 // coefficients come from 1-D tables with one more unit of angular momentum.
 //
 // Two-electron part (adjoint form): derivative integrals are never stored.
-// For each primitive quartet, with R_{tuv} the Hermite Coulomb integrals up to
-// order L+1,
-//   H_cd(tau)  = s_cd sum_tau' (-1)^{|tau'|} E^{cd}_tau' R_{tau+tau'}
-//   T_ab(tau)  = sum_cd Gamma8_abcd H_cd(tau)
-//   g_A       += s_ab sum_tau (d_A E^{ab})_tau T_ab(tau)   (and g_B the same way)
-// and the mirror image for the ket centres C and D; Gamma8 = 8 Gamma.  A team of
-// lanes (a power of two, picked per class) owns one shell quartet; its lanes
-// split the (component pair, Hermite index) work of each primitive quartet,
-// with R, H and the six density blocks of the quartet in shared memory.  The
-// quartets are those the energy path evaluated (same Schwarz screening).
+// Per ordered quartet class, generated kernels (gen_grad.py, grad_kernel.cuh)
+// differentiate one pair of each screened quartet: the other pair's
+// primitives are summed first into Hermite intermediates
+//   X_cd(tau) = sum_{ket prims} sum_tau' (-1)^{|tau'|} E^{cd}_tau' R_{tau+tau'}
+// (R up to order L+1), which are then contracted once per bra primitive pair
+// with Gamma8 = 8 Gamma and the bra's derivative coefficients:
+//   g_A += sum_ab Gamma8 c_a c_b sum_tau (d_A E^{ab})_tau X_cd(tau),
+//   g_A + g_B from the Hermite shift tau -> tau + 1 (both centres moved).
+// A second launch with the pairs swapped gives g_C, and g_D follows from
+// translational invariance.  The quartets are those the energy path evaluated
+// (same Schwarz screening).
 //
 // One-electron part: one thread per basis-function pair and pair of nuclei; dS/dA and dT/dA from
 // shifted 1-D overlaps (dB = -dA for two-centre integrals), dV from the shifted
@@ -36,20 +37,15 @@
 
 #include "boys.cuh"
 #include "eri_plan.h"
+#include "grad_kernel.cuh"
 #include "internal.h"
 #include "md.cuh"
 
 namespace hfgpu {
-
 // ------------------------------------------------------------- 1-D tables
 // E[i][j][t] for i <= la+1, j <= lb+1, t <= i+j, zero elsewhere
 constexpr int GE_I = 4, GE_J = 4, GE_T = 7;
 constexpr int GE_DIM = GE_I * GE_J * GE_T;
-constexpr int GP_HDR = 8;  // alpha_a, alpha_b, p, Px, Py, Pz, exp(-mu R_AB^2)/p, unused
-constexpr int GP_STRIDE = GP_HDR + 3 * GE_DIM;
-constexpr int GRAD_LMAX = 9;  // L + 1 for (dd|dd)
-constexpr int GRAD_NH = nherm(GRAD_LMAX);
-constexpr int GRAD_BLOCK = 128;
 
 __device__ __forceinline__ int ge(int i, int j, int t) { return (i * GE_J + j) * GE_T + t; }
 
@@ -76,40 +72,63 @@ __device__ static void e1d_rt(double* E, int imax, int jmax, double xpa, double 
 }
 
 // one thread per primitive pair of every shell pair
+// one thread per primitive pair of every shell pair: the bra-side record of
+// the gradient kernels (layout in grad_kernel.cuh: header, then the 1-D
+// Hermite coefficients E and the derivative coefficients
+// D(i, j, t) = 2a E(i+1, j, t) - i E(i-1, j, t) of each axis)
 __global__ void grad_pair_kernel(const int* __restrict__ sL, const int* __restrict__ snp, const int* __restrict__ sp0,
-                                 const double* __restrict__ sxyz, const double* __restrict__ alpha,
-                                 const int* __restrict__ pA, const int* __restrict__ pB, const int4* __restrict__ items,
-                                 int nitems, double* __restrict__ gp)
+                                 const int* __restrict__ sc0, const double* __restrict__ sxyz,
+                                 const double* __restrict__ alpha, const double* __restrict__ coef,
+                                 const int* __restrict__ pA, const int* __restrict__ pB, const int2* __restrict__ items,
+                                 int nitems, const int64_t* __restrict__ goff, double* __restrict__ gd)
 {
     const int it = blockIdx.x * blockDim.x + threadIdx.x;
     if (it >= nitems) return;
-    const int4 item = items[it];  // (pair, record index, primitive pair within the pair)
+    const int2 item = items[it];  // (pair, primitive pair within the pair)
     const int P = item.x;
     const int A = pA[P], B = pB[P];
-    double* rec = gp + (int64_t)item.y * GP_STRIDE;
-    const int nb = snp[B];
-    const int ia = item.z / nb, ib = item.z - ia * nb;  // ia-major, as in the energy records
+    const int la = sL[A], lb = sL[B];
+    const int npa = snp[A], nb = snp[B];
+    const int ia = item.y / nb, ib = item.y - ia * nb;  // ia-major, as in the energy records
+    double* rec = gd + goff[P] + (int64_t)item.y * grad_stride(la, lb);
     const double a = alpha[sp0[A] + ia], b = alpha[sp0[B] + ib];
     const double ax = sxyz[3 * A], ay = sxyz[3 * A + 1], az = sxyz[3 * A + 2];
     const double bx = sxyz[3 * B], by = sxyz[3 * B + 1], bz = sxyz[3 * B + 2];
     const double p = a + b, ip = 1.0 / p, mu = a * b * ip;
     const double px = (a * ax + b * bx) * ip, py = (a * ay + b * by) * ip, pz = (a * az + b * bz) * ip;
     const double rab2 = (ax - bx) * (ax - bx) + (ay - by) * (ay - by) + (az - bz) * (az - bz);
+    const double kab = exp(-mu * rab2) * ip;
     rec[0] = a;
     rec[1] = b;
     rec[2] = p;
     rec[3] = px;
     rec[4] = py;
     rec[5] = pz;
-    rec[6] = exp(-mu * rab2) * ip;
+    rec[6] = kab;
     rec[7] = 0.0;
-    const int la = sL[A] + 1, lb = sL[B] + 1;
-    e1d_rt(rec + GP_HDR, la, lb, px - ax, px - bx, 0.5 * ip);
-    e1d_rt(rec + GP_HDR + GE_DIM, la, lb, py - ay, py - by, 0.5 * ip);
-    e1d_rt(rec + GP_HDR + 2 * GE_DIM, la, lb, pz - az, pz - bz, 0.5 * ip);
+    for (int c = 0; c < 6; ++c) {
+        rec[8 + c] = c < ncart(la) ? coef[sc0[A] + c * npa + ia] * kab : 0.0;
+        rec[14 + c] = c < ncart(lb) ? coef[sc0[B] + c * nb + ib] : 0.0;
+    }
+    const int ts = grad_table(la, lb), tw = la + lb + 2;
+    const double xa[3] = {px - ax, py - ay, pz - az}, xb[3] = {px - bx, py - by, pz - bz};
+    double E[GE_DIM];
+    for (int d = 0; d < 3; ++d) {
+        e1d_rt(E, la + 1, lb, xa[d], xb[d], 0.5 * ip);
+        double* te = rec + GR_HDR + d * ts;
+        double* td = rec + GR_HDR + (3 + d) * ts;
+        for (int i = 0; i <= la; ++i)
+            for (int j = 0; j <= lb; ++j)
+                for (int t = 0; t < tw; ++t) {
+                    const int o = (i * (lb + 1) + j) * tw + t;
+                    te[o] = t <= i + j ? E[ge(i, j, t)] : 0.0;
+                    const double up = E[ge(i + 1, j, t)];
+                    const double dn = (i > 0 && t <= i + j - 1) ? E[ge(i - 1, j, t)] : 0.0;
+                    td[o] = 2.0 * a * up - (double)i * dn;
+                }
+    }
 }
 
-// Boys values F[0..M] scaled as in boys_scaled, for a runtime order M
 __device__ static void boys_rt(int M, double T, double pref, double s, const double* __restrict__ tab, double* F)
 {
     if (T < BOYS_TMAX) {
@@ -148,320 +167,7 @@ __device__ static void boys_rt(int M, double T, double pref, double s, const dou
 }
 
 // ------------------------------------------------------------- two-electron part
-struct GradArgs {
-    const int* pA;
-    const int* pB;
-    const int* pK;
-    const int* snp;
-    const int* sc0;
-    const int* cfn0;
-    const int* comp_fn;
-    const int* sat;  // atom of each shell
-    const double* coef;
-    const int64_t* goff;  // first record of each pair
-    const double* gp;
-    const double* boys;
-    const int* gpairs;
-    const int64_t* prefix;
-    const Seg* segs;
-    int nseg;
-    int64_t nq;
-    const int* herm;   // Hermite index -> t | u << 4 | v << 8
-    const int* cartc;  // (L, component) -> l | m << 4 | n << 8
-    const double* P;
-    int n;
-    double* grad;  // 3 per atom
-    int la, lb, lc, ld;
-    int team;       // lanes per quartet
-    int smem_team;  // doubles of shared memory per team
-};
-
-__device__ __forceinline__ int tq(int c, int s) { return (c >> s) & 15; }
-
-// PRIV = false: the team's lanes split each primitive quartet's component loops
-// (classes with many components).  PRIV = true: each lane takes every tm-th
-// primitive quartet with a private workspace, the density blocks shared (light
-// classes such as (ss|ss), whose 1 - 9 components would leave most lanes idle
-// while one walks up to 36 x 36 primitive quartets).
-template <bool PRIV>
-__global__ void __launch_bounds__(GRAD_BLOCK) eri_grad_kernel(GradArgs g)
-{
-    extern __shared__ double sm[];
-    const int tm = g.team;
-    const int tid = threadIdx.x;
-    const int lt = tid & (tm - 1);
-    const unsigned lane = tid & 31;
-    const unsigned mask = tm == 32 ? 0xffffffffu : (((1u << tm) - 1u) << (lane & ~(unsigned)(tm - 1)));
-    const int64_t qg = ((int64_t)blockIdx.x * GRAD_BLOCK + tid) / tm;
-    if (qg >= g.nq) return;  // the whole team leaves together
-    const int qg32 = (int)qg;
-    double* ws = sm + (int64_t)(tid / tm) * g.smem_team;
-
-    int lo = 0, hi = g.nseg - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if ((int)(g.segs[mid].qoff) <= qg32) lo = mid; else hi = mid - 1;
-    }
-    const Seg sg = g.segs[lo];
-    const int q = qg32 - (int)sg.qoff;  // class quartet counts stay below 2^31 (plan check)
-    int bra, ket;
-    {
-        const int64_t* pf = g.prefix + sg.pref0;
-        int l2 = 0, h2 = sg.nbra - 1;
-        while (l2 < h2) {
-            const int mid = (l2 + h2 + 1) >> 1;
-            if ((int)pf[mid] <= q) l2 = mid; else h2 = mid - 1;
-        }
-        bra = g.gpairs[sg.bra0 + l2];
-        ket = g.gpairs[sg.ket0 + (q - (int)pf[l2])];
-    }
-    const int A = g.pA[bra], B = g.pB[bra], C = g.pA[ket], D = g.pB[ket];
-    const int la = g.la, lb = g.lb, lc = g.lc, ld = g.ld;
-    const int NA = ncart(la), NB = ncart(lb), NC = ncart(lc), ND = ncart(ld);
-    const int NAB = NA * NB, NCD = NC * ND;
-    const int L = la + lb + lc + ld;
-    const int nHp = nherm(la + lb + 1), nHq = nherm(lc + ld + 1), nR = nherm(L + 1);
-
-    double* PAB = ws;
-    double* PCD = PAB + NAB;
-    double* PAC = PCD + NCD;
-    double* PBD = PAC + NA * NC;
-    double* PAD = PBD + NB * ND;
-    double* PBC = PAD + NA * ND;
-    // per-primitive workspace: the team's, or this lane's own
-    const int nshared = NAB + NCD + NA * NC + NB * ND + NA * ND + NB * NC;
-    const int npriv = NAB + NCD + 2 * nR + (NCD * nHp > NAB * nHq ? NCD * nHp : NAB * nHq);
-    double* sab = PBC + NB * NC + (PRIV ? lt * npriv : 0);
-    double* scd = sab + NAB;
-    double* R0 = scd + NCD;
-    double* R1 = R0 + nR;
-    double* H = R1 + nR;
-
-    const int* fa = g.comp_fn + g.cfn0[A];
-    const int* fb = g.comp_fn + g.cfn0[B];
-    const int* fc = g.comp_fn + g.cfn0[C];
-    const int* fd = g.comp_fn + g.cfn0[D];
-    const int n = g.n;
-    // component loops: split over the team, or whole in each lane
-    const int c0 = PRIV ? 0 : lt, cs = PRIV ? 1 : tm;
-    auto team_sync = [&]() {
-        if (!PRIV) __syncwarp(mask);
-    };
-    auto Pv = [&](int x, int y) -> double { return (x < 0 || y < 0) ? 0.0 : __ldg(g.P + x + (int64_t)y * n); };
-    for (int e = lt; e < NAB; e += tm) PAB[e] = Pv(fa[e / NB], fb[e % NB]);
-    for (int e = lt; e < NCD; e += tm) PCD[e] = Pv(fc[e / ND], fd[e % ND]);
-    for (int e = lt; e < NA * NC; e += tm) PAC[e] = Pv(fa[e / NC], fc[e % NC]);
-    for (int e = lt; e < NB * ND; e += tm) PBD[e] = Pv(fb[e / ND], fd[e % ND]);
-    for (int e = lt; e < NA * ND; e += tm) PAD[e] = Pv(fa[e / ND], fd[e % ND]);
-    for (int e = lt; e < NB * NC; e += tm) PBC[e] = Pv(fb[e / NC], fc[e % NC]);
-    __syncwarp(mask);
-
-    const int kb = g.pK[bra], kk = g.pK[ket];
-    const int npA = g.snp[A], npB = g.snp[B], npC = g.snp[C], npD = g.snp[D];
-    const double* cA = g.coef + g.sc0[A];
-    const double* cB = g.coef + g.sc0[B];
-    const double* cC = g.coef + g.sc0[C];
-    const double* cD = g.coef + g.sc0[D];
-    const int* cla = g.cartc + la * 6;
-    const int* clb = g.cartc + lb * 6;
-    const int* clc = g.cartc + lc * 6;
-    const int* cld = g.cartc + ld * 6;
-    double gr[12];
-#pragma unroll
-    for (int k = 0; k < 12; ++k) gr[k] = 0.0;
-
-    for (int pq = PRIV ? lt : 0; pq < kb * kk; pq += PRIV ? tm : 1) {
-        {
-            const int pb = pq / kk, pk = pq - pb * kk;
-            const double* rb = g.gp + (g.goff[bra] + pb) * GP_STRIDE;
-            const double* rk = g.gp + (g.goff[ket] + pk) * GP_STRIDE;
-            const double p = __ldg(rb + 2), q_ = __ldg(rk + 2);
-            const double X = __ldg(rb + 3) - __ldg(rk + 3), Y = __ldg(rb + 4) - __ldg(rk + 4),
-                         Z = __ldg(rb + 5) - __ldg(rk + 5);
-            const double r = rsqrt_nr(p + q_);
-            const double alp = p * q_ * (r * r);
-            const double T = alp * (X * X + Y * Y + Z * Z);
-            double F[GRAD_LMAX + 1];
-            boys_rt(L + 1, T, TWO_PI_2_5 * r, -2.0 * alp, g.boys, F);
-            {
-                const int ia = pb / npB, ib = pb - ia * npB, ic = pk / npD, id = pk - ic * npD;
-                const double kab = __ldg(rb + 6), kcd = __ldg(rk + 6);
-                for (int e = c0; e < NAB; e += cs) sab[e] = cA[(e / NB) * npA + ia] * cB[(e % NB) * npB + ib] * kab;
-                for (int e = c0; e < NCD; e += cs) scd[e] = cC[(e / ND) * npC + ic] * cD[(e % ND) * npD + id] * kcd;
-            }
-            // R^{(m)}_{tuv}, from m = L+1 down to m = 0
-            double* cur = R0;
-            double* nxt = R1;
-            if (PRIV || lt == 0) cur[0] = F[L + 1];
-            team_sync();
-            for (int m = L; m >= 0; --m) {
-                const int cnt = nherm(L + 1 - m);
-                for (int h = c0; h < cnt; h += cs) {
-                    const int c = __ldg(g.herm + h);
-                    const int t = tq(c, 0), u = tq(c, 4), v = tq(c, 8);
-                    double val;
-                    if (h == 0) {
-                        val = F[m];
-                    } else if (t > 0) {
-                        val = X * cur[hidx(t - 1, u, v)];
-                        if (t > 1) val = fma((double)(t - 1), cur[hidx(t - 2, u, v)], val);
-                    } else if (u > 0) {
-                        val = Y * cur[hidx(0, u - 1, v)];
-                        if (u > 1) val = fma((double)(u - 1), cur[hidx(0, u - 2, v)], val);
-                    } else {
-                        val = Z * cur[hidx(0, 0, v - 1)];
-                        if (v > 1) val = fma((double)(v - 1), cur[hidx(0, 0, v - 2)], val);
-                    }
-                    nxt[h] = val;
-                }
-                team_sync();
-                double* tmp = cur;
-                cur = nxt;
-                nxt = tmp;
-            }
-            const double* R = cur;
-            const double* Bx = rb + GP_HDR;
-            const double* By = Bx + GE_DIM;
-            const double* Bz = By + GE_DIM;
-            const double* Kx = rk + GP_HDR;
-            const double* Ky = Kx + GE_DIM;
-            const double* Kz = Ky + GE_DIM;
-
-            // ---- bra centres A, B
-            for (int it = c0; it < NCD * nHp; it += cs) {
-                const int cd = it / nHp, h = it - cd * nHp;
-                const int c = cd / ND, d = cd - c * ND;
-                const int cc = clc[c], dc = cld[d], hc = __ldg(g.herm + h);
-                const int cx = tq(cc, 0), cy = tq(cc, 4), cz = tq(cc, 8);
-                const int dx = tq(dc, 0), dy = tq(dc, 4), dz = tq(dc, 8);
-                const int t = tq(hc, 0), u = tq(hc, 4), v = tq(hc, 8);
-                double acc = 0.0;
-                for (int t2 = 0; t2 <= cx + dx; ++t2) {
-                    const double ex = __ldg(Kx + ge(cx, dx, t2));
-                    for (int u2 = 0; u2 <= cy + dy; ++u2) {
-                        const double exy = ex * __ldg(Ky + ge(cy, dy, u2));
-                        for (int v2 = 0; v2 <= cz + dz; ++v2) {
-                            const double e = exy * __ldg(Kz + ge(cz, dz, v2));
-                            const double rv = R[hidx(t + t2, u + u2, v + v2)];
-                            acc = ((t2 + u2 + v2) & 1) ? fma(-e, rv, acc) : fma(e, rv, acc);
-                        }
-                    }
-                }
-                H[it] = acc * scd[cd];
-            }
-            team_sync();
-            {
-                const double al = __ldg(rb), be = __ldg(rb + 1);
-                for (int it = c0; it < NAB * nHp; it += cs) {
-                    const int ab = it / nHp, h = it - ab * nHp;
-                    const int a = ab / NB, b = ab - a * NB;
-                    const int ac = cla[a], bc = clb[b], hc = __ldg(g.herm + h);
-                    const int ax = tq(ac, 0), ay = tq(ac, 4), az = tq(ac, 8);
-                    const int bx = tq(bc, 0), by = tq(bc, 4), bz = tq(bc, 8);
-                    const int t = tq(hc, 0), u = tq(hc, 4), v = tq(hc, 8);
-                    const int ox = t - ax - bx, oy = u - ay - by, oz = v - az - bz;
-                    if (ox > 1 || oy > 1 || oz > 1 || (ox > 0) + (oy > 0) + (oz > 0) > 1) continue;
-                    double Tv = 0.0;
-                    const double pab4 = 4.0 * PAB[ab];
-                    for (int c = 0; c < NC; ++c) {
-                        const double pac = PAC[a * NC + c], pbc = PBC[b * NC + c];
-                        for (int d = 0; d < ND; ++d) {
-                            const double gm = pab4 * PCD[c * ND + d] - pac * PBD[b * ND + d] - PAD[a * ND + d] * pbc;
-                            Tv = fma(gm, H[(c * ND + d) * nHp + h], Tv);
-                        }
-                    }
-                    const double w = sab[ab] * Tv;
-                    const double ex = __ldg(Bx + ge(ax, bx, t)), ey = __ldg(By + ge(ay, by, u)),
-                                 ez = __ldg(Bz + ge(az, bz, v));
-                    const double dax = 2.0 * al * __ldg(Bx + ge(ax + 1, bx, t)) - (ax ? ax * __ldg(Bx + ge(ax - 1, bx, t)) : 0.0);
-                    const double day = 2.0 * al * __ldg(By + ge(ay + 1, by, u)) - (ay ? ay * __ldg(By + ge(ay - 1, by, u)) : 0.0);
-                    const double daz = 2.0 * al * __ldg(Bz + ge(az + 1, bz, v)) - (az ? az * __ldg(Bz + ge(az - 1, bz, v)) : 0.0);
-                    const double dbx = 2.0 * be * __ldg(Bx + ge(ax, bx + 1, t)) - (bx ? bx * __ldg(Bx + ge(ax, bx - 1, t)) : 0.0);
-                    const double dby = 2.0 * be * __ldg(By + ge(ay, by + 1, u)) - (by ? by * __ldg(By + ge(ay, by - 1, u)) : 0.0);
-                    const double dbz = 2.0 * be * __ldg(Bz + ge(az, bz + 1, v)) - (bz ? bz * __ldg(Bz + ge(az, bz - 1, v)) : 0.0);
-                    gr[0] = fma(w, dax * ey * ez, gr[0]);
-                    gr[1] = fma(w, ex * day * ez, gr[1]);
-                    gr[2] = fma(w, ex * ey * daz, gr[2]);
-                    gr[3] = fma(w, dbx * ey * ez, gr[3]);
-                    gr[4] = fma(w, ex * dby * ez, gr[4]);
-                    gr[5] = fma(w, ex * ey * dbz, gr[5]);
-                }
-            }
-            team_sync();
-
-            // ---- ket centres C, D
-            for (int it = c0; it < NAB * nHq; it += cs) {
-                const int ab = it / nHq, h = it - ab * nHq;
-                const int a = ab / NB, b = ab - a * NB;
-                const int ac = cla[a], bc = clb[b], hc = __ldg(g.herm + h);
-                const int ax = tq(ac, 0), ay = tq(ac, 4), az = tq(ac, 8);
-                const int bx = tq(bc, 0), by = tq(bc, 4), bz = tq(bc, 8);
-                const int t = tq(hc, 0), u = tq(hc, 4), v = tq(hc, 8);
-                double acc = 0.0;
-                for (int t2 = 0; t2 <= ax + bx; ++t2) {
-                    const double ex = __ldg(Bx + ge(ax, bx, t2));
-                    for (int u2 = 0; u2 <= ay + by; ++u2) {
-                        const double exy = ex * __ldg(By + ge(ay, by, u2));
-                        for (int v2 = 0; v2 <= az + bz; ++v2)
-                            acc = fma(exy * __ldg(Bz + ge(az, bz, v2)), R[hidx(t + t2, u + u2, v + v2)], acc);
-                    }
-                }
-                H[it] = ((t + u + v) & 1 ? -acc : acc) * sab[ab];
-            }
-            team_sync();
-            {
-                const double gc = __ldg(rk), gd = __ldg(rk + 1);
-                for (int it = c0; it < NCD * nHq; it += cs) {
-                    const int cd = it / nHq, h = it - cd * nHq;
-                    const int c = cd / ND, d = cd - c * ND;
-                    const int cc = clc[c], dc = cld[d], hc = __ldg(g.herm + h);
-                    const int cx = tq(cc, 0), cy = tq(cc, 4), cz = tq(cc, 8);
-                    const int dx = tq(dc, 0), dy = tq(dc, 4), dz = tq(dc, 8);
-                    const int t = tq(hc, 0), u = tq(hc, 4), v = tq(hc, 8);
-                    const int ox = t - cx - dx, oy = u - cy - dy, oz = v - cz - dz;
-                    if (ox > 1 || oy > 1 || oz > 1 || (ox > 0) + (oy > 0) + (oz > 0) > 1) continue;
-                    double Tv = 0.0;
-                    const double pcd4 = 4.0 * PCD[cd];
-                    for (int a = 0; a < NA; ++a) {
-                        const double pac = PAC[a * NC + c], pad = PAD[a * ND + d];
-                        for (int b = 0; b < NB; ++b) {
-                            const double gm = pcd4 * PAB[a * NB + b] - pac * PBD[b * ND + d] - pad * PBC[b * NC + c];
-                            Tv = fma(gm, H[(a * NB + b) * nHq + h], Tv);
-                        }
-                    }
-                    const double w = scd[cd] * Tv;
-                    const double ex = __ldg(Kx + ge(cx, dx, t)), ey = __ldg(Ky + ge(cy, dy, u)),
-                                 ez = __ldg(Kz + ge(cz, dz, v));
-                    const double dcx = 2.0 * gc * __ldg(Kx + ge(cx + 1, dx, t)) - (cx ? cx * __ldg(Kx + ge(cx - 1, dx, t)) : 0.0);
-                    const double dcy = 2.0 * gc * __ldg(Ky + ge(cy + 1, dy, u)) - (cy ? cy * __ldg(Ky + ge(cy - 1, dy, u)) : 0.0);
-                    const double dcz = 2.0 * gc * __ldg(Kz + ge(cz + 1, dz, v)) - (cz ? cz * __ldg(Kz + ge(cz - 1, dz, v)) : 0.0);
-                    const double ddx = 2.0 * gd * __ldg(Kx + ge(cx, dx + 1, t)) - (dx ? dx * __ldg(Kx + ge(cx, dx - 1, t)) : 0.0);
-                    const double ddy = 2.0 * gd * __ldg(Ky + ge(cy, dy + 1, u)) - (dy ? dy * __ldg(Ky + ge(cy, dy - 1, u)) : 0.0);
-                    const double ddz = 2.0 * gd * __ldg(Kz + ge(cz, dz + 1, v)) - (dz ? dz * __ldg(Kz + ge(cz, dz - 1, v)) : 0.0);
-                    gr[6] = fma(w, dcx * ey * ez, gr[6]);
-                    gr[7] = fma(w, ex * dcy * ez, gr[7]);
-                    gr[8] = fma(w, ex * ey * dcz, gr[8]);
-                    gr[9] = fma(w, ddx * ey * ez, gr[9]);
-                    gr[10] = fma(w, ex * ddy * ez, gr[10]);
-                    gr[11] = fma(w, ex * ey * ddz, gr[11]);
-                }
-            }
-            team_sync();
-        }
-    }
-    for (int o = tm >> 1; o > 0; o >>= 1)
-#pragma unroll
-        for (int k = 0; k < 12; ++k) gr[k] += __shfl_xor_sync(mask, gr[k], o);
-    if (lt == 0) {
-        const double f = (A == B ? 0.5 : 1.0) * (C == D ? 0.5 : 1.0) * (bra == ket ? 0.5 : 1.0);
-        const int at[4] = {g.sat[A], g.sat[B], g.sat[C], g.sat[D]};
-#pragma unroll
-        for (int s = 0; s < 4; ++s)
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-                if (gr[3 * s + k] != 0.0) atomicAdd(g.grad + 3 * at[s] + k, f * gr[3 * s + k]);
-    }
-}
+// (the class kernels: grad_kernel.cuh and gen/grad_class_*.cu)
 
 // ------------------------------------------------------------- one-electron part
 struct OneArgs {
@@ -644,36 +350,34 @@ __global__ void onee_grad_kernel(OneArgs o)
 }
 
 // ------------------------------------------------------------- host side
-static int grad_team(int la, int lb, int lc, int ld)
+#define HF_GDECL(B, K) GradKernelFn grad_kernel_##B##K(bool withp);
+HF_GDECL(0, 0) HF_GDECL(0, 1) HF_GDECL(0, 2) HF_GDECL(0, 3) HF_GDECL(0, 4) HF_GDECL(0, 5)
+HF_GDECL(1, 0) HF_GDECL(1, 1) HF_GDECL(1, 2) HF_GDECL(1, 3) HF_GDECL(1, 4) HF_GDECL(1, 5)
+HF_GDECL(2, 0) HF_GDECL(2, 1) HF_GDECL(2, 2) HF_GDECL(2, 3) HF_GDECL(2, 4) HF_GDECL(2, 5)
+HF_GDECL(3, 0) HF_GDECL(3, 1) HF_GDECL(3, 2) HF_GDECL(3, 3) HF_GDECL(3, 4) HF_GDECL(3, 5)
+HF_GDECL(4, 0) HF_GDECL(4, 1) HF_GDECL(4, 2) HF_GDECL(4, 3) HF_GDECL(4, 4) HF_GDECL(4, 5)
+HF_GDECL(5, 0) HF_GDECL(5, 1) HF_GDECL(5, 2) HF_GDECL(5, 3) HF_GDECL(5, 4) HF_GDECL(5, 5)
+#undef HF_GDECL
+
+static GradKernelFn get_grad_kernel(int tb, int tk, bool withp)
 {
-    const int w = ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) *
-                  std::max(nherm(la + lb + 1), nherm(lc + ld + 1));
-    if (w >= 2000) return 32;
-    if (w >= 500) return 16;
-    if (w >= 120) return 8;
-    return 4;
+#define HF_GROW(B) {grad_kernel_##B##0, grad_kernel_##B##1, grad_kernel_##B##2, grad_kernel_##B##3, grad_kernel_##B##4, grad_kernel_##B##5}
+    static GradKernelFn (*const table[6][6])(bool) = {HF_GROW(0), HF_GROW(1), HF_GROW(2), HF_GROW(3), HF_GROW(4), HF_GROW(5)};
+#undef HF_GROW
+    return table[tb][tk](withp);
 }
 
-// classes with at most this many component quartets run the primitive loop one
-// primitive quartet per lane (eri_grad_kernel<true>), 8 lanes per shell quartet
-constexpr int GRAD_PRIV_MAX = 9, GRAD_PRIV_TEAM = 8;
-
-static bool grad_priv(int la, int lb, int lc, int ld)
+// lanes per quartet: enough primitive quartets per lane (16 to 32), so that a
+// quartet with many primitives does not hold its warp long after the others
+static int grad_split(int kb, int kk)
 {
-    return ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) <= GRAD_PRIV_MAX;
+    int s = 1;
+    while (s < 32 && (int64_t)kb * kk >= 2 * 16 * (int64_t)s) s <<= 1;
+    return s;
 }
 
-// doubles of shared memory per team: the six density blocks, then the
-// per-primitive workspace (one per lane in the private mode)
-static int grad_smem_team(int la, int lb, int lc, int ld, bool priv, int team)
-{
-    const int NA = ncart(la), NB = ncart(lb), NC = ncart(lc), ND = ncart(ld);
-    const int NAB = NA * NB, NCD = NC * ND;
-    const int nHp = nherm(la + lb + 1), nHq = nherm(lc + ld + 1), nR = nherm(la + lb + lc + ld + 1);
-    const int shared = NAB + NCD + NA * NC + NB * ND + NA * ND + NB * NC;
-    const int work = NAB + NCD + 2 * nR + std::max(NCD * nHp, NAB * nHq);
-    return shared + (priv ? team : 1) * work;
-}
+// the max dynamic shared memory of the kernels that have been raised so far
+static std::mutex g_smem_mu;
 
 void eri_gradient(Context& ctx, EriPlan* P, const double* dP, double* d_grad, float* ms_out)
 {
@@ -681,81 +385,126 @@ void eri_gradient(Context& ctx, EriPlan* P, const double* dP, double* d_grad, fl
     const Basis& b = P->basis;
     const int ns = (int)b.shells.size();
     std::vector<int> sat(ns);
+    int nat = 0;
     for (int s = 0; s < ns; ++s) {
         HF_CHECK(b.shells[s].atom >= 0, HFGPU_ERR_UNSUPPORTED, "gradient needs a basis built from atoms");
         HF_CHECK(b.shells[s].L <= 2, HFGPU_ERR_UNSUPPORTED, "gradient supports s, p and d shells");
         sat[s] = b.shells[s].atom;
+        nat = std::max(nat, sat[s] + 1);
     }
+    constexpr int MAX_GAM = 36;  // largest NAB x NCDC of any ordered class (a dd bra)
+    const size_t smem_max = ((size_t)MAX_GAM * GRAD_BLK + 3 * (size_t)nat) * sizeof(double);
+    HF_CHECK(smem_max <= 200 * 1024, HFGPU_ERR_UNSUPPORTED, "gradient: too many atoms for the per-block sums");
     // gradient pair records: pair P's records are consecutive, (ia, ib) ia-major
     std::vector<int64_t> goff(P->npair);
-    std::vector<int4> items;
+    std::vector<int2> items;
     int64_t nrec = 0;
     for (int id = 0; id < P->npair; ++id) {
         goff[id] = nrec;
-        for (int k = 0; k < P->pK[id]; ++k) items.push_back(make_int4(id, (int)(nrec + k), k, 0));
-        nrec += P->pK[id];
+        const int la = b.shells[P->pA[id]].L, lb = b.shells[P->pB[id]].L;
+        for (int k = 0; k < P->pK[id]; ++k) items.push_back(make_int2(id, k));
+        nrec += (int64_t)P->pK[id] * grad_stride(la, lb);
     }
-    DBuf<double> gp((size_t)nrec * GP_STRIDE, st);
-    DBuf<int4> dit = to_device(items, st);
+    DBuf<double> gd((size_t)std::max<int64_t>(nrec, 1), st);
+    DBuf<int2> dit = to_device(items, st);
+    DBuf<int64_t> dgoff = to_device(goff, st);
     {
         const int ni = (int)items.size();
-        grad_pair_kernel<<<(ni + 127) / 128, 128, 0, st>>>(P->sL.p, P->snp.p, P->sp0.p, P->sxyz.p, P->alpha.p,
-                                                          P->dA.p, P->dB.p, dit.p, ni, gp.p);
-        count_launch();
-        HF_CUDA(cudaGetLastError());
-    }
-    std::vector<int> herm(GRAD_NH), cartc(3 * 6, 0);
-    for (int s = 0; s <= GRAD_LMAX; ++s)
-        for (int w = 0; w <= s; ++w)
-            for (int v = 0; v <= w; ++v) {
-                const int u = w - v, t = s - w;
-                herm[hidx(t, u, v)] = t | (u << 4) | (v << 8);
-            }
-    for (int L = 0; L <= 2; ++L)
-        for (int c = 0; c < ncart(L); ++c) {
-            const Cart cc = cart(L, c);
-            cartc[L * 6 + c] = cc.l | (cc.m << 4) | (cc.n << 8);
+        if (ni > 0) {
+            grad_pair_kernel<<<(ni + 127) / 128, 128, 0, st>>>(P->sL.p, P->snp.p, P->sp0.p, P->sc0.p, P->sxyz.p,
+                                                              P->alpha.p, P->coef.p, P->dA.p, P->dB.p, dit.p, ni,
+                                                              dgoff.p, gd.p);
+            count_launch();
+            HF_CUDA(cudaGetLastError());
         }
-    DBuf<int> dherm = to_device(herm, st), dcart = to_device(cartc, st), dsat = to_device(sat, st);
-    DBuf<int64_t> dgoff = to_device(goff, st);
-
-    static std::once_flag once;
-    std::call_once(once, [] {
-        cudaFuncSetAttribute(eri_grad_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(eri_grad_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    });
+    }
+    DBuf<int> dsat = to_device(sat, st);
     ctx.trace_mark("grad pair data");
+
+    // two launches per class: the bra side of (tb, tk), then its ket side as
+    // the swapped class (tk, tb); each with its own warp layout
+    struct Launch {
+        GradKernelFn fn;
+        int64_t nwarps;
+        int gam;
+        int seg0, nseg;
+        double work;  // primitive quartets x component quartets, for the launch order
+    };
+    std::vector<Launch> launches;
+    std::vector<Seg> segs;
+    for (int i = (int)P->classes.size() - 1; i >= 0; --i) {
+        const ClassPlan& c = P->classes[i];
+        if (c.nq == 0) continue;
+        for (int side = 0; side < 2; ++side) {
+            const int tb = side == 0 ? c.tb : c.tk, tk = side == 0 ? c.tk : c.tb;
+            const int G = ncart(ptype_la(tk)) * ncart(ptype_lb(tk)) / grad_ncd(tb, tk);
+            Launch l;
+            l.fn = get_grad_kernel(tb, tk, side == 0);
+            HF_CHECK(l.fn != nullptr, HFGPU_ERR_UNSUPPORTED, "missing gradient kernel");
+            l.gam = ncart(ptype_la(tb)) * ncart(ptype_lb(tb)) * grad_ncd(tb, tk);
+            l.seg0 = (int)segs.size();
+            l.nwarps = 0;
+            l.work = 0;
+            for (const Seg& s0 : c.segs) {
+                HF_CHECK(s0.list == 0, HFGPU_ERR_UNSUPPORTED, "gradient expects prefix-mode segments");
+                Seg s = s0;
+                const int kbra = P->pK[P->h_gpairs[s0.bra0]], kket = P->pK[P->h_gpairs[s0.ket0]];
+                s.split = side == 0 ? grad_split(kbra, kket) : grad_split(kket, kbra);
+                s.warp0 = l.nwarps;
+                const int64_t qpw = 32 / s.split;
+                l.nwarps += (s.nq + qpw - 1) / qpw * G;
+                l.work += (double)s.nq * kbra * kket * ncart(ptype_la(tb)) * ncart(ptype_lb(tb)) *
+                          ncart(ptype_la(tk)) * ncart(ptype_lb(tk));
+                segs.push_back(s);
+            }
+            l.nseg = (int)segs.size() - l.seg0;
+            HF_CHECK(l.nwarps < ((int64_t)1 << 31), HFGPU_ERR_UNSUPPORTED, "gradient class too large");
+            launches.push_back(l);
+        }
+    }
+    DBuf<Seg> dsegs = to_device(segs, st);
+    // the launches are independent (their sums meet in atomics): spread them over
+    // the side streams, largest first, so that small classes fill the GPU
+    // around the large ones instead of each draining it alone
+    std::sort(launches.begin(), launches.end(),
+              [](const Launch& x, const Launch& y) { return x.work > y.work; });
     cudaEvent_t e0, e1;
     HF_CUDA(cudaEventCreate(&e0));
     HF_CUDA(cudaEventCreate(&e1));
     HF_CUDA(cudaEventRecord(e0, st));
-    for (int i = (int)P->classes.size() - 1; i >= 0; --i) {
-        const ClassPlan& c = P->classes[i];
-        if (c.nq == 0) continue;
+    ctx.fork();
+    int slot = 0;
+    for (const Launch& l : launches) {
+        cudaStream_t ls = ctx.aux[slot++ % Context::NAUX];
         GradArgs a;
         a.pA = P->dA.p; a.pB = P->dB.p; a.pK = P->dK.p;
-        a.snp = P->snp.p; a.sc0 = P->sc0.p; a.cfn0 = P->scf.p; a.comp_fn = P->cfn.p;
-        a.sat = dsat.p; a.coef = P->coef.p;
-        a.goff = dgoff.p; a.gp = gp.p; a.boys = ctx.boys;
+        a.poff = P->doff.p; a.pdata = P->pdata.p;
+        a.goff = dgoff.p; a.gdata = gd.p;
+        a.boys = ctx.boys;
         a.gpairs = P->gpairs.p; a.prefix = P->prefix.p;
-        a.segs = c.dsegs.p; a.nseg = (int)c.segs.size(); a.nq = c.nq;
-        a.herm = dherm.p; a.cartc = dcart.p;
-        a.P = dP; a.n = b.nbf; a.grad = d_grad;
-        a.la = ptype_la(c.tb); a.lb = ptype_lb(c.tb); a.lc = ptype_la(c.tk); a.ld = ptype_lb(c.tk);
-        const bool priv = grad_priv(a.la, a.lb, a.lc, a.ld);
-        int team = priv ? GRAD_PRIV_TEAM : grad_team(a.la, a.lb, a.lc, a.ld);
-        int smt = grad_smem_team(a.la, a.lb, a.lc, a.ld, priv, team);
-        while (!priv && team < 32 && (size_t)(GRAD_BLOCK / team) * smt * sizeof(double) > 200 * 1024) team <<= 1;
-        const size_t smem = (size_t)(GRAD_BLOCK / team) * smt * sizeof(double);
-        HF_CHECK(smem <= 200 * 1024, HFGPU_ERR_UNSUPPORTED, "gradient workspace exceeds shared memory");
-        a.team = team;
-        a.smem_team = smt;
-        const int64_t blocks = (c.nq * team + GRAD_BLOCK - 1) / GRAD_BLOCK;
-        if (priv) eri_grad_kernel<true><<<(unsigned)blocks, GRAD_BLOCK, smem, st>>>(a);
-        else eri_grad_kernel<false><<<(unsigned)blocks, GRAD_BLOCK, smem, st>>>(a);
+        a.segs = dsegs.p + l.seg0; a.nseg = l.nseg; a.nwarps = l.nwarps;
+        a.cfn0 = P->scf.p; a.comp_fn = P->cfn.p; a.sat = dsat.p;
+        a.P = dP; a.n = b.nbf; a.nat = nat;
+        a.gam_stride = l.gam;
+        a.grad = d_grad;
+        const size_t smem = ((size_t)l.gam * GRAD_BLK + 3 * (size_t)nat) * sizeof(double);
+        {
+            std::lock_guard<std::mutex> lk(g_smem_mu);
+            static std::vector<std::pair<GradKernelFn, size_t>> raised;
+            bool ok = false;
+            for (auto& r : raised)
+                if (r.first == l.fn && r.second >= smem) ok = true;
+            if (!ok && smem > 48 * 1024) {
+                HF_CUDA(cudaFuncSetAttribute(l.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
+                raised.push_back({l.fn, smem_max});
+            }
+        }
+        const int64_t blocks = (l.nwarps + GRAD_BLK / 32 - 1) / (GRAD_BLK / 32);
+        l.fn<<<(unsigned)blocks, GRAD_BLK, smem, ls>>>(a);
         count_launch();
         HF_CUDA(cudaGetLastError());
     }
+    ctx.join();
     HF_CUDA(cudaEventRecord(e1, st));
     HF_CUDA(cudaEventSynchronize(e1));
     float ms = 0;
@@ -764,6 +513,7 @@ void eri_gradient(Context& ctx, EriPlan* P, const double* dP, double* d_grad, fl
     cudaEventDestroy(e1);
     if (ms_out) *ms_out = ms;
 }
+
 
 void onee_gradient(Context& ctx, const Basis& b, int nat, const int* atno, const double* xyz, const double* dP,
                    const double* dW, double* d_grad)
@@ -826,7 +576,7 @@ __global__ void scale_occ_kernel(int n, int nocc, const double* __restrict__ C, 
 }
 
 void rhf_gradient(Context& ctx, EriPlan* plan, int natoms, const int* atno, const double* xyz, const double* dC,
-                  const double* dL, int nocc, double* grad, double* ms_grad)
+                  const double* dL, int nocc, double* grad, double* ms_grad, double* ms_grad_eri)
 {
     cudaStream_t st = ctx.stream;
     const Basis& b = plan->basis;
@@ -853,7 +603,8 @@ void rhf_gradient(Context& ctx, EriPlan* plan, int natoms, const int* atno, cons
     ctx.trace_mark("grad densities");
     onee_gradient(ctx, b, natoms, atno, xyz, dP.p, dW.p, dg.p);
     ctx.trace_mark("grad one-elec");
-    eri_gradient(ctx, plan, dP.p, dg.p, nullptr);
+    float ms_eri = 0;
+    eri_gradient(ctx, plan, dP.p, dg.p, &ms_eri);
     ctx.trace_mark("grad two-elec");
     std::vector<double> g((size_t)3 * natoms);
     dg.download(g.data(), g.size());
@@ -874,6 +625,7 @@ void rhf_gradient(Context& ctx, EriPlan* plan, int natoms, const int* atno, cons
         }
     for (size_t k = 0; k < g.size(); ++k) grad[k] = g[k];
     if (ms_grad) *ms_grad = ms;
+    if (ms_grad_eri) *ms_grad_eri = ms_eri;
 }
 
 }  // namespace hfgpu

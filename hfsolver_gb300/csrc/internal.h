@@ -240,7 +240,7 @@ void sad_guess(Context& ctx, int natoms, const int* atno, int nbf, double* dP0);
 // analytic RHF nuclear gradient (grad.cu) at converged orbitals dC, energies dL
 // (device, n x n and n); grad gets 3 values per atom (Ha/bohr), host memory
 void rhf_gradient(Context& ctx, EriPlan* plan, int natoms, const int* atno, const double* xyz, const double* dC,
-                  const double* dL, int nocc, double* grad, double* ms_grad);
+                  const double* dL, int nocc, double* grad, double* ms_grad, double* ms_grad_eri);
 
 // probe.cu: measured FP64 FMA rate (TFLOP/s)
 double probe_fp64_tflops(Context& ctx);

@@ -262,6 +262,7 @@ typedef struct {
     double block_elems;      /* component quartets a full Fock build digests (12 flops each) */
     double ms_tc_step1;      /* the tensor-core GEMMs over the packed integrals (transform step 1) */
     double n_tc_step1;       /* their launches */
+    double ms_grad_eri;      /* the two-electron part of ms_grad (the ERI gradient class kernels) */
 } hfgpu_result;
 
 void hfgpu_default_options(hfgpu_options *opt);

@@ -49,7 +49,7 @@ def test_struct_layouts(L):
     L.hfgpu_default_options(o)
     assert o.nscf == 40 and o.mix_alpha == 1.0 and o.tolE == 1e-10 and o.tolP == 1e-8
     assert ctypes.sizeof(_lib.Options) == 88  # int, 3 doubles, 2 ints, double, 2 ints, int[8]
-    assert ctypes.sizeof(_lib.Result) == 208  # 6 doubles, 4 ints, 3 int64, 15 doubles
+    assert ctypes.sizeof(_lib.Result) == 216  # 6 doubles, 4 ints, 3 int64, 16 doubles
 
 
 def test_basis_size(L):
