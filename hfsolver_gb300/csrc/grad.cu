@@ -170,23 +170,37 @@ __device__ static void boys_rt(int M, double T, double pref, double s, const dou
 // (the class kernels: grad_kernel.cuh and gen/grad_class_*.cu)
 
 // ------------------------------------------------------------- one-electron part
-struct OneArgs {
-    const int* lmn;  // 3 per function
-    const int* nprim;
-    const int* a0;
-    const int* c0;
-    const int* fatom;
-    const double* xyz;  // 3 per function
+// Two passes.  onee_grad_pair_kernel: one thread per primitive pair of a shell
+// pair adds the overlap and kinetic terms and leaves the nuclear-attraction
+// derivatives of all its component pairs folded into six Hermite densities,
+//   H_{A,k}(tau) = sum_ab w_ab c_a c_b (2a E^{a+1_k, b}_tau - a_k E^{a-1_k, b}_tau)
+//   H_{B,k}(tau) = sum_ab w_ab c_a c_b (2b E^{a, b+1_k}_tau - b_k E^{a, b-1_k}_tau)
+// (w = the density P counted for both triangle entries, |tau| <= l_A + l_B + 1).
+// onee_grad_nuc_kernel: one thread per (primitive pair, nucleus C) evaluates
+// R_tuv(p, P - C) once and contracts it with the six densities:
+//   dV/dA_k = -Z_C K 2pi/p sum_tau H_{A,k}(tau) R_tau (and B), and the
+// Hellmann-Feynman term of C is -(dV/dA + dV/dB).
+struct OnePairArgs {
+    const int* sL;
+    const int* snp;
+    const int* sp0;
+    const int* sc0;
+    const int* scf;
+    const int* satom;
+    const double* sxyz;
     const double* alpha;
     const double* coef;
-    int n, nat;
-    const int* Z;
-    const double* C;  // 3 per nucleus
-    const double* boys;
+    const int* comp_fn;
     const double* P;
     const double* W;
+    int n, nat;
+    const int4* items;  // (shell A, shell B, primitive pair, record offset in doubles)
+    int nitems;
+    double* rec;        // per primitive pair: header (8) + 6 densities of nherm(l_A + l_B + 1)
     double* grad;
 };
+
+constexpr int OG_HDR = 8;  // p, Px, Py, Pz, K 2pi/p, atom A, atom B, unused
 
 constexpr int OG_I = 4, OG_J = 6, OG_T = 9;  // i <= la+1, j <= lb+3, t <= i+j (only t <= 5 used)
 constexpr int OG_L = 5;                     // la + lb + 1
@@ -213,140 +227,165 @@ __device__ static void e1d_oe(double* E, int imax, int jmax, double xpa, double 
             }
 }
 
-// nuclei per block row: the grid's second dimension splits the nuclear-attraction
-// loop, so that a function pair's nuclei run in parallel (row 0 also does the
-// overlap and kinetic terms)
-constexpr int ONEE_GRAD_NUCLEI = 2;
-
-__global__ void onee_grad_kernel(OneArgs o)
+__global__ void onee_grad_pair_kernel(OnePairArgs o)
 {
     const double PI = 3.14159265358979323846;
     extern __shared__ double sg[];  // 3 per nucleus
     for (int k = threadIdx.x; k < 3 * o.nat; k += blockDim.x) sg[k] = 0.0;
     __syncthreads();
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int n = o.n;
-    if (idx < (int64_t)n * (n + 1) / 2) {
-        int i = (int)((sqrtf(8.0f * (float)idx + 1.0f) - 1.0f) * 0.5f);
-        while ((int64_t)i * (i + 1) / 2 > idx) --i;
-        while ((int64_t)(i + 1) * (i + 2) / 2 <= idx) ++i;
-        const int j = (int)(idx - (int64_t)i * (i + 1) / 2);
-        const double sym = (i == j) ? 1.0 : 2.0;
-        const double wP = sym * o.P[i + (int64_t)j * n], wW = sym * o.W[i + (int64_t)j * n];
-        const int la[3] = {o.lmn[3 * i], o.lmn[3 * i + 1], o.lmn[3 * i + 2]};
-        const int lb[3] = {o.lmn[3 * j], o.lmn[3 * j + 1], o.lmn[3 * j + 2]};
-        const double A[3] = {o.xyz[3 * i], o.xyz[3 * i + 1], o.xyz[3 * i + 2]};
-        const double B[3] = {o.xyz[3 * j], o.xyz[3 * j + 1], o.xyz[3 * j + 2]};
-        const double rab2 = (A[0] - B[0]) * (A[0] - B[0]) + (A[1] - B[1]) * (A[1] - B[1]) + (A[2] - B[2]) * (A[2] - B[2]);
-        double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0};
+    const int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it < o.nitems) {
+        const int4 item = o.items[it];
+        const int A = item.x, B = item.y;
+        const int la = o.sL[A], lb = o.sL[B];
+        const int npa = o.snp[A], npb = o.snp[B];
+        const int pa = item.z / npb, pb = item.z - pa * npb;
+        const double a = o.alpha[o.sp0[A] + pa], b = o.alpha[o.sp0[B] + pb];
+        const double Ax[3] = {o.sxyz[3 * A], o.sxyz[3 * A + 1], o.sxyz[3 * A + 2]};
+        const double Bx[3] = {o.sxyz[3 * B], o.sxyz[3 * B + 1], o.sxyz[3 * B + 2]};
+        const double p = a + b, ip = 1.0 / p;
+        double Pc[3], rab2 = 0.0;
         double E[3][OG_I * OG_J * OG_T];
-        for (int pa = 0; pa < o.nprim[i]; ++pa)
-            for (int pb = 0; pb < o.nprim[j]; ++pb) {
-                const double a = o.alpha[o.a0[i] + pa], b = o.alpha[o.a0[j] + pb];
-                const double cc = o.coef[o.c0[i] + pa] * o.coef[o.c0[j] + pb];
-                const double p = a + b, ip = 1.0 / p;
-                double Pc[3];
-                for (int k = 0; k < 3; ++k) {
-                    Pc[k] = (a * A[k] + b * B[k]) * ip;
-                    e1d_oe(E[k], la[k] + 1, lb[k] + 3, Pc[k] - A[k], Pc[k] - B[k], 0.5 * ip);
-                }
-                const double K = exp(-a * b * ip * rab2);
-                const double pre = cc * K * PI * ip * sqrt(PI * ip);
-                // 1-D overlap of powers (i, j) in direction k
-                auto s1 = [&](int k, int ii, int jj) -> double { return (ii < 0 || jj < 0) ? 0.0 : E[k][og(ii, jj, 0)]; };
-                // overlap and kinetic for bra powers q[] (cints.c:186-232 in 1-D overlaps)
-                auto st = [&](const int* q, double& s, double& t) {
-                    const double sx = s1(0, q[0], lb[0]), sy = s1(1, q[1], lb[1]), sz = s1(2, q[2], lb[2]);
-                    s = sx * sy * sz;
-                    double t0 = b * (2 * (lb[0] + lb[1] + lb[2]) + 3) * s;
-                    double t1 = -2 * b * b *
-                                (s1(0, q[0], lb[0] + 2) * sy * sz + sx * s1(1, q[1], lb[1] + 2) * sz +
-                                 sx * sy * s1(2, q[2], lb[2] + 2));
-                    double t2 = lb[0] * (lb[0] - 1) * s1(0, q[0], lb[0] - 2) * sy * sz +
-                                lb[1] * (lb[1] - 1) * sx * s1(1, q[1], lb[1] - 2) * sz +
-                                lb[2] * (lb[2] - 1) * sx * sy * s1(2, q[2], lb[2] - 2);
-                    t = t0 + t1 - 0.5 * t2;
+        for (int k = 0; k < 3; ++k) {
+            Pc[k] = (a * Ax[k] + b * Bx[k]) * ip;
+            rab2 += (Ax[k] - Bx[k]) * (Ax[k] - Bx[k]);
+            e1d_oe(E[k], la + 1, lb + 3, Pc[k] - Ax[k], Pc[k] - Bx[k], 0.5 * ip);
+        }
+        const double K = exp(-a * b * ip * rab2);
+        const double pre = K * PI * ip * sqrt(PI * ip);
+        const int L = la + lb + 1, nh = nherm(L);
+        double* h = o.rec + item.w;
+        h[0] = p;
+        h[1] = Pc[0];
+        h[2] = Pc[1];
+        h[3] = Pc[2];
+        h[4] = K * 2 * PI * ip;
+        h[5] = (double)o.satom[A];
+        h[6] = (double)o.satom[B];
+        h[7] = 0.0;
+        double* H = h + OG_HDR;
+        for (int k = 0; k < 6 * nh; ++k) H[k] = 0.0;
+        const int* fa = o.comp_fn + o.scf[A];
+        const int* fb = o.comp_fn + o.scf[B];
+        const double* coA = o.coef + o.sc0[A];
+        const double* coB = o.coef + o.sc0[B];
+        auto s1 = [&](int k, int ii, int jj) -> double { return (ii < 0 || jj < 0) ? 0.0 : E[k][og(ii, jj, 0)]; };
+        double gA[3] = {0, 0, 0};
+        for (int i = 0; i < ncart(la); ++i)
+            for (int j = 0; j < ncart(lb); ++j) {
+                if (A == B && i < j) continue;
+                const int x = fa[i], y = fb[j];
+                if (x < 0 || y < 0) continue;
+                const double sym = (A == B && i == j) ? 1.0 : 2.0;
+                const double cc = coA[i * npa + pa] * coB[j * npb + pb];
+                const double wP = sym * o.P[x + (int64_t)y * o.n], wW = sym * o.W[x + (int64_t)y * o.n];
+                const Cart ca = cart(la, i), cb = cart(lb, j);
+                const int qa[3] = {ca.l, ca.m, ca.n}, qb[3] = {cb.l, cb.m, cb.n};
+                // overlap and kinetic (cints.c:186-232 in terms of 1-D overlaps)
+                auto st = [&](const int* q, double& sv, double& tv) {
+                    const double sx = s1(0, q[0], qb[0]), sy = s1(1, q[1], qb[1]), sz = s1(2, q[2], qb[2]);
+                    sv = sx * sy * sz;
+                    const double t0 = b * (2 * (qb[0] + qb[1] + qb[2]) + 3) * sv;
+                    const double t1 = -2 * b * b *
+                                      (s1(0, q[0], qb[0] + 2) * sy * sz + sx * s1(1, q[1], qb[1] + 2) * sz +
+                                       sx * sy * s1(2, q[2], qb[2] + 2));
+                    const double t2 = qb[0] * (qb[0] - 1) * s1(0, q[0], qb[0] - 2) * sy * sz +
+                                      qb[1] * (qb[1] - 1) * sx * s1(1, q[1], qb[1] - 2) * sz +
+                                      qb[2] * (qb[2] - 1) * sx * sy * s1(2, q[2], qb[2] - 2);
+                    tv = t0 + t1 - 0.5 * t2;
                 };
-                for (int k = 0; k < 3 && blockIdx.y == 0; ++k) {
-                    int up[3] = {la[0], la[1], la[2]}, dn[3] = {la[0], la[1], la[2]};
+                for (int k = 0; k < 3; ++k) {
+                    int up[3] = {qa[0], qa[1], qa[2]}, dn[3] = {qa[0], qa[1], qa[2]};
                     up[k] += 1;
                     dn[k] -= 1;
                     double su, tu, sd = 0, td = 0;
                     st(up, su, tu);
-                    if (la[k] > 0) st(dn, sd, td);
-                    const double dS = pre * (2 * a * su - la[k] * sd);
-                    const double dT = pre * (2 * a * tu - la[k] * td);
-                    const double gk = wP * dT - wW * dS;
-                    gA[k] += gk;  // two-centre: d/dB = -d/dA
-                    gB[k] -= gk;
+                    if (qa[k] > 0) st(dn, sd, td);
+                    const double dS = pre * cc * (2 * a * su - qa[k] * sd);
+                    const double dT = pre * cc * (2 * a * tu - qa[k] * td);
+                    gA[k] += wP * dT - wW * dS;  // two-centre: d/dB = -d/dA
                 }
-                // nuclear attraction
-                const int L = la[0] + la[1] + la[2] + lb[0] + lb[1] + lb[2] + 1;
-                const double vpre = wP * cc * K * 2 * PI * ip;
-                const int c_end = min(o.nat, (int)(blockIdx.y + 1) * ONEE_GRAD_NUCLEI);
-                for (int c = blockIdx.y * ONEE_GRAD_NUCLEI; c < c_end; ++c) {
-                    const double X = Pc[0] - o.C[3 * c], Y = Pc[1] - o.C[3 * c + 1], Zc = Pc[2] - o.C[3 * c + 2];
-                    double F[OG_L + 1];
-                    boys_rt(L, p * (X * X + Y * Y + Zc * Zc), 1.0, -2.0 * p, o.boys, F);
-                    double R[OG_L + 1][nherm(OG_L)];
-                    for (int m = 0; m <= L; ++m) R[m][0] = F[m];
-                    for (int m = L - 1; m >= 0; --m)
-                        for (int s = 1; s <= L - m; ++s)
-                            for (int t = s; t >= 0; --t)
-                                for (int v = 0; v <= s - t; ++v) {
-                                    const int u = s - t - v;
-                                    double r;
-                                    if (t > 0) {
-                                        r = X * R[m + 1][hidx(t - 1, u, v)];
-                                        if (t > 1) r = fma((double)(t - 1), R[m + 1][hidx(t - 2, u, v)], r);
-                                    } else if (u > 0) {
-                                        r = Y * R[m + 1][hidx(0, u - 1, v)];
-                                        if (u > 1) r = fma((double)(u - 1), R[m + 1][hidx(0, u - 2, v)], r);
+                // nuclear attraction: the six Hermite densities
+                const double w = wP * cc;
+                for (int t = 0; t <= L; ++t)
+                    for (int u = 0; u <= L - t; ++u)
+                        for (int v = 0; v <= L - t - u; ++v) {
+                            const int hh = hidx(t, u, v);
+                            const int tt[3] = {t, u, v};
+                            for (int k = 0; k < 3; ++k) {
+                                // A: bra power qa[k] +- 1 along k; B: ket power qb[k] +- 1
+                                double eA = 1.0, eB = 1.0;
+                                for (int d = 0; d < 3; ++d) {
+                                    if (d == k) {
+                                        const double up = E[d][og(qa[d] + 1, qb[d], tt[d])];
+                                        const double dn = qa[d] > 0 ? E[d][og(qa[d] - 1, qb[d], tt[d])] : 0.0;
+                                        eA *= 2 * a * up - qa[d] * dn;
+                                        const double ub = E[d][og(qa[d], qb[d] + 1, tt[d])];
+                                        const double db = qb[d] > 0 ? E[d][og(qa[d], qb[d] - 1, tt[d])] : 0.0;
+                                        eB *= 2 * b * ub - qb[d] * db;
                                     } else {
-                                        r = Zc * R[m + 1][hidx(0, 0, v - 1)];
-                                        if (v > 1) r = fma((double)(v - 1), R[m + 1][hidx(0, 0, v - 2)], r);
+                                        const double e = E[d][og(qa[d], qb[d], tt[d])];
+                                        eA *= e;
+                                        eB *= e;
                                     }
-                                    R[m][hidx(t, u, v)] = r;
                                 }
-                    // Hermite sum for bra powers q[] and ket powers w[]
-                    auto hs = [&](const int* q, const int* w) -> double {
-                        if (q[0] < 0 || q[1] < 0 || q[2] < 0 || w[0] < 0 || w[1] < 0 || w[2] < 0) return 0.0;
-                        double acc = 0;
-                        for (int t = 0; t <= q[0] + w[0]; ++t)
-                            for (int u = 0; u <= q[1] + w[1]; ++u)
-                                for (int v = 0; v <= q[2] + w[2]; ++v)
-                                    acc += E[0][og(q[0], w[0], t)] * E[1][og(q[1], w[1], u)] * E[2][og(q[2], w[2], v)] *
-                                           R[0][hidx(t, u, v)];
-                        return acc;
-                    };
-                    const double zc = -(double)o.Z[c] * vpre;
-                    double hc[3];
-                    for (int k = 0; k < 3; ++k) {
-                        int up[3] = {la[0], la[1], la[2]}, dn[3] = {la[0], la[1], la[2]};
-                        up[k] += 1;
-                        dn[k] -= 1;
-                        const double dA = zc * (2 * a * hs(up, lb) - la[k] * hs(dn, lb));
-                        int ub[3] = {lb[0], lb[1], lb[2]}, db[3] = {lb[0], lb[1], lb[2]};
-                        ub[k] += 1;
-                        db[k] -= 1;
-                        const double dB = zc * (2 * b * hs(la, ub) - lb[k] * hs(la, db));
-                        gA[k] += dA;
-                        gB[k] += dB;
-                        hc[k] = -(dA + dB);  // Hellmann-Feynman term of nucleus c
-                    }
-                    for (int k = 0; k < 3; ++k)
-                        if (hc[k] != 0.0) atomicAdd(sg + 3 * c + k, hc[k]);
-                }
+                                H[k * nh + hh] += w * eA;
+                                H[(3 + k) * nh + hh] += w * eB;
+                            }
+                        }
             }
-        const int ai = o.fatom[i], aj = o.fatom[j];
+        const int ta = 3 * o.satom[A], tb = 3 * o.satom[B];
         for (int k = 0; k < 3; ++k) {
-            atomicAdd(sg + 3 * ai + k, gA[k]);
-            atomicAdd(sg + 3 * aj + k, gB[k]);
+            if (gA[k] != 0.0) {
+                atomicAdd(sg + ta + k, gA[k]);
+                atomicAdd(sg + tb + k, -gA[k]);
+            }
         }
     }
     __syncthreads();
     for (int k = threadIdx.x; k < 3 * o.nat; k += blockDim.x)
         if (sg[k] != 0.0) atomicAdd(o.grad + k, sg[k]);
+}
+
+template <int L>
+__global__ void __launch_bounds__(128) onee_grad_nuc_kernel(const double* __restrict__ rec, int nrec, int nat,
+                                                            const int* __restrict__ Z, const double* __restrict__ C,
+                                                            const double* __restrict__ boys, double* grad)
+{
+    constexpr int NH = nherm(L);
+    extern __shared__ double sg[];  // 3 per nucleus
+    for (int k = threadIdx.x; k < 3 * nat; k += blockDim.x) sg[k] = 0.0;
+    __syncthreads();
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < (int64_t)nrec * nat) {
+        const int r = (int)(idx / nat), c = (int)(idx - (int64_t)r * nat);
+        const double* h = rec + (int64_t)r * (OG_HDR + 6 * NH);
+        const double p = __ldg(h);
+        const double X = __ldg(h + 1) - C[3 * c], Y = __ldg(h + 2) - C[3 * c + 1], Zc = __ldg(h + 3) - C[3 * c + 2];
+        double F[L + 1];
+        boys_scaled<L>(p * (X * X + Y * Y + Zc * Zc), 1.0, -2.0 * p, boys, F);
+        double R[NH];
+        r_ct<L>(R, F, X, Y, Zc);
+        const double zc = -(double)Z[c] * __ldg(h + 4);
+        const int ta = 3 * (int)__ldg(h + 5), tb = 3 * (int)__ldg(h + 6);
+        const double* H = h + OG_HDR;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double sA = 0.0, sB = 0.0;
+#pragma unroll
+            for (int t = 0; t < NH; ++t) {
+                sA = fma(__ldg(H + k * NH + t), R[t], sA);
+                sB = fma(__ldg(H + (3 + k) * NH + t), R[t], sB);
+            }
+            const double dA = zc * sA, dB = zc * sB;
+            atomicAdd(sg + ta + k, dA);
+            atomicAdd(sg + tb + k, dB);
+            atomicAdd(sg + 3 * c + k, -(dA + dB));
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 3 * nat; k += blockDim.x)
+        if (sg[k] != 0.0) atomicAdd(grad + k, sg[k]);
 }
 
 // ------------------------------------------------------------- host side
@@ -520,47 +559,83 @@ void onee_gradient(Context& ctx, const Basis& b, int nat, const int* atno, const
 {
     cudaStream_t st = ctx.stream;
     const int n = b.nbf;
-    std::vector<int> lmn(3 * n), np(n), a0(n), c0(n), fat(n);
-    std::vector<double> fx(3 * n);
-    for (auto& sh : b.shells) {
+    const int ns = (int)b.shells.size();
+    std::vector<int> sL(ns), snp(ns), sp0(ns), sc0(ns), scf(ns), sat(ns);
+    std::vector<double> sxyz(3 * ns);
+    for (int s = 0; s < ns; ++s) {
+        const Shell& sh = b.shells[s];
         HF_CHECK(sh.atom >= 0, HFGPU_ERR_UNSUPPORTED, "gradient needs a basis built from atoms");
-        for (int c = 0; c < ncart(sh.L); c++) {
-            const int fn = b.comp_fn[sh.cfn0 + c];
-            if (fn < 0) continue;
-            const Cart cc = cart(sh.L, c);
-            lmn[3 * fn] = cc.l; lmn[3 * fn + 1] = cc.m; lmn[3 * fn + 2] = cc.n;
-            np[fn] = sh.nprim;
-            a0[fn] = sh.prim0;
-            c0[fn] = sh.coef0 + c * sh.nprim;
-            fat[fn] = sh.atom;
-            fx[3 * fn] = sh.x; fx[3 * fn + 1] = sh.y; fx[3 * fn + 2] = sh.z;
+        HF_CHECK(sh.L <= 2, HFGPU_ERR_UNSUPPORTED, "gradient supports s, p and d shells");
+        sL[s] = sh.L; snp[s] = sh.nprim; sp0[s] = sh.prim0; sc0[s] = sh.coef0; scf[s] = sh.cfn0; sat[s] = sh.atom;
+        sxyz[3 * s] = sh.x; sxyz[3 * s + 1] = sh.y; sxyz[3 * s + 2] = sh.z;
+    }
+    // primitive pairs grouped by L = l_A + l_B + 1 (the order of R), records consecutive per group
+    constexpr int NL = 6;  // L = 1 .. 5
+    std::vector<int4> items[NL];
+    for (int s1 = 0; s1 < ns; ++s1)
+        for (int s2 = 0; s2 <= s1; ++s2) {
+            const int A = sL[s1] >= sL[s2] ? s1 : s2, B = A == s1 ? s2 : s1;
+            const int L = sL[A] + sL[B] + 1;
+            for (int k = 0; k < snp[A] * snp[B]; ++k) items[L].push_back(make_int4(A, B, k, 0));
+        }
+    std::vector<int4> all;
+    int64_t off = 0;
+    int64_t goff[NL + 1] = {}, gcount[NL] = {};
+    for (int L = 1; L < NL; ++L) {
+        goff[L] = off;
+        gcount[L] = (int64_t)items[L].size();
+        for (auto& it : items[L]) {
+            it.w = (int)off;
+            off += OG_HDR + 6 * nherm(L);
+            all.push_back(it);
         }
     }
+    HF_CHECK(off < ((int64_t)1 << 31), HFGPU_ERR_UNSUPPORTED, "one-electron gradient records exceed 2^31 doubles");
     std::vector<int> Z(nat);
     std::vector<double> C(3 * nat);
     for (int i = 0; i < nat; i++) {
         Z[i] = atno[i];
         for (int k = 0; k < 3; ++k) C[3 * i + k] = xyz[3 * i + k];
     }
-    auto dl = to_device(lmn, st);
-    auto dn = to_device(np, st);
-    auto da = to_device(a0, st);
-    auto dc = to_device(c0, st);
-    auto dfa = to_device(fat, st);
-    auto dx = to_device(fx, st);
-    auto dal = to_device(b.alpha, st);
-    auto dco = to_device(b.coef, st);
-    auto dZ = to_device(Z, st);
-    auto dC = to_device(C, st);
-    OneArgs o{dl.p, dn.p, da.p, dc.p, dfa.p, dx.p, dal.p, dco.p, n, nat, dZ.p, dC.p, ctx.boys, dP, dW, d_grad};
-    const int64_t npair = (int64_t)n * (n + 1) / 2;
     const size_t smem = (size_t)3 * nat * sizeof(double);
     HF_CHECK(smem <= 48 * 1024, HFGPU_ERR_UNSUPPORTED, "too many atoms for the one-electron gradient kernel");
-    const dim3 grid((unsigned)((npair + 127) / 128), (unsigned)((nat + ONEE_GRAD_NUCLEI - 1) / ONEE_GRAD_NUCLEI));
-    onee_grad_kernel<<<grid, 128, smem, st>>>(o);
-    count_launch();
-    HF_CUDA(cudaGetLastError());
-    HF_CUDA(cudaStreamSynchronize(st));
+    auto dL = to_device(sL, st);
+    auto dn = to_device(snp, st);
+    auto dp0 = to_device(sp0, st);
+    auto dc0 = to_device(sc0, st);
+    auto dcf = to_device(scf, st);
+    auto dat = to_device(sat, st);
+    auto dxyz = to_device(sxyz, st);
+    auto dal = to_device(b.alpha, st);
+    auto dco = to_device(b.coef, st);
+    auto dfn = to_device(b.comp_fn, st);
+    auto dit = to_device(all, st);
+    auto dZ = to_device(Z, st);
+    auto dC = to_device(C, st);
+    DBuf<double> rec((size_t)std::max<int64_t>(off, 1), st);
+    OnePairArgs o{dL.p, dn.p, dp0.p, dc0.p, dcf.p, dat.p, dxyz.p, dal.p, dco.p, dfn.p, dP, dW, n, nat,
+                  dit.p, (int)all.size(), rec.p, d_grad};
+    if (o.nitems > 0) {
+        onee_grad_pair_kernel<<<(unsigned)((o.nitems + 127) / 128), 128, smem, st>>>(o);
+        count_launch();
+        HF_CUDA(cudaGetLastError());
+    }
+    for (int L = 1; L < NL; ++L) {
+        const int64_t nth = gcount[L] * nat;
+        if (nth == 0) continue;
+        const unsigned blocks = (unsigned)((nth + 127) / 128);
+        const double* r0 = rec.p + goff[L];
+        const int nr = (int)gcount[L];
+        switch (L) {
+            case 1: onee_grad_nuc_kernel<1><<<blocks, 128, smem, st>>>(r0, nr, nat, dZ.p, dC.p, ctx.boys, d_grad); break;
+            case 2: onee_grad_nuc_kernel<2><<<blocks, 128, smem, st>>>(r0, nr, nat, dZ.p, dC.p, ctx.boys, d_grad); break;
+            case 3: onee_grad_nuc_kernel<3><<<blocks, 128, smem, st>>>(r0, nr, nat, dZ.p, dC.p, ctx.boys, d_grad); break;
+            case 4: onee_grad_nuc_kernel<4><<<blocks, 128, smem, st>>>(r0, nr, nat, dZ.p, dC.p, ctx.boys, d_grad); break;
+            default: onee_grad_nuc_kernel<5><<<blocks, 128, smem, st>>>(r0, nr, nat, dZ.p, dC.p, ctx.boys, d_grad); break;
+        }
+        count_launch();
+        HF_CUDA(cudaGetLastError());
+    }
 }
 
 }  // namespace hfgpu

@@ -63,39 +63,6 @@ __device__ __forceinline__ void e1d_ct(double (&E)[IA + 1][JB + 1][IA + JB + 1],
             }
 }
 
-// R_tuv(p, PC) for t+u+v <= L (Helgaker et al. eqs. 9.9.18-9.9.20), compile-time L
-template <int L>
-__device__ __forceinline__ void r_ct(double (&R)[nherm(L)], const double (&F)[L + 1], double X, double Y, double Z)
-{
-    double Rn[L + 1][nherm(L)];
-#pragma unroll
-    for (int n = 0; n <= L; ++n) Rn[n][0] = F[n];
-#pragma unroll
-    for (int n = L - 1; n >= 0; --n)
-#pragma unroll
-        for (int s = 1; s <= L - n; ++s)
-#pragma unroll
-            for (int t = s; t >= 0; --t)
-#pragma unroll
-                for (int v = 0; v <= s - t; ++v) {
-                    const int u = s - t - v;
-                    double r;
-                    if (t > 0) {
-                        r = X * Rn[n + 1][hidx(t - 1, u, v)];
-                        if (t > 1) r = fma((double)(t - 1), Rn[n + 1][hidx(t - 2, u, v)], r);
-                    } else if (u > 0) {
-                        r = Y * Rn[n + 1][hidx(0, u - 1, v)];
-                        if (u > 1) r = fma((double)(u - 1), Rn[n + 1][hidx(0, u - 2, v)], r);
-                    } else {
-                        r = Z * Rn[n + 1][hidx(0, 0, v - 1)];
-                        if (v > 1) r = fma((double)(v - 1), Rn[n + 1][hidx(0, 0, v - 2)], r);
-                    }
-                    Rn[n][hidx(t, u, v)] = r;
-                }
-#pragma unroll
-    for (int h = 0; h < nherm(L); ++h) R[h] = Rn[0][h];
-}
-
 // blockIdx.y = a chunk of ONEE_ATOMS nuclei: chunk 0 also writes S and T; every
 // chunk adds its nuclei's attraction to V (zeroed by the caller) atomically.
 constexpr int ONEE_ATOMS = 4;
