@@ -491,12 +491,27 @@ __global__ void shell_dmax_kernel(int ns, const int* __restrict__ L, const int* 
     Dm[idx] = m;
 }
 
+// quartets a warp screens before digesting the survivors: one pass when nothing
+// is screened; with a screen, up to 8 passes as long as the class still has
+// about 16 warps per SM
+static int digest_rounds(const Context& ctx, const ClassPlan& c, int split, bool screened)
+{
+    if (!screened) return 1;
+    const int64_t warps1 = (c.nq * split + 31) / 32;
+    int r = 1;
+    while (r < 8 && warps1 / (2 * r) >= (int64_t)ctx.num_sms * 16) r *= 2;
+    return r;
+}
+
 static void launch_digest(const ClassPlan& c, const DigestArgs& a, cudaStream_t s)
 {
+    const int64_t qpw = (int64_t)(32 / a.split) * a.rounds;
+    const int64_t warps = (c.nq + qpw - 1) / qpw;
+    const unsigned blocks = (unsigned)((warps + 3) / 4);
     if (a.split == 1)
-        digest_fn(c.tb, c.tk)<<<(unsigned)((c.nq + 127) / 128), 128, 0, s>>>(a);
+        digest_fn(c.tb, c.tk)<<<blocks, 128, 0, s>>>(a);
     else
-        digest_wide_fn(c.tb, c.tk)<<<(unsigned)((c.nq * a.split + 127) / 128), 128, 0, s>>>(a);
+        digest_wide_fn(c.tb, c.tk)<<<blocks, 128, 0, s>>>(a);
     count_launch();
     HF_CUDA(cudaGetLastError());
 }
@@ -520,6 +535,7 @@ static int digest_split_tuned(Context& ctx, const ClassPlan& c, DigestArgs a, in
     float best = 1e30f;
     for (int cand = 1; cand <= 32 && (cand == 1 || cand / 2 < nab); cand <<= 1) {
         a.split = cand;
+        a.rounds = digest_rounds(ctx, c, cand, a.screen > 0);
         HF_CUDA(cudaEventRecord(e0, ctx.stream));
         launch_digest(c, a, ctx.stream);
         HF_CUDA(cudaEventRecord(e1, ctx.stream));
@@ -588,7 +604,9 @@ void eri_digest(Context& ctx, EriPlan* P, const double* dP, double* dG, double s
         a.mol_sh0 = nullptr;
         a.qlist = P->qlist.p ? P->qlist.p + c.qbase : nullptr;
         a.pair_mol = nullptr;
+        a.rounds = 1;
         a.split = digest_split_tuned(ctx, c, a, nn);
+        a.rounds = digest_rounds(ctx, c, a.split, screen > 0);
         cudaStream_t s = ctx.aux[slot++ % Context::NAUX];
         launch_digest(c, a, s);
     }
@@ -967,6 +985,8 @@ static void batch_digest_launches(Context& ctx, EriPlan* P, BatchDigest& t, cuda
         int split = digest_split(c);
         if (ctx.tune) tune_get(TUNE_DIGEST, c.tb, c.tk, tune_bucket(c.nq), &split);
         a.split = split;
+        // captured once for all builds, screened or not
+        a.rounds = digest_rounds(ctx, c, split, true);
         launch_digest(c, a, ctx.aux[slot++ % Context::NAUX]);
     }
     for (int i = 0; i < Context::NAUX; ++i) {

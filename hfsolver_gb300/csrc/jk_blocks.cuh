@@ -32,7 +32,8 @@ struct DigestArgs {
     const double* P;
     int n;
     double* Gh;
-    int split;  // lanes per quartet (digest_wide_kernel; a power of two <= 32)
+    int split;   // lanes per quartet (digest_wide_kernel; a power of two <= 32)
+    int rounds;  // a warp screens rounds x (32 / split) quartets and digests the survivors (1 to 8)
     // density-difference screening (screen > 0): pair Schwarz bounds Q and the
     // largest |P| element of each shell pair, Dm[S1 * ns + S2]
     double screen;
@@ -133,19 +134,48 @@ __device__ __forceinline__ bool digest_skip(const DigestArgs& a, const DigestMol
     return a.Q[bra] * a.Q[ket] * fmax(2.0 * dj, 0.5 * dk) < m.screen;
 }
 
+// v != 0 tested on the bit pattern (integer pipe; -0 counts as zero)
+__device__ __forceinline__ bool digest_nonzero(double v) { return (__double_as_longlong(v) << 1) != 0; }
+
+constexpr int DIGEST_MAX_Q = 256;  // quartets screened per warp: 32 x 8 rounds
+
+// Screen the warp's quartets q0 .. q0 + cnt - 1 (density-difference screen,
+// molecules not in this build) and leave the offsets of the survivors in the
+// warp's list; returns their number.  The survivors are then digested in full
+// warps, instead of each warp idling on the lanes whose quartets were skipped.
+__device__ __forceinline__ int digest_compact(const DigestArgs& a, int64_t q0, int cnt, int* list, int lane)
+{
+    int ns = 0;
+    for (int r = 0; r < cnt; r += 32) {
+        const int k = r + lane;
+        const int64_t qg = q0 + k;
+        bool keep = false;
+        if (k < cnt && qg < a.nq) {
+            int bra, ket, mol;
+            digest_quartet(a, qg, bra, ket, mol);
+            DigestMol mm;
+            if (digest_mol(a, mol, mm))
+                keep = !digest_skip(a, mm, bra, ket, a.pr.A[bra], a.pr.B[bra], a.pr.A[ket], a.pr.B[ket]);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) list[ns + __popc(m & ((1u << lane) - 1u))] = k;
+        ns += __popc(m);
+    }
+    __syncwarp();
+    return ns;
+}
+
+// one thread digests one whole quartet (already screened)
 template <int TB, int TK>
-__global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
+__device__ __forceinline__ void digest_one(const DigestArgs& a, int64_t qg)
 {
     using CI = ClassInfo<TB, TK>;
     constexpr int NA = ncart(CI::LA), NB = ncart(CI::LB), NC = ncart(CI::LC), ND = ncart(CI::LD);
-    const int64_t qg = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (qg >= a.nq) return;
     int bra, ket, mol;
     digest_quartet(a, qg, bra, ket, mol);
     DigestMol mm;
-    if (!digest_mol(a, mol, mm)) return;
+    digest_mol(a, mol, mm);
     const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
-    if (digest_skip(a, mm, bra, ket, A, B, C, D)) return;
     int fa[NA], fb[NB], fc[NC], fd[ND];
 #pragma unroll
     for (int i = 0; i < NA; ++i) fa[i] = a.sh.comp_fn[a.sh.cfn0[A] + i];
@@ -159,12 +189,13 @@ __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
     const double* Pm = mm.P;
     auto Pv = [&](int x, int y) { return (x < 0 || y < 0) ? 0.0 : __ldg(Pm + x + (int64_t)y * n); };
     const double f = (A == B ? 0.5 : 1.0) * (C == D ? 0.5 : 1.0) * (bra == ket ? 0.5 : 1.0);
-    // accumulators indexed by the rolled (a, b) loop live in local memory and are
-    // touched once per (a, b); everything indexed by (c, d) stays in registers
+    // every output is multiplied once by its weight (J: 2f, K: -f/2) instead of
+    // every integral by f: on this GPU each FP64 instruction is as dear as an FMA
+    const double cj = 2.0 * f, ck = -0.5 * f;
+    // accumulators indexed by the rolled (a, b) loop live in local memory; each
+    // FMA chain starts from the stored partial sum, so no separate FP64 adds
     double jab[NA * NB], kac[NA * NC], kbc[NB * NC], kad[NA * ND], kbd[NB * ND];
     double jcd[NC * ND], Pcd[NC * ND];
-#pragma unroll
-    for (int i = 0; i < NA * NB; ++i) jab[i] = 0.0;
 #pragma unroll
     for (int i = 0; i < NA * NC; ++i) kac[i] = 0.0;
 #pragma unroll
@@ -198,14 +229,17 @@ __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
             }
             double s_ab = 0.0, s_ad[ND], s_bd[ND];
 #pragma unroll
-            for (int id = 0; id < ND; ++id) s_ad[id] = s_bd[id] = 0.0;
+            for (int id = 0; id < ND; ++id) {
+                s_ad[id] = kad[ia * ND + id];
+                s_bd[id] = kbd[ib * ND + id];
+            }
             const double* blk = a.blocks + (int64_t)((ia * NB + ib) * CI::NCDT) * a.nq + qg;
 #pragma unroll
             for (int ic = 0; ic < NC; ++ic) {
-                double s_ac = 0.0, s_bc = 0.0;
+                double s_ac = kac[ia * NC + ic], s_bc = kbc[ib * NC + ic];
 #pragma unroll
                 for (int id = 0; id < ND; ++id) {
-                    const double v = __ldg(blk + (int64_t)(ic * ND + id) * a.nq) * f;
+                    const double v = __ldg(blk + (int64_t)(ic * ND + id) * a.nq);
                     s_ab = fma(v, Pcd[ic * ND + id], s_ab);
                     jcd[ic * ND + id] = fma(v, Pab, jcd[ic * ND + id]);
                     s_ac = fma(v, Pbd[id], s_ac);
@@ -213,38 +247,56 @@ __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
                     s_ad[id] = fma(v, Pbc[ic], s_ad[id]);
                     s_bd[id] = fma(v, Pac[ic], s_bd[id]);
                 }
-                kac[ia * NC + ic] += s_ac;
-                kbc[ib * NC + ic] += s_bc;
+                kac[ia * NC + ic] = s_ac;
+                kbc[ib * NC + ic] = s_bc;
             }
-            jab[ia * NB + ib] += s_ab;
+            jab[ia * NB + ib] = s_ab;
 #pragma unroll
             for (int id = 0; id < ND; ++id) {
-                kad[ia * ND + id] += s_ad[id];
-                kbd[ib * ND + id] += s_bd[id];
+                kad[ia * ND + id] = s_ad[id];
+                kbd[ib * ND + id] = s_bd[id];
             }
         }
     double* Gh = mm.Gh;
     auto add = [&](int x, int y, double v) {
-        if (x >= 0 && y >= 0 && v != 0.0) atomicAdd(Gh + x + (int64_t)y * n, v);
+        if (x >= 0 && y >= 0 && digest_nonzero(v)) atomicAdd(Gh + x + (int64_t)y * n, v);
     };
 #pragma unroll 1
     for (int ia = 0; ia < NA; ++ia)
-        for (int ib = 0; ib < NB; ++ib) add(fa[ia], fb[ib], 2.0 * jab[ia * NB + ib]);
+        for (int ib = 0; ib < NB; ++ib) add(fa[ia], fb[ib], cj * jab[ia * NB + ib]);
 #pragma unroll 1
     for (int ic = 0; ic < NC; ++ic)
-        for (int id = 0; id < ND; ++id) add(fc[ic], fd[id], 2.0 * jcd[ic * ND + id]);
+        for (int id = 0; id < ND; ++id) add(fc[ic], fd[id], cj * jcd[ic * ND + id]);
 #pragma unroll 1
     for (int ia = 0; ia < NA; ++ia)
-        for (int ic = 0; ic < NC; ++ic) add(fa[ia], fc[ic], -0.5 * kac[ia * NC + ic]);
+        for (int ic = 0; ic < NC; ++ic) add(fa[ia], fc[ic], ck * kac[ia * NC + ic]);
 #pragma unroll 1
     for (int ib = 0; ib < NB; ++ib)
-        for (int ic = 0; ic < NC; ++ic) add(fb[ib], fc[ic], -0.5 * kbc[ib * NC + ic]);
+        for (int ic = 0; ic < NC; ++ic) add(fb[ib], fc[ic], ck * kbc[ib * NC + ic]);
 #pragma unroll 1
     for (int ia = 0; ia < NA; ++ia)
-        for (int id = 0; id < ND; ++id) add(fa[ia], fd[id], -0.5 * kad[ia * ND + id]);
+        for (int id = 0; id < ND; ++id) add(fa[ia], fd[id], ck * kad[ia * ND + id]);
 #pragma unroll 1
     for (int ib = 0; ib < NB; ++ib)
-        for (int id = 0; id < ND; ++id) add(fb[ib], fd[id], -0.5 * kbd[ib * ND + id]);
+        for (int id = 0; id < ND; ++id) add(fb[ib], fd[id], ck * kbd[ib * ND + id]);
+}
+
+template <int TB, int TK>
+__global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
+{
+    __shared__ int sl[4][DIGEST_MAX_Q];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int qpw = 32 * a.rounds;
+    const int64_t q0 = ((int64_t)blockIdx.x * 4 + warp) * qpw;
+    if (q0 >= a.nq) return;  // the whole warp
+    if (a.screen <= 0.0 && !a.mol_n) {  // nothing is screened: no list
+        for (int k = lane; k < qpw; k += 32)
+            if (q0 + k < a.nq) digest_one<TB, TK>(a, q0 + k);
+        return;
+    }
+    const int ns = digest_compact(a, q0, qpw, sl[warp], lane);
+    for (int base = 0; base < ns; base += 32)
+        if (base + lane < ns) digest_one<TB, TK>(a, q0 + sl[warp][base + lane]);
 }
 
 // The same Fock contribution with `split` lanes per quartet, for classes with
@@ -253,23 +305,15 @@ __global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
 // each row's J_ab and K contributions straight to Gh, and sum their partial
 // J_cd with warp shuffles before one lane per (c, d) adds it.
 template <int TB, int TK>
-__global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
+__device__ __forceinline__ void digest_wide_one(const DigestArgs& a, int64_t qg, int split, int sub, unsigned mask)
 {
     using CI = ClassInfo<TB, TK>;
     constexpr int NA = ncart(CI::LA), NB = ncart(CI::LB), NC = ncart(CI::LC), ND = ncart(CI::LD);
-    const int split = a.split;
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int sub = (int)(tid & (split - 1));
-    const unsigned lane = threadIdx.x & 31;
-    const unsigned mask = split == 32 ? 0xffffffffu : (((1u << split) - 1u) << (lane & ~(unsigned)(split - 1)));
-    const int64_t qg = tid / split;
-    if (qg >= a.nq) return;  // all lanes of a quartet leave together
     int bra, ket, mol;
     digest_quartet(a, qg, bra, ket, mol);
     DigestMol mm;
-    if (!digest_mol(a, mol, mm)) return;  // same answer for all lanes of the quartet
+    digest_mol(a, mol, mm);
     const int A = a.pr.A[bra], B = a.pr.B[bra], C = a.pr.A[ket], D = a.pr.B[ket];
-    if (digest_skip(a, mm, bra, ket, A, B, C, D)) return;  // same answer for all lanes of the quartet
     int fc[NC], fd[ND];
 #pragma unroll
     for (int i = 0; i < NC; ++i) fc[i] = a.sh.comp_fn[a.sh.cfn0[C] + i];
@@ -282,9 +326,10 @@ __global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
     auto Pv = [&](int x, int y) { return (x < 0 || y < 0) ? 0.0 : __ldg(Pm + x + (int64_t)y * n); };
     double* Gh = mm.Gh;
     auto add = [&](int x, int y, double v) {
-        if (x >= 0 && y >= 0 && v != 0.0) atomicAdd(Gh + x + (int64_t)y * n, v);
+        if (x >= 0 && y >= 0 && digest_nonzero(v)) atomicAdd(Gh + x + (int64_t)y * n, v);
     };
     const double f = (A == B ? 0.5 : 1.0) * (C == D ? 0.5 : 1.0) * (bra == ket ? 0.5 : 1.0);
+    const double cj = 2.0 * f, ck = -0.5 * f;
     double jcd[NC * ND], Pcd[NC * ND];
 #pragma unroll
     for (int ic = 0; ic < NC; ++ic)
@@ -318,7 +363,7 @@ __global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
             double s_ac = 0.0, s_bc = 0.0;
 #pragma unroll
             for (int id = 0; id < ND; ++id) {
-                const double v = __ldg(blk + (int64_t)(ic * ND + id) * a.nq) * f;
+                const double v = __ldg(blk + (int64_t)(ic * ND + id) * a.nq);
                 s_ab = fma(v, Pcd[ic * ND + id], s_ab);
                 jcd[ic * ND + id] = fma(v, Pab, jcd[ic * ND + id]);
                 s_ac = fma(v, Pbd[id], s_ac);
@@ -326,14 +371,14 @@ __global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
                 s_ad[id] = fma(v, Pbc[ic], s_ad[id]);
                 s_bd[id] = fma(v, Pac[ic], s_bd[id]);
             }
-            add(xa, fc[ic], -0.5 * s_ac);
-            add(xb, fc[ic], -0.5 * s_bc);
+            add(xa, fc[ic], ck * s_ac);
+            add(xb, fc[ic], ck * s_bc);
         }
-        add(xa, xb, 2.0 * s_ab);
+        add(xa, xb, cj * s_ab);
 #pragma unroll
         for (int id = 0; id < ND; ++id) {
-            add(xa, fd[id], -0.5 * s_ad[id]);
-            add(xb, fd[id], -0.5 * s_bd[id]);
+            add(xa, fd[id], ck * s_ad[id]);
+            add(xb, fd[id], ck * s_bd[id]);
         }
     }
     for (int o = split >> 1; o > 0; o >>= 1)
@@ -341,7 +386,32 @@ __global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
         for (int i = 0; i < NC * ND; ++i) jcd[i] += __shfl_xor_sync(mask, jcd[i], o);
 #pragma unroll
     for (int i = 0; i < NC * ND; ++i)
-        if ((i & (split - 1)) == sub) add(fc[i / ND], fd[i % ND], 2.0 * jcd[i]);
+        if ((i & (split - 1)) == sub) add(fc[i / ND], fd[i % ND], cj * jcd[i]);
+}
+
+template <int TB, int TK>
+__global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
+{
+    __shared__ int sl[4][DIGEST_MAX_Q];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int split = a.split, per = 32 / split;
+    const int qpw = per * a.rounds;
+    const int64_t q0 = ((int64_t)blockIdx.x * 4 + warp) * qpw;
+    if (q0 >= a.nq) return;  // the whole warp
+    const int sub = lane & (split - 1);
+    const unsigned mask = split == 32 ? 0xffffffffu : (((1u << split) - 1u) << (lane & ~(unsigned)(split - 1)));
+    if (a.screen <= 0.0 && !a.mol_n) {  // nothing is screened: no list
+        for (int base = 0; base < qpw; base += per) {
+            const int64_t qg = q0 + base + lane / split;  // the same for all lanes of a quartet
+            if (qg < a.nq) digest_wide_one<TB, TK>(a, qg, split, sub, mask);
+        }
+        return;
+    }
+    const int ns = digest_compact(a, q0, qpw, sl[warp], lane);
+    for (int base = 0; base < ns; base += per) {
+        const int k = base + lane / split;  // the same for all lanes of a quartet
+        if (k < ns) digest_wide_one<TB, TK>(a, q0 + sl[warp][k], split, sub, mask);
+    }
 }
 
 using DigestFn = void (*)(DigestArgs);
