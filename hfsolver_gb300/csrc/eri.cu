@@ -196,7 +196,7 @@ double md_flops(int la, int lb, int lc, int ld)
 }
 
 static void launch_class(Context& ctx, EriPlan* P, ClassPlan& c, int mode, double* out, const int2* list,
-                         double* blocks = nullptr)
+                         double* blocks = nullptr, cudaStream_t on = nullptr)
 {
     if (c.nwarps == 0) return;
     EriArgs a;
@@ -215,7 +215,7 @@ static void launch_class(Context& ctx, EriPlan* P, ClassPlan& c, int mode, doubl
     a.nwarps = c.nwarps;
     a.out = out;
     const int64_t nblocks = (c.nwarps + ERI_BLOCK / 32 - 1) / (ERI_BLOCK / 32);
-    get_kernel(c.tb, c.tk, mode)<<<(unsigned)nblocks, ERI_BLOCK, 0, ctx.stream>>>(a);
+    get_kernel(c.tb, c.tk, mode)<<<(unsigned)nblocks, ERI_BLOCK, 0, on ? on : ctx.stream>>>(a);
     count_launch();
     HF_CUDA(cudaGetLastError());
 }
@@ -650,7 +650,9 @@ static void layout_class(Context& ctx, ClassPlan& c, int target)
 // first molecule of a (class, size bucket) with tuning on, every candidate
 // target is timed on the real launch (the class writes the same values each
 // time) and the fastest is recorded.
-static void eri_class_tuned(Context& ctx, EriPlan* P, ClassPlan& c, double* d_out, double* blocks)
+// the class's lanes-per-quartet layout: tuned once per (class, size bucket) by
+// timing the candidates on the main stream, then laid out for the winner
+static void eri_class_layout(Context& ctx, EriPlan* P, ClassPlan& c, double* d_out, double* blocks)
 {
     int target = 16;
     if (ctx.tune && c.nq > 0) {
@@ -677,7 +679,6 @@ static void eri_class_tuned(Context& ctx, EriPlan* P, ClassPlan& c, double* d_ou
         }
     }
     if (c.lane_target != target) layout_class(ctx, c, target);
-    launch_class(ctx, P, c, MODE_PACKED, d_out, nullptr, blocks);
 }
 
 void eri_compute(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks, EriStats* st)
@@ -699,9 +700,19 @@ void eri_compute(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks, EriS
     HF_CUDA(cudaEventCreate(&e0));
     HF_CUDA(cudaEventCreate(&e1));
     HF_CUDA(cudaEventRecord(e0, ctx.stream));
-    // heaviest classes first so the tail of the launch sequence is short
     for (int i = (int)P->classes.size() - 1; i >= 0; --i)
-        eri_class_tuned(ctx, P, P->classes[i], d_out, keep_blocks ? P->blocks.p + P->classes[i].boff : nullptr);
+        eri_class_layout(ctx, P, P->classes[i], d_out, keep_blocks ? P->blocks.p + P->classes[i].boff : nullptr);
+    // the classes write disjoint outputs: spread them over the side streams,
+    // heaviest first, so that the small ones fill the SMs around the large ones
+    ctx.fork();
+    int slot = 0;
+    for (int i = (int)P->classes.size() - 1; i >= 0; --i) {
+        ClassPlan& c = P->classes[i];
+        if (c.nwarps == 0) continue;
+        launch_class(ctx, P, c, MODE_PACKED, d_out, nullptr, keep_blocks ? P->blocks.p + c.boff : nullptr,
+                     ctx.aux[slot++ % Context::NAUX]);
+    }
+    ctx.join();
     HF_CUDA(cudaEventRecord(e1, ctx.stream));
     HF_CUDA(cudaEventSynchronize(e1));
     float ms = 0;
