@@ -305,16 +305,16 @@ __global__ void onee_grad_pair_kernel(OnePairArgs o)
                     const double dT = pre * cc * (2 * a * tu - qa[k] * td);
                     gA[k] += wP * dT - wW * dS;  // two-centre: d/dB = -d/dA
                 }
-                // nuclear attraction: the six Hermite densities
+                // nuclear attraction: the six Hermite densities, over each derivative's
+                // support only (the component pair's box, one longer along k)
                 const double w = wP * cc;
-                for (int t = 0; t <= L; ++t)
-                    for (int u = 0; u <= L - t; ++u)
-                        for (int v = 0; v <= L - t - u; ++v) {
-                            const int hh = hidx(t, u, v);
-                            const int tt[3] = {t, u, v};
-                            for (int k = 0; k < 3; ++k) {
-                                // A: bra power qa[k] +- 1 along k; B: ket power qb[k] +- 1
-                                double eA = 1.0, eB = 1.0;
+                for (int k = 0; k < 3; ++k) {
+                    const int tmax[3] = {qa[0] + qb[0] + (k == 0), qa[1] + qb[1] + (k == 1), qa[2] + qb[2] + (k == 2)};
+                    for (int t = 0; t <= tmax[0]; ++t)
+                        for (int u = 0; u <= tmax[1]; ++u)
+                            for (int v = 0; v <= tmax[2]; ++v) {
+                                const int tt[3] = {t, u, v};
+                                double eA = w, eB = w;
                                 for (int d = 0; d < 3; ++d) {
                                     if (d == k) {
                                         const double up = E[d][og(qa[d] + 1, qb[d], tt[d])];
@@ -329,10 +329,11 @@ __global__ void onee_grad_pair_kernel(OnePairArgs o)
                                         eB *= e;
                                     }
                                 }
-                                H[k * nh + hh] += w * eA;
-                                H[(3 + k) * nh + hh] += w * eB;
+                                const int hh = hidx(t, u, v);
+                                H[k * nh + hh] += eA;
+                                H[(3 + k) * nh + hh] += eB;
                             }
-                        }
+                }
             }
         const int ta = 3 * o.satom[A], tb = 3 * o.satom[B];
         for (int k = 0; k < 3; ++k) {
