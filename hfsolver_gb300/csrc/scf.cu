@@ -202,16 +202,20 @@ __device__ __forceinline__ void block_add(double v, double* dst)
 // squares its tt x tt upper-triangle tile from its tt rows and tt columns of X_k,
 // staged whole in shared memory (stride n + 1: no bank conflicts).  The result
 // ends in X0.  T = float for the coarse steps of early SCF iterations.  The tile
-// edge tt (8 .. 16) is chosen so that the tiles spread the FP64 work evenly over
-// the SMs (sp2_tile).
+// edge tt (8 .. 16) and the number of k-slices ks each output's dot product is
+// split into (their partial sums meet in shared memory) are chosen so that the
+// FP64 work spreads evenly over the SMs and over each SM's four sub-partitions
+// (sp2_shape).
 template <typename T>
-__global__ void __launch_bounds__(256) sp2_persistent_kernel(int n, int nocc, int tt, T* X0, T* X1, double* tr,
-                                                             int maxs, double tol_idem, double tol_n, Sp2Sync* sync)
+__global__ void __launch_bounds__(1024) sp2_persistent_kernel(int n, int nocc, int tt, int ks, T* X0, T* X1,
+                                                              double* tr, int maxs, double tol_idem, double tol_n,
+                                                              Sp2Sync* sync)
 {
     extern __shared__ __align__(16) unsigned char sp2_smem[];
     const int ld = n + 1;
     T* Ar = (T*)sp2_smem;  // rows i0 .. i0+tt-1 of X_k, all k
     T* Bc = Ar + tt * ld;  // columns j0 .. j0+tt-1 (rows by symmetry)
+    T* part = Bc + tt * ld;  // partial dot products of k-slices 1 .. ks-1
     const int nt = (n + tt - 1) / tt;
     int b = blockIdx.x, ti = 0;
     while (b >= nt - ti) {
@@ -220,11 +224,16 @@ __global__ void __launch_bounds__(256) sp2_persistent_kernel(int n, int nocc, in
     }
     const int tj = ti + b;
     const int i0 = ti * tt, j0 = tj * tt;
-    // tt x tt workers; the block is rounded up to whole warps for the reductions
-    const bool worker = (int)threadIdx.x < tt * tt;
-    const int ty = threadIdx.x / tt, tx = threadIdx.x % tt;
+    // ks x tt x tt workers: output (ty, tx) of k-slice `slice` (ks slices spread the
+    // tile's FP64 work over all four sub-partitions of the SM); the block is rounded
+    // up to whole warps for the reductions
+    const int outs = tt * tt;
+    const bool worker = (int)threadIdx.x < ks * outs;
+    const int slice = (int)threadIdx.x / outs, o = (int)threadIdx.x - slice * outs;
+    const int ty = o / tt, tx = o % tt;
     const int i = i0 + ty, j = j0 + tx;
-    const bool own = worker && i < n && j < n;
+    const int kc = (n + ks - 1) / ks, k0 = slice * kc, k1 = min(n, k0 + kc);
+    const bool own = worker && slice == 0 && i < n && j < n;
     for (int it = 0; it < maxs; ++it) {
         T* Xc = (it & 1) ? X1 : X0;
         T* Xn = (it & 1) ? X0 : X1;
@@ -248,7 +257,13 @@ __global__ void __launch_bounds__(256) sp2_persistent_kernel(int n, int nocc, in
         if (worker) {
             const T* ar = Ar + ty * ld;
             const T* bc = Bc + tx * ld;
-            for (int k = 0; k < n; ++k) acc = fma(ar[k], bc[k], acc);
+            for (int k = k0; k < k1; ++k) acc = fma(ar[k], bc[k], acc);
+            if (slice > 0) part[(slice - 1) * outs + o] = acc;
+        }
+        if (ks > 1) {
+            __syncthreads();
+            if (worker && slice == 0)
+                for (int q = 1; q < ks; ++q) acc += part[(q - 1) * outs + o];
         }
         double pt = 0.0, pn = 0.0;
         if (own) {
@@ -313,8 +328,11 @@ __global__ void sp2_step_kernel(int n, int nocc, const double* __restrict__ t, c
     if (i == j) atomicAdd(tnext, x);
 }
 
-static int sp2_threads(int tt) { return (tt * tt + 31) / 32 * 32; }
-static size_t sp2_smem_bytes(int n, int tt, size_t elem) { return 2 * (size_t)tt * (n + 1) * elem; }
+static int sp2_threads(int tt, int ks) { return (ks * tt * tt + 31) / 32 * 32; }
+static size_t sp2_smem_bytes(int n, int tt, int ks, size_t elem)
+{
+    return (2 * (size_t)tt * (n + 1) + (size_t)(ks - 1) * tt * tt) * elem;
+}
 static unsigned sp2_tiles(int n, int tt)
 {
     const int nt = (n + tt - 1) / tt;
@@ -322,7 +340,7 @@ static unsigned sp2_tiles(int n, int tt)
 }
 
 // can all blocks of the persistent SP2 kernel with tile edge tt be resident at once?
-static bool coop_ok(Context& ctx, int n, int tt)
+static bool coop_ok(Context& ctx, int n, int tt, int ks)
 {
     int coop = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx.device) != cudaSuccess || !coop) return false;
@@ -331,44 +349,53 @@ static bool coop_ok(Context& ctx, int n, int tt)
     static std::once_flag once;
     static bool attr_ok = false;
     std::call_once(once, [] {
-        const int most = (int)sp2_smem_bytes(512, 16, sizeof(double));
+        const int most = (int)sp2_smem_bytes(512, 16, 4, sizeof(double));
         attr_ok = cudaFuncSetAttribute(sp2_persistent_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        most) == cudaSuccess &&
                   cudaFuncSetAttribute(sp2_persistent_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        most) == cudaSuccess;
     });
     if (!attr_ok || n > 512) return false;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sp2_persistent_kernel<double>, sp2_threads(tt),
-                                                      sp2_smem_bytes(n, tt, sizeof(double))) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sp2_persistent_kernel<double>, sp2_threads(tt, ks),
+                                                      sp2_smem_bytes(n, tt, ks, sizeof(double))) != cudaSuccess)
         return false;
     return (int64_t)per_sm * ctx.num_sms >= (int64_t)sp2_tiles(n, tt);
 }
 
-// tile edge of the persistent SP2 kernel.  Per step, the busiest SM squares
-// ceil(tiles / SMs) tiles of tt^2 length-n dot products (~n/2 cycles each at
-// two FP64 FMAs per cycle), and every block adds ~40 cycles of atomics at the
-// barrier and the trace sums; take the tt in 8 .. 16 with the least of both
-// among those whose grid can be co-resident.  0: none fits.
-static int sp2_tile(Context& ctx, int n)
+// tile edge tt and k-slices ks of the persistent SP2 kernel.  Per step, a warp's
+// FP64 FMA keeps its sub-partition's FP64 pipe ~64 cycles busy on this GPU, so the
+// busiest sub-partition of the busiest SM takes ceil(resident warps / 4) x n/ks
+// such instructions; every block adds ~40 cycles of atomics at the barrier and the
+// trace sums.  Take the (tt in 8 .. 16, ks in 1 .. 4) with the least of both
+// among those whose grid can be co-resident.  tt = 0: none fits.
+struct Sp2Shape {
+    int tt = 0, ks = 1;
+};
+
+static Sp2Shape sp2_shape(Context& ctx, int n)
 {
-    int best = 0;
+    Sp2Shape best;
     int64_t best_cost = 0;
-    for (int tt = 16; tt >= 8; --tt) {
-        if (!coop_ok(ctx, n, tt)) continue;
-        const int64_t tiles = sp2_tiles(n, tt);
-        const int64_t per_sm = (tiles + ctx.num_sms - 1) / ctx.num_sms;
-        const int64_t cost = per_sm * tt * tt * n / 2 + 40 * tiles;
-        if (best == 0 || cost < best_cost) {
-            best = tt;
-            best_cost = cost;
+    for (int tt = 16; tt >= 8; --tt)
+        for (int ks = 1; ks <= 4; ++ks) {
+            if (ks * tt * tt > 1024 || !coop_ok(ctx, n, tt, ks)) continue;
+            const int64_t tiles = sp2_tiles(n, tt);
+            const int64_t per_sm = (tiles + ctx.num_sms - 1) / ctx.num_sms;
+            const int64_t warps = sp2_threads(tt, ks) / 32;
+            const int64_t cost = (per_sm * warps + 3) / 4 * ((n + ks - 1) / ks) * 64 + 40 * tiles;
+            if (best.tt == 0 || cost < best_cost) {
+                best.tt = tt;
+                best.ks = ks;
+                best_cost = cost;
+            }
         }
-    }
     return best;
 }
 
 struct Purifier {
     int n = 0, nocc = 0;
-    int tile = 0;  // persistent-kernel tile edge (sp2_tile); -1: per-step fallback
+    int tile = 0;  // persistent-kernel tile edge (sp2_shape); -1: per-step fallback
+    int kslices = 1;
     DBuf<double> X, T1, T2, B, tr;  // orthogonaliser S^-1/2 and work
     DBuf<float> Xf;                 // FP32 iterate of the coarse steps
     DBuf<Sp2Sync> sync;
@@ -395,11 +422,12 @@ struct Purifier {
     {
         cudaStream_t st = ctx.stream;
         HF_CUDA(cudaMemsetAsync(sync.p + which, 0, sizeof(Sp2Sync), st));
-        int n_ = n, nocc_ = nocc, tt_ = tt;
+        int n_ = n, nocc_ = nocc, tt_ = tt, ks_ = kslices;
         Sp2Sync* sp = sync.p + which;
-        void* args[] = {&n_, &nocc_, &tt_, &Xs, &Xw, &trs, &maxs, &tol_idem, &tol_n, &sp};
+        void* args[] = {&n_, &nocc_, &tt_, &ks_, &Xs, &Xw, &trs, &maxs, &tol_idem, &tol_n, &sp};
         HF_CUDA(cudaLaunchCooperativeKernel((const void*)sp2_persistent_kernel<T>, dim3(sp2_tiles(n, tt)),
-                                            dim3(sp2_threads(tt)), args, sp2_smem_bytes(n, tt, sizeof(T)), st));
+                                            dim3(sp2_threads(tt, kslices)), args,
+                                            sp2_smem_bytes(n, tt, kslices, sizeof(T)), st));
         count_launch();
     }
     // The outcome of the last cooperative purification (barrier timeouts, final
@@ -450,8 +478,9 @@ struct Purifier {
         double h[2] = {0, 1};
         bool done = false;
         if (tile == 0) {
-            tile = sp2_tile(ctx, n);
-            if (tile == 0) tile = -1;
+            const Sp2Shape sh = sp2_shape(ctx, n);
+            tile = sh.tt == 0 ? -1 : sh.tt;
+            kslices = sh.ks;
         }
         if (tile > 0) {
             if (!sync.p) {
