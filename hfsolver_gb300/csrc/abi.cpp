@@ -172,21 +172,22 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         }
         res->ms_setup = total.ms();
         ctx.trace_mark("one-electron + plan");
-        // the packed array feeds MBPT2; the screened quartet blocks feed every Fock build
+        // the packed array feeds MBPT2; the screened quartet blocks feed every Fock build.
+        // One molecule: the ERI classes run on the side streams while the SCF queues
+        // its set-up on the main stream (ScfIn::begin / end below).
+        struct EriHook {
+            Context* ctx;
+            EriPlan* plan;
+            double* out;
+            EriStats* es;
+        } hook{&ctx, plan.get(), dI.p, &es};
         if (bm) {
             d_int2 = bm->wave->eri_rendezvous(bm->mol, ctx, plan.get(), &es.ms);
             const double ms = es.ms;
             es = eri_plan_stats(plan.get());
             es.ms = ms;
-        } else {
-            eri_compute(ctx, plan.get(), dI.p, true, &es);
+            ctx.trace_mark("eri");
         }
-        res->ms_eri = es.ms;
-        res->n_quartets = es.n_quartets;
-        res->n_bf_quartets = es.n_bf_quartets;
-        res->n_prim_quartets = es.n_prim_quartets;
-        res->eri_flops = es.flops;
-        ctx.trace_mark("eri");
         // SCF
         Timer ts(st);
         DBuf<double> dC(nn, st), dP(nn, st), dL(n, st);
@@ -204,6 +205,18 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         // iterations remove what they left out before convergence is accepted
         if (opt.incremental) in.inc_screen = std::max(opt.schwarz, 1e-10);
         in.direct_ctx = plan.get();
+        if (!bm) {
+            in.begin = [](void* u) {
+                auto* h = (EriHook*)u;
+                eri_compute_start(*h->ctx, h->plan, h->out, true);
+            };
+            in.end = [](void* u) {
+                auto* h = (EriHook*)u;
+                eri_compute_finish(*h->ctx, h->plan, h->es);
+                h->ctx->trace_mark("eri");
+            };
+            in.hook_user = &hook;
+        }
         if (bm) {  // Fock builds shared with the rest of the wave
             in.direct_jk = [](Context& c, void* user, const double* P, double* G, double screen) {
                 auto* m = (BatchMember*)user;
@@ -219,9 +232,14 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
             ctx.trace_mark("guess");
         }
         ScfOut so = run_scf(ctx, in, dC.p, dP.p, dL.p);
+        res->ms_eri = es.ms;
+        res->n_quartets = es.n_quartets;
+        res->n_bf_quartets = es.n_bf_quartets;
+        res->n_prim_quartets = es.n_prim_quartets;
+        res->eri_flops = es.flops;
         if (bm) res->ms_fock = bm->wave->fock_ms();
         wave_exit.now();
-        res->ms_scf = ts.ms();
+        res->ms_scf = ts.ms() - (bm ? 0.0 : es.ms);  // the ERI pass ran inside, under the SCF's set-up
         conv = so.converged;
         double Enuc = 0;
         for (int i = 0; i < natoms; i++)

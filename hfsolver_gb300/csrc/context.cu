@@ -72,7 +72,14 @@ static Context* make_context(int dev)
 {
     auto* c = new Context();
     c->device = dev;
-    HF_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+    // the main stream outranks the side streams: its chains of small dependent
+    // kernels (the SCF set-up under the ERI pass, the symmetrisation after a
+    // Fock build) take SMs first as blocks of the side streams' classes drain
+    {
+        int least = 0, greatest = 0;
+        HF_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        HF_CUDA(cudaStreamCreateWithPriority(&c->own_stream, cudaStreamNonBlocking, greatest));
+    }
     c->stream = c->own_stream;
     HF_CUBLAS(cublasCreate(&c->blas));
     HF_CUBLAS(cublasSetStream(c->blas, c->stream));

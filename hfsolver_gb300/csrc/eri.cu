@@ -681,7 +681,11 @@ static void eri_class_layout(Context& ctx, EriPlan* P, ClassPlan& c, double* d_o
     if (c.lane_target != target) layout_class(ctx, c, target);
 }
 
-void eri_compute(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks, EriStats* st)
+// The ERI pass in two halves: eri_compute_start tunes and lays out the classes
+// on the main stream, then launches them over the side streams and returns;
+// work the caller queues on the main stream meanwhile runs beside them;
+// eri_compute_finish joins the side streams and reports the time.
+void eri_compute_start(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks)
 {
     P->stats.n_block_elems = 0;
     for (auto& c : P->classes) P->stats.n_block_elems += c.nq * block_size(c.tb, c.tk);
@@ -696,10 +700,9 @@ void eri_compute(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks, EriS
         P->blocks.alloc(std::max<int64_t>(total, 1), ctx.stream);
         P->qlist.alloc(std::max<int64_t>(nqt, 1), ctx.stream);
     }
-    cudaEvent_t e0, e1;
-    HF_CUDA(cudaEventCreate(&e0));
-    HF_CUDA(cudaEventCreate(&e1));
-    HF_CUDA(cudaEventRecord(e0, ctx.stream));
+    if (!P->ev0) HF_CUDA(cudaEventCreate(&P->ev0));
+    if (!P->ev1) HF_CUDA(cudaEventCreate(&P->ev1));
+    HF_CUDA(cudaEventRecord(P->ev0, ctx.stream));
     for (int i = (int)P->classes.size() - 1; i >= 0; --i)
         eri_class_layout(ctx, P, P->classes[i], d_out, keep_blocks ? P->blocks.p + P->classes[i].boff : nullptr);
     // the classes write disjoint outputs: spread them over the side streams,
@@ -712,17 +715,25 @@ void eri_compute(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks, EriS
         launch_class(ctx, P, c, MODE_PACKED, d_out, nullptr, keep_blocks ? P->blocks.p + c.boff : nullptr,
                      ctx.aux[slot++ % Context::NAUX]);
     }
+}
+
+void eri_compute_finish(Context& ctx, EriPlan* P, EriStats* st)
+{
     ctx.join();
-    HF_CUDA(cudaEventRecord(e1, ctx.stream));
-    HF_CUDA(cudaEventSynchronize(e1));
+    HF_CUDA(cudaEventRecord(P->ev1, ctx.stream));
+    HF_CUDA(cudaEventSynchronize(P->ev1));
     float ms = 0;
-    HF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    HF_CUDA(cudaEventElapsedTime(&ms, P->ev0, P->ev1));
     if (st) {
         *st = P->stats;
         st->ms = ms;
     }
+}
+
+void eri_compute(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks, EriStats* st)
+{
+    eri_compute_start(ctx, P, d_out, keep_blocks);
+    eri_compute_finish(ctx, P, st);
 }
 
 

@@ -44,6 +44,7 @@ struct EriPlan {
     DBuf<int2> qlist;     // (bra, ket) pair ids of every kept quartet, class by class
     DBuf<int> pair_mol;   // batched plans: the molecule of every pair
     EriStats stats;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the ERI pass (eri_compute_start / _finish)
     // host copies of the grouped pair ids and prefix sums (for merging plans)
     std::vector<int> h_gpairs;
     std::vector<int64_t> h_prefix;
@@ -53,6 +54,15 @@ struct EriPlan {
     int nmol = 1;
     std::vector<int> mol_nbf, mol_ns, mol_sh0;
     DBuf<int64_t> mol_out;
+
+    EriPlan() = default;
+    EriPlan(const EriPlan&) = delete;
+    EriPlan& operator=(const EriPlan&) = delete;
+    ~EriPlan()
+    {
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+    }
 
     ShellDev shdev() const
     {

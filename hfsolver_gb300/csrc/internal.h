@@ -215,6 +215,8 @@ void eri_compute_packed(Context& ctx, EriPlan* p, double* d_out, EriStats* st);
 // the same, d_out may be null; keep_blocks also keeps the screened quartet blocks
 // in HBM for eri_digest
 void eri_compute(Context& ctx, EriPlan* p, double* d_out, bool keep_blocks, EriStats* st);
+void eri_compute_start(Context& ctx, EriPlan* p, double* d_out, bool keep_blocks);
+void eri_compute_finish(Context& ctx, EriPlan* p, EriStats* st);
 // G = J - K/2 of density dP from the kept quartet blocks (n x n); screen > 0
 // leaves out quartets whose Schwarz bound times the largest |dP| element they
 // touch is below screen (for density differences)

@@ -575,6 +575,7 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
     const int n = in.n;
     const int64_t nn = (int64_t)n * n;
     HF_CHECK(in.nocc >= 0 && in.nocc <= n, HFGPU_ERR_INVALID, "nocc out of range");
+    if (in.begin) in.begin(in.hook_user);
     DBuf<double> G(nn, st), F(nn, st), Fw(nn, st), Sw(nn, st), Pold(nn, st), scal(4, st);
     DBuf<int> info(1, st);
     info.zero();  // written by dsygvd; the own eigensolver reports errors by exception
@@ -646,6 +647,7 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
     double last_dP = 1.0;
     const double* last_F = nullptr;  // the Fock matrix of the last eigensolve
     ctx.trace_mark("scf setup");
+    if (in.end) in.end(in.hook_user);
     for (int it = 1; it <= in.nscf; ++it) {
         const double* Gcur = G.p;
         if (inc) {

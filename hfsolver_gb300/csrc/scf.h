@@ -30,6 +30,12 @@ struct ScfIn {
     // eigensolver: 0 = own (eigh.cu: GPU tridiagonalisation, host tridiagonal
     // solve) where it fits (3 <= n <= 1024), else cuSOLVER dsygvd; 1 = dsygvd
     int eigensolver = 0;
+    // optional: called first (before the SCF's own set-up is queued) and right
+    // before the first Fock build, so that work started by `begin` on side
+    // streams (the ERI pass) runs under the set-up; `end` joins it
+    void (*begin)(void* user) = nullptr;
+    void (*end)(void* user) = nullptr;
+    void* hook_user = nullptr;
 };
 
 struct ScfOut {
