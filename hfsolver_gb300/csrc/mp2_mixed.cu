@@ -60,9 +60,10 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
     // steps 2 and 4 (N = v) read their FP64 rows straight into the gather-fed GEMM
     // (coalesced rows, no slice planes through HBM) while the virtual block spans
     // at most DENSE_GATHER_TILES output tiles of 80 columns; wider ones use slicing
-    // + TMA.  The gather GEMM walks whole 80-column tiles of B, so C2's slices are
+    // + TMA.  Measured at 16 waters (v = 320, four tiles): gathering each row four
+    // times beats slicing it once through HBM (steps 2 + 4: 131 -> 91 ms).  The gather GEMM walks whole 80-column tiles of B, so C2's slices are
     // then padded to a multiple of 80 rows.
-    constexpr int DENSE_GATHER_TILES = 2;
+    constexpr int DENSE_GATHER_TILES = 4;
     const bool dense_gather = n2 <= 80 * DENSE_GATHER_TILES;
     slice_dense(ctx, C1, n1, n, n, B1, SLICE_TILE_B);  // rows of B^T = columns of C1
     slice_dense(ctx, C2, n2, n, n, B2, dense_gather ? 80 : SLICE_TILE_B);
