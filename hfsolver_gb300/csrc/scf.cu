@@ -202,7 +202,7 @@ __device__ __forceinline__ void block_add(double v, double* dst)
 // squares its tt x tt upper-triangle tile from its tt rows and tt columns of X_k,
 // staged whole in shared memory (stride n + 1: no bank conflicts).  The result
 // ends in X0.  T = float for the coarse steps of early SCF iterations.  The tile
-// edge tt (8 .. 16) and the number of k-slices ks each output's dot product is
+// edge tt (8 .. 32) and the number of k-slices ks each output's dot product is
 // split into (their partial sums meet in shared memory) are chosen so that the
 // FP64 work spreads evenly over the SMs and over each SM's four sub-partitions
 // (sp2_shape).
@@ -344,18 +344,30 @@ static bool coop_ok(Context& ctx, int n, int tt, int ks)
 {
     int coop = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx.device) != cudaSuccess || !coop) return false;
-    // the attribute is per process: set it once, for the largest case (n = 512,
-    // tt = 16), so that concurrent molecules of other sizes never lower it
+    // the attribute is per process: set it once, to the most a block may have,
+    // so that concurrent molecules of other sizes never lower it
+    // (the block's opt-in maximum less the kernels' static shared memory)
     static std::once_flag once;
     static bool attr_ok = false;
-    std::call_once(once, [] {
-        const int most = (int)sp2_smem_bytes(512, 16, 4, sizeof(double));
+    static size_t most = 0;
+    const int dev = ctx.device;
+    std::call_once(once, [dev] {
+        int optin = 0;
+        cudaFuncAttributes fd{}, ff{};
+        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+            cudaFuncGetAttributes(&fd, sp2_persistent_kernel<double>) != cudaSuccess ||
+            cudaFuncGetAttributes(&ff, sp2_persistent_kernel<float>) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return;
+        }
+        most = (size_t)optin - std::max(fd.sharedSizeBytes, ff.sharedSizeBytes);
         attr_ok = cudaFuncSetAttribute(sp2_persistent_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       most) == cudaSuccess &&
+                                       (int)most) == cudaSuccess &&
                   cudaFuncSetAttribute(sp2_persistent_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       most) == cudaSuccess;
+                                       (int)most) == cudaSuccess;
+        if (!attr_ok) (void)cudaGetLastError();  // no pending error for the next launch check
     });
-    if (!attr_ok || n > 512) return false;
+    if (!attr_ok || n > 512 || sp2_smem_bytes(n, tt, ks, sizeof(double)) > most) return false;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sp2_persistent_kernel<double>, sp2_threads(tt, ks),
                                                       sp2_smem_bytes(n, tt, ks, sizeof(double))) != cudaSuccess)
         return false;
@@ -366,8 +378,10 @@ static bool coop_ok(Context& ctx, int n, int tt, int ks)
 // FP64 FMA keeps its sub-partition's FP64 pipe ~64 cycles busy on this GPU, so the
 // busiest sub-partition of the busiest SM takes ceil(resident warps / 4) x n/ks
 // such instructions; every block adds ~40 cycles of atomics at the barrier and the
-// trace sums.  Take the (tt in 8 .. 16, ks in 1 .. 4) with the least of both
-// among those whose grid can be co-resident.  tt = 0: none fits.
+// trace sums.  Take the (tt in 8 .. 32, ks in 1 .. 4, at most 1024 threads) with
+// the least of both among those whose grid can be co-resident (n = 400: edge 17
+// or 25, where 8 .. 16 would need more blocks per SM than shared memory allows).
+// tt = 0: none fits.
 struct Sp2Shape {
     int tt = 0, ks = 1;
 };
@@ -376,7 +390,7 @@ static Sp2Shape sp2_shape(Context& ctx, int n)
 {
     Sp2Shape best;
     int64_t best_cost = 0;
-    for (int tt = 16; tt >= 8; --tt)
+    for (int tt = 32; tt >= 8; --tt)
         for (int ks = 1; ks <= 4; ++ks) {
             if (ks * tt * tt > 1024 || !coop_ok(ctx, n, tt, ks)) continue;
             const int64_t tiles = sp2_tiles(n, tt);
