@@ -239,7 +239,7 @@ static void rhf_impl(int natoms, const int* atno, const double* xyz, const hfgpu
         res->eri_flops = es.flops;
         if (bm) res->ms_fock = bm->wave->fock_ms();
         wave_exit.now();
-        res->ms_scf = ts.ms() - (bm ? 0.0 : es.ms);  // the ERI pass ran inside, under the SCF's set-up
+        res->ms_scf = ts.ms() - (bm ? 0.0 : es.ms);  // the ERI pass ran inside, beside the SCF's set-up
         conv = so.converged;
         double Enuc = 0;
         for (int i = 0; i < natoms; i++)

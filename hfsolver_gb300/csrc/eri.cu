@@ -715,6 +715,14 @@ void eri_compute_start(Context& ctx, EriPlan* P, double* d_out, bool keep_blocks
         launch_class(ctx, P, c, MODE_PACKED, d_out, nullptr, keep_blocks ? P->blocks.p + c.boff : nullptr,
                      ctx.aux[slot++ % Context::NAUX]);
     }
+    // the pass ends with the last class kernel of each side stream (not with
+    // whatever the caller queues on the main stream before the join)
+    static_assert(Context::NAUX <= 8, "one end event per side stream");
+    P->n_ev_end = std::min(slot, (int)Context::NAUX);
+    for (int i = 0; i < P->n_ev_end; ++i) {
+        if (!P->ev_end[i]) HF_CUDA(cudaEventCreate(&P->ev_end[i]));
+        HF_CUDA(cudaEventRecord(P->ev_end[i], ctx.aux[i]));
+    }
 }
 
 void eri_compute_finish(Context& ctx, EriPlan* P, EriStats* st)
@@ -724,6 +732,14 @@ void eri_compute_finish(Context& ctx, EriPlan* P, EriStats* st)
     HF_CUDA(cudaEventSynchronize(P->ev1));
     float ms = 0;
     HF_CUDA(cudaEventElapsedTime(&ms, P->ev0, P->ev1));
+    if (P->n_ev_end > 0) {
+        ms = 0;
+        for (int i = 0; i < P->n_ev_end; ++i) {
+            float m = 0;
+            HF_CUDA(cudaEventElapsedTime(&m, P->ev0, P->ev_end[i]));
+            ms = std::max(ms, m);
+        }
+    }
     if (st) {
         *st = P->stats;
         st->ms = ms;

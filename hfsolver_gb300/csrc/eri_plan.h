@@ -44,7 +44,11 @@ struct EriPlan {
     DBuf<int2> qlist;     // (bra, ket) pair ids of every kept quartet, class by class
     DBuf<int> pair_mol;   // batched plans: the molecule of every pair
     EriStats stats;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the ERI pass (eri_compute_start / _finish)
+    // around the ERI pass (eri_compute_start / _finish): ev0 on the main stream
+    // before it, ev_end[i] after the last class launched on side stream i
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev_end[8] = {};
+    int n_ev_end = 0;
     // host copies of the grouped pair ids and prefix sums (for merging plans)
     std::vector<int> h_gpairs;
     std::vector<int64_t> h_prefix;
@@ -62,6 +66,8 @@ struct EriPlan {
     {
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        for (auto e : ev_end)
+            if (e) cudaEventDestroy(e);
     }
 
     ShellDev shdev() const
