@@ -325,10 +325,12 @@ EriPlan* eri_plan_create(Context& ctx, const Basis& b, double thr)
             DBuf<int2> ddl = to_device(dl, st);
             DBuf<double> diag((size_t)P->npair * 36, st);
             diag.zero();
-            for (auto& c : dcls) {
-                c.dsegs = to_device(c.segs, st);
-                launch_class(ctx, P, c, MODE_DIAG, diag.p, ddl.p);
-            }
+            for (auto& c : dcls) c.dsegs = to_device(c.segs, st);
+            // one small class per pair type, each latency-bound: side by side
+            ctx.fork();
+            for (size_t i = 0; i < dcls.size(); ++i)
+                launch_class(ctx, P, dcls[i], MODE_DIAG, diag.p, ddl.p, nullptr, ctx.aux[i % Context::NAUX]);
+            ctx.join();
             // Q = sqrt(max |(ab|ab)|) per pair on the device; only Q comes back
             DBuf<double> dq(P->npair, st);
             pair_qmax_kernel<<<(P->npair + 127) / 128, 128, 0, st>>>(P->npair, diag.p, dq.p);
