@@ -509,11 +509,11 @@ static void launch_digest(const ClassPlan& c, const DigestArgs& a, cudaStream_t 
 {
     const int64_t qpw = (int64_t)(32 / a.split) * a.rounds;
     const int64_t warps = (c.nq + qpw - 1) / qpw;
-    const unsigned blocks = (unsigned)((warps + 3) / 4);
+    const unsigned blocks = (unsigned)((warps + DIGEST_WARPS - 1) / DIGEST_WARPS);
     if (a.split == 1)
-        digest_fn(c.tb, c.tk)<<<blocks, 128, 0, s>>>(a);
+        digest_fn(c.tb, c.tk)<<<blocks, DIGEST_BLOCK, 0, s>>>(a);
     else
-        digest_wide_fn(c.tb, c.tk)<<<blocks, 128, 0, s>>>(a);
+        digest_wide_fn(c.tb, c.tk)<<<blocks, DIGEST_BLOCK, 0, s>>>(a);
     count_launch();
     HF_CUDA(cudaGetLastError());
 }

@@ -504,10 +504,10 @@ void eri_gradient(Context& ctx, EriPlan* P, const double* dP, double* d_grad, fl
     }
     DBuf<Seg> dsegs = to_device(segs, st);
     // the launches are independent (their sums meet in atomics): spread them over
-    // the side streams, largest first, so that small classes fill the GPU
-    // around the large ones instead of each draining it alone
+    // the side streams, smallest first, so that the large ones come last and
+    // fill the GPU to the end instead of small ones leaving a ragged tail
     std::sort(launches.begin(), launches.end(),
-              [](const Launch& x, const Launch& y) { return x.work > y.work; });
+              [](const Launch& x, const Launch& y) { return x.work < y.work; });
     cudaEvent_t e0, e1;
     HF_CUDA(cudaEventCreate(&e0));
     HF_CUDA(cudaEventCreate(&e1));

@@ -138,6 +138,9 @@ __device__ __forceinline__ bool digest_skip(const DigestArgs& a, const DigestMol
 __device__ __forceinline__ bool digest_nonzero(double v) { return (__double_as_longlong(v) << 1) != 0; }
 
 constexpr int DIGEST_MAX_Q = 256;  // quartets screened per warp: 32 x 8 rounds
+// threads per block of the digest kernels (two warps: a class with few quartets
+// still reaches most SMs)
+constexpr int DIGEST_BLOCK = 64, DIGEST_WARPS = DIGEST_BLOCK / 32;
 
 // Screen the warp's quartets q0 .. q0 + cnt - 1 (density-difference screen,
 // molecules not in this build) and leave the offsets of the survivors in the
@@ -282,12 +285,12 @@ __device__ __forceinline__ void digest_one(const DigestArgs& a, int64_t qg)
 }
 
 template <int TB, int TK>
-__global__ void __launch_bounds__(128) digest_kernel(DigestArgs a)
+__global__ void __launch_bounds__(DIGEST_BLOCK) digest_kernel(DigestArgs a)
 {
-    __shared__ int sl[4][DIGEST_MAX_Q];
+    __shared__ int sl[DIGEST_WARPS][DIGEST_MAX_Q];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int qpw = 32 * a.rounds;
-    const int64_t q0 = ((int64_t)blockIdx.x * 4 + warp) * qpw;
+    const int64_t q0 = ((int64_t)blockIdx.x * DIGEST_WARPS + warp) * qpw;
     if (q0 >= a.nq) return;  // the whole warp
     if (a.screen <= 0.0 && !a.mol_n) {  // nothing is screened: no list
         for (int k = lane; k < qpw; k += 32)
@@ -390,13 +393,13 @@ __device__ __forceinline__ void digest_wide_one(const DigestArgs& a, int64_t qg,
 }
 
 template <int TB, int TK>
-__global__ void __launch_bounds__(128) digest_wide_kernel(DigestArgs a)
+__global__ void __launch_bounds__(DIGEST_BLOCK) digest_wide_kernel(DigestArgs a)
 {
-    __shared__ int sl[4][DIGEST_MAX_Q];
+    __shared__ int sl[DIGEST_WARPS][DIGEST_MAX_Q];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int split = a.split, per = 32 / split;
     const int qpw = per * a.rounds;
-    const int64_t q0 = ((int64_t)blockIdx.x * 4 + warp) * qpw;
+    const int64_t q0 = ((int64_t)blockIdx.x * DIGEST_WARPS + warp) * qpw;
     if (q0 >= a.nq) return;  // the whole warp
     const int sub = lane & (split - 1);
     const unsigned mask = split == 32 ? 0xffffffffu : (((1u << split) - 1u) << (lane & ~(unsigned)(split - 1)));
