@@ -303,7 +303,7 @@ def run_gpu(args):
                  "hbm_GBps": 8.0 * elems / (full_ms * 1e-3) / 1e9},
     }
     o, v = r["nocc"], n - r["nocc"]
-    # transform + MBPT2 work in the survey's unit: dense quarter transforms, no
+    # transform + MBPT2 work in the algorithmic unit: dense quarter transforms, no
     # permutational saving, 2 o N^4 + 2 o v N^3 + 2 o^2 v N^2 + 2 o^2 v^2 N flops;
     # the split-bf16 tensor work counted as 3x those flops (3-term split)
     dense_q = [2.0 * o * n ** 4, 2.0 * o * v * n ** 3, 2.0 * o * o * v * n ** 2, 2.0 * o * o * v * v * n]
