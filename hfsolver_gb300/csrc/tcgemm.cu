@@ -849,6 +849,11 @@ static void gather_gemm(Context& ctx, const Src& src, int64_t M, int64_t M_rows,
 // coalesced loads); each element counts for si (shared-memory atomicMax,
 // distinct per lane) and, as the run's maximum, for la.
 __device__ __forceinline__ unsigned abs_hi(double x) { return (unsigned)__double2hiint(x) & 0x7FFFFFFFu; }
+// the same straight from memory: the upper 32-bit word of the element, loaded as an integer
+__device__ __forceinline__ unsigned abs_hi_at(const double* p)
+{
+    return __ldg(reinterpret_cast<const unsigned*>(p) + 1) & 0x7FFFFFFFu;
+}
 
 __device__ __forceinline__ unsigned warp_max_u32(unsigned v)
 {
@@ -876,7 +881,7 @@ __global__ void row_max_tri_kernel(const double* __restrict__ src, int64_t ld, i
         const int smx = min(len - 1 - t0, la);
         unsigned m = 0u;
         for (int si = lane; si <= smx; si += 32) {
-            const unsigned v = abs_hi(__ldg(row + t0 + si));
+            const unsigned v = abs_hi_at(row + t0 + si);
             atomicMax(&smax32[si], v);
             m = max(m, v);
         }
@@ -900,17 +905,28 @@ __global__ void row_max_cols_kernel(const double* __restrict__ ints, int npair, 
     for (int i = threadIdx.x; i < n * 33; i += blockDim.x) smax32[i] = 0u;
     __syncthreads();
     const int a = a0 + lane;
-#pragma unroll 4
-    for (int b = a0 + 1 + warp; b < npair; b += nw) {
-        // pair b = (la, si), la >= si: la = floor((sqrt(8 b + 1) - 1) / 2), corrected
-        int la = (int)((sqrtf(8.0f * (float)b + 1.0f) - 1.0f) * 0.5f);
-        while (la * (la + 1) / 2 > b) --la;
-        while ((la + 1) * (la + 2) / 2 <= b) ++la;
-        const int si = b - la * (la + 1) / 2;
+    // the warp's stored rows b = b0, b0 + nw, ...: the pair (la, si) of b and the
+    // row's offset b (b + 1) / 2 are carried along by additions (64-bit multiplies
+    // and divisions are slow on this GPU)
+    int b = a0 + 1 + warp;
+    int la = (int)((sqrtf(8.0f * (float)b + 1.0f) - 1.0f) * 0.5f);
+    while (la * (la + 1) / 2 > b) --la;
+    while ((la + 1) * (la + 2) / 2 <= b) ++la;
+    int si = b - la * (la + 1) / 2;
+    const double* rowb = ints + (((int64_t)b * (b + 1)) >> 1);
+    for (; b < npair; ) {
         if (a < b) {
-            const unsigned v = abs_hi(__ldg(ints + (int64_t)b * (b + 1) / 2 + a));
+            const unsigned v = abs_hi_at(rowb + a);
             atomicMax(&smax32[la * 33 + lane], v);
             atomicMax(&smax32[si * 33 + lane], v);
+        }
+        // advance by nw: row offset (b + 1) + (b + 2) + ... + (b + nw)
+        rowb += (int64_t)nw * b + (nw * (nw + 1)) / 2;
+        b += nw;
+        si += nw;
+        while (si > la) {  // la grows by one for every la + 1 pairs
+            si -= la + 1;
+            ++la;
         }
     }
     __syncthreads();
@@ -954,7 +970,7 @@ __global__ void dense_row_max_kernel(const double* __restrict__ A, int64_t rows,
     if (r >= rows) return;
     const double* row = A + r * ld;
     unsigned m = 0u;
-    for (int k = lane; k < K; k += 32) m = max(m, abs_hi(__ldg(row + k)));
+    for (int k = lane; k < K; k += 32) m = max(m, abs_hi_at(row + k));
     m = warp_max_u32(m);
     if (lane == 0) out[r] = m;
 }
