@@ -141,7 +141,7 @@ void ao2mo_sliced(Context& ctx, int n, const double* d_int2, const double* C1, i
     }
 }
 
-// one block per (i, j): sum_ab (ia|jb) [2 (ia|jb) - (ib|ja)] / (e_i + e_j - e_a - e_b)
+// one block per pair i >= j: sum_ab (ia|jb) [2 (ia|jb) - (ib|ja)] / (e_i + e_j - e_a - e_b)
 // from T[j][b][i][a] (relative error of each term ~1e-14 from the refined reciprocal).  For fixed (i, j) the v x v block X[b][a] = (ia|jb) has rows
 // of consecutive a; (ib|ja) = X[a][b] is its transpose.  32 x 32 tiles of X and of
 // the mirrored tile are staged in shared memory with coalesced row reads, so T is
@@ -150,7 +150,14 @@ __global__ void __launch_bounds__(256) mp2_pair_energy_kernel(int o, int v, cons
                                                              const double* __restrict__ eps, double* partial)
 {
     __shared__ double A[32][33], B[32][33];
-    const int i = blockIdx.x % o, j = blockIdx.x / o;
+    // block p = the pair i >= j (p = i (i + 1) / 2 + j): the (j, i) block holds the
+    // same terms with a and b exchanged ((jb|ia) = (ia|jb)), so it counts twice
+    const int p = blockIdx.x;
+    int i = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
+    while (i * (i + 1) / 2 > p) --i;
+    while ((i + 1) * (i + 2) / 2 <= p) ++i;
+    const int j = p - i * (i + 1) / 2;
+    (void)o;
     const double eij = eps[i] + eps[j];
     const int64_t rs = (int64_t)o * v;  // stride between consecutive b (rows of X)
     const double* X = T + ((int64_t)j * v * o + i) * v;  // X[b][a] = X[b * rs + a]
@@ -186,7 +193,7 @@ __global__ void __launch_bounds__(256) mp2_pair_energy_kernel(int o, int v, cons
         if ((int)threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
         __syncthreads();
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+    if (threadIdx.x == 0) partial[blockIdx.x] = (i == j ? 1.0 : 2.0) * sh[0];
 }
 
 double mp2_energy_mixed(Context& ctx, int n, const double* d_int2, const double* dC, int o, const double* d_eps)
@@ -195,11 +202,12 @@ double mp2_energy_mixed(Context& ctx, int n, const double* d_int2, const double*
     if (o <= 0 || v <= 0) return 0.0;
     DBuf<double> T((size_t)o * v * o * v, ctx.stream);
     ao2mo_sliced(ctx, n, d_int2, dC, o, dC + (size_t)n * o, v, T.p);
-    DBuf<double> part((size_t)o * o, ctx.stream);
-    mp2_pair_energy_kernel<<<o * o, 256, 0, ctx.stream>>>(o, v, T.p, d_eps, part.p);
+    const int npairs = o * (o + 1) / 2;
+    DBuf<double> part((size_t)npairs, ctx.stream);
+    mp2_pair_energy_kernel<<<npairs, 256, 0, ctx.stream>>>(o, v, T.p, d_eps, part.p);
     count_launch();
     HF_CUDA(cudaGetLastError());
-    std::vector<double> h((size_t)o * o);
+    std::vector<double> h((size_t)npairs);
     part.download(h.data(), h.size());
     HF_CUDA(cudaStreamSynchronize(ctx.stream));
     double E = 0;
