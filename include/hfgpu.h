@@ -249,8 +249,8 @@ typedef struct {
     int64_t n_bf_quartets;   /* unique contracted basis-function quartets evaluated */
     int64_t n_prim_quartets; /* primitive shell quartets evaluated */
     double eri_flops;        /* McMurchie-Davidson reference flop count of those */
-    double ms_eri;           /* ERI class kernels */
-    double ms_scf, ms_mp2;   /* SCF loop; AO->MO transform + MBPT2 */
+    double ms_eri;           /* ERI class kernels (to the last of them; the SCF's set-up runs beside them) */
+    double ms_scf, ms_mp2;   /* SCF set-up and loop beyond ms_eri; AO->MO transform + MBPT2 */
     double ms_total;         /* the whole call */
     double ms_setup;         /* basis, one-electron integrals, pairs, Schwarz bounds */
     double ms_fock;          /* Fock two-electron kernels summed over the SCF iterations */
