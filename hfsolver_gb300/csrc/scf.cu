@@ -558,29 +558,68 @@ static void form_density(Context& ctx, int n, int nocc, const double* C, double*
 }
 
 // small dense solve with partial pivoting (DIIS system, size <= 21)
-static bool solve_small(std::vector<double>& A, std::vector<double>& b, int m)
+// The DIIS step on the device (one thread), so that the SCF iteration needs no
+// host round trip for it: Bd (nd x nd) keeps <e_k, e_l>; its row and column
+// `head` come from bvec (<e_k, e_head>, k < nhist).  The system
+// [[B / scale, -1], [-1, 0]] c = [0 .. 0, -1] is solved by Gaussian elimination
+// with partial pivoting; cvec receives the nhist coefficients, or selects the
+// newest Fock matrix alone when the system is singular.
+constexpr int DIIS_MAX = 20;  // the history length run_scf allows
+__global__ void diis_solve_kernel(int nd, int nhist, int head, double* __restrict__ Bd,
+                                  const double* __restrict__ bvec, double* __restrict__ cvec)
 {
-    for (int c = 0; c < m; c++) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int k = 0; k < nhist; k++) {
+        Bd[head * nd + k] = bvec[k];
+        Bd[k * nd + head] = bvec[k];
+    }
+    const int m = nhist + 1;
+    double A[(DIIS_MAX + 1) * (DIIS_MAX + 1)], b[DIIS_MAX + 1];
+    double scale = 0;
+    for (int a = 0; a < nhist; a++) scale = fmax(scale, fabs(Bd[a * nd + a]));
+    if (scale <= 0) scale = 1;
+    for (int a = 0; a < m; a++) {
+        for (int c = 0; c < m; c++) A[a * m + c] = 0.0;
+        b[a] = 0.0;
+    }
+    for (int a = 0; a < nhist; a++) {
+        for (int c = 0; c < nhist; c++) A[a * m + c] = Bd[a * nd + c] / scale;
+        A[a * m + nhist] = -1;
+        A[nhist * m + a] = -1;
+    }
+    b[nhist] = -1;
+    bool ok = true;
+    for (int c = 0; c < m && ok; c++) {
         int piv = c;
         for (int r = c + 1; r < m; r++)
-            if (std::fabs(A[r * m + c]) > std::fabs(A[piv * m + c])) piv = r;
-        if (std::fabs(A[piv * m + c]) < 1e-300) return false;
+            if (fabs(A[r * m + c]) > fabs(A[piv * m + c])) piv = r;
+        if (fabs(A[piv * m + c]) < 1e-300) {
+            ok = false;
+            break;
+        }
         if (piv != c) {
-            for (int k = 0; k < m; k++) std::swap(A[c * m + k], A[piv * m + k]);
-            std::swap(b[c], b[piv]);
+            for (int k = 0; k < m; k++) {
+                const double t = A[c * m + k];
+                A[c * m + k] = A[piv * m + k];
+                A[piv * m + k] = t;
+            }
+            const double t = b[c];
+            b[c] = b[piv];
+            b[piv] = t;
         }
         for (int r = c + 1; r < m; r++) {
-            double f = A[r * m + c] / A[c * m + c];
+            const double f = A[r * m + c] / A[c * m + c];
             for (int k = c; k < m; k++) A[r * m + k] -= f * A[c * m + k];
             b[r] -= f * b[c];
         }
     }
-    for (int c = m - 1; c >= 0; c--) {
-        double s = b[c];
-        for (int k = c + 1; k < m; k++) s -= A[c * m + k] * b[k];
-        b[c] = s / A[c * m + c];
-    }
-    return true;
+    if (ok)
+        for (int c = m - 1; c >= 0; c--) {
+            double sum = b[c];
+            for (int k = c + 1; k < m; k++) sum -= A[c * m + k] * b[k];
+            b[c] = sum / A[c * m + c];
+        }
+    for (int k = 0; k < nd; k++) cvec[k] = ok ? (k < nhist ? b[k] : 0.0) : (k == head ? 1.0 : 0.0);
 }
 
 ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dLam)
@@ -604,14 +643,16 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
 
     const bool diis = in.accel == HFGPU_SCF_DIIS;
     const int nd = std::max(2, std::min(in.diis_size, 20));
-    DBuf<double> Fh, Eh, Y, bvec;
+    DBuf<double> Fh, Eh, Y, bvec, cvec, Bd;
     if (diis) {
         Fh.alloc((size_t)nd * nn, st);
         Eh.alloc((size_t)nd * nn, st);
         Y.alloc(nn, st);
         bvec.alloc(nd, st);
+        cvec.alloc(nd, st);
+        Bd.alloc((size_t)nd * nd, st);
+        Bd.zero();
     }
-    std::vector<double> B((size_t)nd * nd, 0.0);
     int nhist = 0, head = 0;
 
     Purifier pur;
@@ -701,36 +742,16 @@ ScfOut run_scf(Context& ctx, const ScfIn& in, double* dC, double* dP, double* dL
             count_launch();
             HF_CUDA(cudaMemcpyAsync(Fh.p + (size_t)head * nn, F.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
             nhist = std::min(nhist + 1, nd);
-            // new row of B: <e_k, e_head>
+            // new row of B: <e_k, e_head>; the DIIS system is solved on the device
             HF_CUBLAS(cublasDgemv(ctx.blas, CUBLAS_OP_T, (int)nn, nd, &one, Eh.p, (int)nn, ek, 1, &zero, bvec.p, 1));
-            std::vector<double> row(nd);
-            bvec.download(row.data(), nd);
-            HF_CUDA(cudaStreamSynchronize(st));
+            diis_solve_kernel<<<1, 32, 0, st>>>(nd, nhist, head, Bd.p, bvec.p, cvec.p);
+            count_launch();
+            HF_CUDA(cudaGetLastError());
             ctx.trace_mark("diis error");
-            for (int k = 0; k < nhist; k++) {
-                B[(size_t)head * nd + k] = row[k];
-                B[(size_t)k * nd + head] = row[k];
-            }
             if (nhist >= 2) {
-                int m = nhist + 1;
-                std::vector<double> A((size_t)m * m, 0.0), rhs(m, 0.0);
-                double scale = 0;
-                for (int a = 0; a < nhist; a++) scale = std::max(scale, std::fabs(B[(size_t)a * nd + a]));
-                if (scale <= 0) scale = 1;
-                for (int a = 0; a < nhist; a++) {
-                    for (int b = 0; b < nhist; b++) A[(size_t)a * m + b] = B[(size_t)a * nd + b] / scale;
-                    A[(size_t)a * m + nhist] = -1;
-                    A[(size_t)nhist * m + a] = -1;
-                }
-                rhs[nhist] = -1;
-                if (solve_small(A, rhs, m)) {
-                    std::vector<double> c(nd, 0.0);
-                    for (int a = 0; a < nhist; a++) c[a] = rhs[a];
-                    bvec.upload(c.data(), nd);
-                    HF_CUBLAS(cublasDgemv(ctx.blas, CUBLAS_OP_N, (int)nn, nhist, &one, Fh.p, (int)nn, bvec.p, 1,
-                                          &zero, Y.p, 1));
-                    Fsolve = Y.p;
-                }
+                HF_CUBLAS(cublasDgemv(ctx.blas, CUBLAS_OP_N, (int)nn, nhist, &one, Fh.p, (int)nn, cvec.p, 1, &zero,
+                                      Y.p, 1));
+                Fsolve = Y.p;
             }
             head = (head + 1) % nd;
             ctx.trace_mark("diis extrap");
